@@ -1,0 +1,145 @@
+"""Flatten a ``ChemicalNetwork`` into what the code templates need.
+
+Orders follow the reference's generated code exactly:
+
+* species: ``sorted(required_species)`` (rates_and_rate_tables.C.template:323);
+* tables: reactions by name, then each cooling action by name with its
+  tables by name (rates_and_rate_tables.h.template:57-80,
+  rates_and_rate_tables.C.template:402-453).  Reactions whose name contains
+  ``pi`` and actions whose name contains ``ph`` are tabulated in redshift,
+  all others in log T;
+* Jacobian: column (variable) major, ``J[var*N + eq]``
+  (rates_and_rate_tables.C.template:578-594).
+"""
+
+from dataclasses import dataclass, field
+
+import sympy
+
+from .printers import ccode_device, ccode_ref
+
+
+@dataclass
+class SpeciesSpec:
+    index: int
+    name: str
+    weight: str          # literal as the reference's template prints it
+    free_electrons: str  # literal; "0.0" for ge/de
+    is_ge: bool
+    is_de: bool
+
+    @property
+    def counts_in_mdensity(self):
+        # rates_and_rate_tables.C.template:496-499
+        return self.name not in ("ge", "de", "us_e_0")
+
+
+@dataclass
+class TableSpec:
+    index: int
+    name: str            # C identifier used by the expressions, e.g. k01, ceHI_ceHI
+    kind: str            # "rate" or "cool"
+    zdep: bool           # tabulated in redshift instead of log T
+
+
+@dataclass
+class NetworkSpec:
+    name: str
+    species: list
+    tables: list
+    T_bounds: tuple      # literals
+    nT: int              # table length in T (nbins + 1)
+    z_bounds: tuple
+    nz: int
+    input_is_number: bool
+    mass_density_ref: str
+    mass_density_dev: str
+    T_ref: str
+    T_dev: str
+    Tge_ref: str
+    Tge_dev: str
+    rhs_ref: list        # per species, "rhs[j] = ...;"
+    rhs_dev: list        # per species, "f[k] = ...;"
+    jac_ref: list        # [var][eq] "Joutput[j] = ...;"
+    jac_dev: list        # [var][eq] device statement or None for a structural zero
+    jac_nonzero: list = field(default_factory=list)   # [var][eq] bool
+
+    @property
+    def N(self):
+        return len(self.species)
+
+    @property
+    def NT(self):
+        return len(self.tables)
+
+    @property
+    def ige(self):
+        return [s.index for s in self.species if s.is_ge][0]
+
+    @property
+    def ide(self):
+        d = [s.index for s in self.species if s.is_de]
+        return d[0] if d else -1
+
+    @property
+    def has_z_tables(self):
+        return any(t.zdep for t in self.tables)
+
+    def nnz(self):
+        return sum(sum(1 for v in col if v) for col in self.jac_nonzero)
+
+
+def _lit(v):
+    """The text Jinja prints for a Python number (``str``), as the reference's
+    templates do for weights, charges and bounds."""
+    return str(v)
+
+
+def network_spec(net, name):
+    species = []
+    for i, s in enumerate(sorted(net.required_species)):
+        species.append(SpeciesSpec(
+            index=i, name=s.name, weight=_lit(s.weight),
+            free_electrons=_lit(getattr(s, "free_electrons", 0.0)),
+            is_ge=(s.name == "ge"), is_de=(s.name in ("de", "us_e_0"))))
+    tables = []
+    for rname in sorted(net.reactions):
+        tables.append(TableSpec(len(tables), rname, "rate", "pi" in rname))
+    for cname in sorted(net.cooling_actions):
+        for tname in sorted(net.cooling_actions[cname].tables):
+            tables.append(TableSpec(len(tables), "%s_%s" % (cname, tname), "cool",
+                                    "ph" in cname))
+    ordered = sorted(net.required_species)
+    rhs_ref, rhs_dev = [], []
+    for i, s in enumerate(ordered):
+        e = net.rhs_expression(s)
+        rhs_ref.append(ccode_ref(e, assign_to=sympy.Symbol("rhs[j]")))
+        rhs_dev.append(ccode_device(e, assign_to=sympy.Symbol("f[%d]" % i)))
+    jac_ref, jac_dev, jac_nz = [], [], []
+    for v, s1 in enumerate(ordered):
+        cr, cd, cn = [], [], []
+        for q, s2 in enumerate(ordered):
+            e = net.jacobian_expression(s2, s1)
+            cr.append(ccode_ref(e, assign_to=sympy.Symbol("Joutput[j]")))
+            nz = not (e == 0)
+            cn.append(nz)
+            cd.append(ccode_device(e, assign_to=sympy.Symbol("jv")) if nz else None)
+        jac_ref.append(cr)
+        jac_dev.append(cd)
+        jac_nz.append(cn)
+    md = net.mass_density_expression()
+    T = net.temperature_expression(False)
+    Tg = net.temperature_expression(True)
+    z = getattr(net, "z", None)
+    return NetworkSpec(
+        name=name, species=species, tables=tables,
+        T_bounds=(_lit(net.T_bounds[0]), _lit(net.T_bounds[1])),
+        nT=len(net.T),
+        z_bounds=(_lit(net.z_bounds[0]), _lit(net.z_bounds[1])),
+        nz=(len(z) if z is not None else 0),
+        input_is_number=bool(getattr(net, "input_is_number", False)),
+        mass_density_ref=ccode_ref(md), mass_density_dev=ccode_device(md),
+        T_ref=ccode_ref(T), T_dev=ccode_device(T),
+        Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),
+        rhs_ref=rhs_ref, rhs_dev=rhs_dev,
+        jac_ref=jac_ref, jac_dev=jac_dev, jac_nonzero=jac_nz)

@@ -1,0 +1,714 @@
+/*
+ * Host side of the C ABI for one network (template parameter Net, generated
+ * per network): builds the device context from the rate tables and
+ * implements every entry point that include/dengo_gb300.h declares.  All
+ * arithmetic runs on the GPU; entry points that take host pointers copy to
+ * and from the device inside the call.
+ */
+#ifndef DG_API_CUH
+#define DG_API_CUH
+
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <initializer_list>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "dg_engine.cuh"
+#include "dg_strip.cuh"
+#include "dg_tablefile.h"
+
+namespace dg {
+
+inline char *last_error_buf()
+{
+    static thread_local char buf[512] = "";
+    return buf;
+}
+
+inline void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(last_error_buf(), 512, fmt, ap);
+    va_end(ap);
+    fprintf(stderr, "dengo_gb300: %s\n", last_error_buf());
+}
+
+#define DG_CUDA(call)                                                               \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::dg::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                            __FILE__, __LINE__);                                    \
+            return (int)e_;                                                         \
+        }                                                                           \
+    } while (0)
+
+/* Device context kept behind <n>_data::gpu. */
+struct Gpu {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    double2 *pairs = nullptr;            /* [nbins][NT] */
+    double *zv = nullptr, *dzv = nullptr;  /* [NT] redshift-table values, derivatives */
+    double *h_zv = nullptr;              /* pinned [2*NT] */
+    unsigned long long *queue = nullptr;
+    TableSet ts{};
+    double z_loaded = NAN;
+    char *d_buf = nullptr;
+    size_t d_cap = 0;
+};
+
+inline int ensure_device_buf(Gpu *g, size_t bytes)
+{
+    if (bytes <= g->d_cap) return 0;
+    if (g->d_buf) cudaFree(g->d_buf);
+    g->d_buf = nullptr;
+    g->d_cap = 0;
+    const size_t cap = bytes + bytes / 4 + 4096;
+    DG_CUDA(cudaMalloc(&g->d_buf, cap));
+    g->d_cap = cap;
+    return 0;
+}
+
+/* Carves 256-byte aligned sub-buffers out of one allocation. */
+struct Carve {
+    char *base;
+    size_t off = 0;
+    template <class T>
+    T *take(size_t n)
+    {
+        off = (off + 255) & ~(size_t)255;
+        T *p = (T *)(base + off);
+        off += n * sizeof(T);
+        return p;
+    }
+};
+
+inline size_t carve_size(std::initializer_list<size_t> bytes)
+{
+    size_t s = 0;
+    for (size_t b : bytes) s = ((s + 255) & ~(size_t)255) + b;
+    return s + 256;
+}
+
+template <class Net>
+struct Api {
+    using Data = typename Net::Data;
+    static constexpr int N = Net::N;
+    static constexpr int NT = Net::NT;
+
+    static Gpu *gpu(Data *d) { return (Gpu *)d->gpu; }
+
+    /* Values and z-derivatives of the redshift tables at z, computed on the
+     * host with the reference's expressions (C.template:388-401,413-422). */
+    static void z_values(const Data *d, double z, double *zv, double *dzv)
+    {
+        const bool in = (z >= d->z_bounds[0]) && (z < d->z_bounds[1]);
+        int zb = 0;
+        double zdef = 0, dz = 1;
+        if (in) {
+            const double lbz = log(d->z_bounds[0] + 1.0);
+            zb = (int)(d->id_zbin * (log(z + 1.0) - lbz));
+            if (zb <= 0) zb = 0;
+            else if (zb >= d->n_zbins) zb = d->n_zbins - 1;
+            const double z1 = (lbz + (zb) * d->d_zbin);
+            const double z2 = (lbz + (zb + 1) * d->d_zbin);
+            zdef = (log(z + 1.0) - z1) / (z2 - z1);
+            dz = (exp(z2) - exp(z1));
+        }
+        for (int k = 0; k < NT; k++) {
+            zv[k] = dzv[k] = 0.0;
+            if (!Net::zdep(k) || !in) continue;
+            const double *r = Net::host_table(const_cast<Data *>(d), k);
+            zv[k] = r[zb] + zdef * (r[zb + 1] - r[zb]);
+            dzv[k] = (r[zb + 1] - r[zb]);
+            dzv[k] /= dz;
+        }
+    }
+
+    static int load_z(Data *d, double z, cudaStream_t st)
+    {
+        Gpu *g = gpu(d);
+        if (!Net::HAS_Z) return 0;
+        if (g->z_loaded == z) return 0;
+        DG_CUDA(cudaStreamSynchronize(st));
+        z_values(d, z, g->h_zv, g->h_zv + NT);
+        DG_CUDA(cudaMemcpyAsync(g->zv, g->h_zv, sizeof(double) * NT, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(g->dzv, g->h_zv + NT, sizeof(double) * NT,
+                                cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        g->z_loaded = z;
+        return 0;
+    }
+
+    static int init_gpu(Data *d)
+    {
+        Gpu *g = new Gpu();
+        d->gpu = g;
+        DG_CUDA(cudaGetDevice(&g->device));
+        DG_CUDA(cudaDeviceGetAttribute(&g->nsm, cudaDevAttrMultiProcessorCount, g->device));
+        DG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        const int nbins = d->nbins;
+        std::vector<double2> pairs((size_t)nbins * NT);
+        for (int k = 0; k < NT; k++) {
+            if (Net::zdep(k)) continue;
+            const double *r = Net::host_table(d, k);
+            for (int b = 0; b < nbins; b++)
+                pairs[(size_t)b * NT + k] = make_double2(r[b], r[b + 1] - r[b]);
+        }
+        DG_CUDA(cudaMalloc(&g->pairs, sizeof(double2) * pairs.size()));
+        DG_CUDA(cudaMemcpy(g->pairs, pairs.data(), sizeof(double2) * pairs.size(),
+                           cudaMemcpyHostToDevice));
+        DG_CUDA(cudaMalloc(&g->zv, sizeof(double) * 2 * NT));
+        g->dzv = g->zv + NT;
+        DG_CUDA(cudaMemset(g->zv, 0, sizeof(double) * 2 * NT));
+        DG_CUDA(cudaMallocHost(&g->h_zv, sizeof(double) * 2 * NT));
+        DG_CUDA(cudaMalloc(&g->queue, sizeof(unsigned long long)));
+        g->ts.pairs = g->pairs;
+        g->ts.zvals = g->zv;
+        g->ts.nbins = nbins;
+        g->ts.lb = log(d->bounds[0]);
+        g->ts.dbin = d->dbin;
+        g->ts.idbin = d->idbin;
+        g->ts.Tlo = d->bounds[0];
+        g->ts.Thi = d->bounds[1];
+        g->ts.z = -1.0;
+        return 0;
+    }
+
+    static Data *setup_from_tables(const double *const *tables, int ntables)
+    {
+        if (ntables != NT) {
+            set_error("%s: expected %d tables, got %d", Net::NAME, NT, ntables);
+            return nullptr;
+        }
+        Data *d = (Data *)calloc(1, sizeof(Data));
+        Net::setup_bins(d);
+        for (int k = 0; k < NT; k++)
+            memcpy(Net::host_table(d, k), tables[k],
+                   sizeof(double) * (Net::zdep(k) ? Net::NZ_LEN : Net::NT_LEN));
+        if (init_gpu(d) != 0) {
+            free_data(d);
+            return nullptr;
+        }
+        return d;
+    }
+
+    /* <n>_setup_data: reads <n>_tables.dgt from $DENGO_TABLE_DIR, the
+     * current directory, or the directory holding this library, in that
+     * order (the reference reads <n>_tables.h5 from the current directory,
+     * C.template:278-304). */
+    static Data *setup_from_file(int *NumberOfFields, char ***FieldNames)
+    {
+        std::string fname = std::string(Net::NAME) + "_tables.dgt";
+        std::vector<std::string> cands;
+        if (const char *dir = getenv("DENGO_TABLE_DIR")) cands.push_back(std::string(dir) + "/" + fname);
+        cands.push_back(fname);
+        Dl_info info;
+        if (dladdr((void *)&setup_from_file, &info) && info.dli_fname) {
+            std::string lib(info.dli_fname);
+            size_t slash = lib.rfind('/');
+            if (slash != std::string::npos) cands.push_back(lib.substr(0, slash + 1) + fname);
+        }
+        std::map<std::string, std::vector<double>> tabs;
+        std::string err, tried;
+        bool ok = false;
+        for (auto &c : cands) {
+            FILE *f = fopen(c.c_str(), "rb");
+            if (!f) {
+                tried += " " + c;
+                continue;
+            }
+            fclose(f);
+            ok = read_table_file(c.c_str(), tabs, err);
+            break;
+        }
+        if (!ok) {
+            set_error("%s_setup_data: %s", Net::NAME,
+                      err.empty() ? ("no table bundle found; tried" + tried).c_str() : err.c_str());
+            return nullptr;
+        }
+        std::vector<const double *> ptrs(NT);
+        for (int k = 0; k < NT; k++) {
+            auto it = tabs.find(Net::table_name(k));
+            const size_t want = Net::zdep(k) ? Net::NZ_LEN : Net::NT_LEN;
+            if (it == tabs.end() || it->second.size() != want) {
+                set_error("%s_setup_data: table %s missing or not %zu long", Net::NAME,
+                          Net::table_name(k), want);
+                return nullptr;
+            }
+            ptrs[k] = it->second.data();
+        }
+        Data *d = setup_from_tables(ptrs.data(), NT);
+        if (d && FieldNames != nullptr && NumberOfFields != nullptr) {
+            NumberOfFields[0] = N;
+            FieldNames[0] = new char *[N];
+            for (int i = 0; i < N; i++) FieldNames[0][i] = strdup(Net::species_name(i));
+        }
+        return d;
+    }
+
+    static void free_data(Data *d)
+    {
+        if (!d) return;
+        Gpu *g = gpu(d);
+        if (g) {
+            if (g->stream) cudaStreamSynchronize(g->stream);
+            cudaFree(g->pairs);
+            cudaFree(g->zv);
+            cudaFreeHost(g->h_zv);
+            cudaFree(g->queue);
+            cudaFree(g->d_buf);
+            if (g->stream) cudaStreamDestroy(g->stream);
+            delete g;
+        }
+        free(d);
+    }
+
+    /* ---------------- the solver ---------------- */
+    template <int BLOCK>
+    static int launch(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
+                      cudaStream_t st)
+    {
+        auto kern = evolve_fp64_kernel<Net, BLOCK>;
+        const size_t smem = Lane<Net, BLOCK>::smem_bytes();
+        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (io.ncells <= 0) return 0;
+        const long long need = (io.ncells + BLOCK - 1) / BLOCK;
+        unsigned long long *queue = nullptr;
+        if (schedule == DENGO_SCHED_PER_THREAD) {
+            grid = (int)need;
+        } else {
+            int per_sm = 0;
+            DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
+            if (per_sm < 1) per_sm = 1;
+            const long long full = (long long)g->nsm * per_sm;
+            if (grid <= 0) grid = (int)(need < full ? need : full);
+            if (schedule != DENGO_SCHED_STRIDE) {
+                queue = g->queue;
+                DG_CUDA(cudaMemsetAsync(queue, 0, sizeof(*queue), st));
+            }
+        }
+        kern<<<grid, BLOCK, smem, st>>>(io, g->ts, kc, queue);
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
+
+    static int solve_device(Data *d, const dengo_cell_batch *b, double z,
+                            const dengo_solver_config *cfg_in, void *stream)
+    {
+        if (!d || !b) {
+            set_error("%s_solve_cells_device: null argument", Net::NAME);
+            return -1;
+        }
+        dengo_solver_config cfg;
+        if (cfg_in) cfg = *cfg_in;
+        else dengo_default_config(&cfg);
+        if (cfg.precision != DENGO_FP64) {
+            set_error("%s_solve_cells_device: precision %d not built", Net::NAME, cfg.precision);
+            return -1;
+        }
+        Gpu *g = gpu(d);
+        cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+        if (load_z(d, z, st) != 0) return -1;
+        CellIO io{};
+        io.state = b->state;
+        io.atol = b->atol;
+        io.rtol = b->rtol;
+        io.rtol_scalar = b->rtol_scalar;
+        io.dtf = b->dtf;
+        io.dtf_scalar = b->dtf_scalar;
+        io.dt = b->dt;
+        io.ttot = b->ttot;
+        io.status = b->status;
+        io.substeps = b->substeps;
+        io.sweeps = b->sweeps;
+        io.failures = b->failures;
+        io.cs = b->cell_stride;
+        io.ss = b->species_stride;
+        io.ncells = b->ncells;
+        KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
+        g->ts.z = z;
+        switch (cfg.block) {
+        case 32: return launch<32>(g, io, kc, cfg.schedule, cfg.grid, st);
+        case 128: return launch<128>(g, io, kc, cfg.schedule, cfg.grid, st);
+        default: return launch<64>(g, io, kc, cfg.schedule, cfg.grid, st);
+        }
+    }
+
+    /* <n>_solve_cells_host: the batch's pointers are host pointers.  The
+     * arrays are copied to the device, solved, and copied back before the
+     * call returns. */
+    static int solve_host(Data *d, const dengo_cell_batch *hb, double z,
+                          const dengo_solver_config *cfg)
+    {
+        if (!d || !hb) {
+            set_error("%s_solve_cells_host: null argument", Net::NAME);
+            return -1;
+        }
+        const long long n = hb->ncells;
+        if (n <= 0) return 0;
+        const size_t ext = (size_t)((n - 1) * hb->cell_stride + (N - 1) * hb->species_stride + 1);
+        const size_t cn = (size_t)n;
+        if (ensure_device_buf(gpu(d), carve_size({ext * 8, ext * 8, ext * 8, cn * 8, cn * 8,
+                                                  cn * 8, cn * 4, cn * 4, cn * 4, cn * 4})) != 0)
+            return -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        Carve cv{g->d_buf};
+        dengo_cell_batch b = *hb;
+        b.state = cv.take<double>(ext);
+        b.atol = cv.take<double>(ext);
+        double *rt = cv.take<double>(ext);
+        double *dtf = cv.take<double>(cn), *dt = cv.take<double>(cn), *tt = cv.take<double>(cn);
+        int *sta = cv.take<int>(cn), *sub = cv.take<int>(cn), *swp = cv.take<int>(cn),
+            *fai = cv.take<int>(cn);
+        b.rtol = hb->rtol ? rt : nullptr;
+        b.dtf = hb->dtf ? dtf : nullptr;
+        b.dt = hb->dt ? dt : nullptr;
+        b.ttot = hb->ttot ? tt : nullptr;
+        b.status = hb->status ? sta : nullptr;
+        b.substeps = hb->substeps ? sub : nullptr;
+        b.sweeps = hb->sweeps ? swp : nullptr;
+        b.failures = hb->failures ? fai : nullptr;
+        auto h2d = [&](void *dst, const void *src, size_t bytes) {
+            return src ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
+        };
+        auto d2h = [&](void *dst, const void *src, size_t bytes) {
+            return dst ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+        };
+        DG_CUDA(h2d(b.state, hb->state, ext * 8));
+        DG_CUDA(h2d(b.atol, hb->atol, ext * 8));
+        DG_CUDA(h2d(rt, hb->rtol, ext * 8));
+        DG_CUDA(h2d(dtf, hb->dtf, cn * 8));
+        DG_CUDA(h2d(dt, hb->dt, cn * 8));
+        if (solve_device(d, &b, z, cfg, st) != 0) return -1;
+        DG_CUDA(d2h(hb->state, b.state, ext * 8));
+        DG_CUDA(d2h(hb->atol, b.atol, ext * 8));
+        DG_CUDA(d2h(hb->dt, dt, cn * 8));
+        DG_CUDA(d2h(hb->ttot, tt, cn * 8));
+        DG_CUDA(d2h(hb->status, sta, cn * 4));
+        DG_CUDA(d2h(hb->substeps, sub, cn * 4));
+        DG_CUDA(d2h(hb->sweeps, swp, cn * 4));
+        DG_CUDA(d2h(hb->failures, fai, cn * 4));
+        DG_CUDA(cudaStreamSynchronize(st));
+        return 0;
+    }
+
+    /* dengo_evolve_<n> with per-cell dt control (each cell behaves as the
+     * reference called with dims = 1).  Every cell starts from *dt (< 0:
+     * dtf/1e5).  On return *dt is the smallest final step over the cells and
+     * the result is the smallest ttot, so ttot < dtf flags a cell that
+     * stopped early, as in the reference. */
+    static double evolve(double dtf, double *dt, double z, double *input, double *rtol,
+                         double *atol, long long dims, Data *d)
+    {
+        if (dims <= 0) return 0.0;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        const size_t n = (size_t)dims * N;
+        if (ensure_device_buf(g, carve_size({n * 8, n * 8, n * 8, (size_t)dims * 8,
+                                             (size_t)dims * 8})) != 0)
+            return -1.0;
+        Carve cv{g->d_buf};
+        double *d_in = cv.take<double>(n), *d_at = cv.take<double>(n), *d_rt = cv.take<double>(n);
+        double *d_dt = cv.take<double>(dims), *d_tt = cv.take<double>(dims);
+        std::vector<double> hdt(dims, *dt), htt(dims);
+        cudaError_t e;
+#define DG_EV(call)                                                              \
+    if ((e = (call)) != cudaSuccess) {                                           \
+        set_error("dengo_evolve_%s: %s: %s", Net::NAME, #call, cudaGetErrorString(e)); \
+        return -1.0;                                                             \
+    }
+        DG_EV(cudaMemcpyAsync(d_in, input, n * 8, cudaMemcpyHostToDevice, st));
+        DG_EV(cudaMemcpyAsync(d_at, atol, n * 8, cudaMemcpyHostToDevice, st));
+        DG_EV(cudaMemcpyAsync(d_rt, rtol, n * 8, cudaMemcpyHostToDevice, st));
+        DG_EV(cudaMemcpyAsync(d_dt, hdt.data(), dims * 8, cudaMemcpyHostToDevice, st));
+        dengo_cell_batch b{};
+        b.ncells = dims;
+        b.cell_stride = N;
+        b.species_stride = 1;
+        b.state = d_in;
+        b.atol = d_at;
+        b.rtol = d_rt;
+        b.dtf_scalar = dtf;
+        b.dt = d_dt;
+        b.ttot = d_tt;
+        dengo_solver_config cfg;
+        dengo_default_config(&cfg);
+        if (solve_device(d, &b, z, &cfg, st) != 0) return -1.0;
+        DG_EV(cudaMemcpyAsync(input, d_in, n * 8, cudaMemcpyDeviceToHost, st));
+        DG_EV(cudaMemcpyAsync(atol, d_at, n * 8, cudaMemcpyDeviceToHost, st));
+        DG_EV(cudaMemcpyAsync(hdt.data(), d_dt, dims * 8, cudaMemcpyDeviceToHost, st));
+        DG_EV(cudaMemcpyAsync(htt.data(), d_tt, dims * 8, cudaMemcpyDeviceToHost, st));
+        DG_EV(cudaStreamSynchronize(st));
+#undef DG_EV
+        double tmin = htt[0], dmin = hdt[0];
+        for (long long c = 1; c < dims; c++) {
+            if (htt[c] < tmin) tmin = htt[c];
+            if (hdt[c] < dmin) dmin = hdt[c];
+        }
+        *dt = dmin;
+        return tmin;
+    }
+
+    /* ---------------- strip-wise entry points ---------------- */
+    struct StripDev {
+        double *in, *out;
+        StripBufs b;
+    };
+
+    static int strip_alloc(Data *d, int nstrip, int nchem, size_t out_per_cell, StripDev &s)
+    {
+        if (nstrip < 0 || nstrip > DENGO_MAX_NCELLS) {
+            set_error("%s: nstrip %d outside [0, %d]", Net::NAME, nstrip, DENGO_MAX_NCELLS);
+            return -1;
+        }
+        if (nchem != N) {
+            set_error("%s: nchem %d != %d", Net::NAME, nchem, N);
+            return -1;
+        }
+        Gpu *g = gpu(d);
+        const size_t ns = DENGO_MAX_NCELLS;
+        if (ensure_device_buf(g, carve_size({ns * N * 8, ns * out_per_cell * 8, 6 * ns * 8,
+                                             2 * NT * ns * 8, 2 * ns * 4})) != 0)
+            return -1;
+        Carve cv{g->d_buf};
+        s.in = cv.take<double>(ns * N);
+        s.out = cv.take<double>(ns * out_per_cell);
+        s.b.Ts = cv.take<double>(ns);
+        s.b.logTs = cv.take<double>(ns);
+        s.b.invTs = cv.take<double>(ns);
+        s.b.dTs_ge = cv.take<double>(ns);
+        s.b.Tdef = cv.take<double>(ns);
+        s.b.dT = cv.take<double>(ns);
+        s.b.rs = cv.take<double>(NT * ns);
+        s.b.drs = cv.take<double>(NT * ns);
+        s.b.bin_id = cv.take<int>(ns);
+        s.b.flag = cv.take<int>(ns);
+        s.b.ld = ns;
+        return 0;
+    }
+
+    static int blocks(int n) { return (n + 127) / 128; }
+
+    static int temperature(Data *d, double *input, int nstrip, int nchem)
+    {
+        StripDev s;
+        if (strip_alloc(d, nstrip, nchem, 0, s) != 0 || nstrip == 0) return nstrip == 0 ? 0 : -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        DG_CUDA(cudaMemcpyAsync(s.in, input, (size_t)nstrip * N * 8, cudaMemcpyHostToDevice, st));
+        strip_temperature_kernel<Net><<<blocks(nstrip), 128, 0, st>>>(s.in, nstrip, N, g->ts, s.b);
+        DG_CUDA(cudaGetLastError());
+        DG_CUDA(cudaMemcpyAsync(d->Ts, s.b.Ts, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(d->logTs, s.b.logTs, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(d->invTs, s.b.invTs, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(Net::host_dTs_ge(d), s.b.dTs_ge, nstrip * 8,
+                                cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        return 0;
+    }
+
+    /* Uses data->logTs / invTs / current_z, as the reference does. */
+    static int interpolate(Data *d, int nstrip)
+    {
+        StripDev s;
+        if (strip_alloc(d, nstrip, N, 0, s) != 0 || nstrip == 0) return nstrip == 0 ? 0 : -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        if (load_z(d, d->current_z, st) != 0) return -1;
+        DG_CUDA(cudaMemcpyAsync(s.b.logTs, d->logTs, nstrip * 8, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(s.b.invTs, d->invTs, nstrip * 8, cudaMemcpyHostToDevice, st));
+        strip_interpolate_kernel<Net><<<blocks(nstrip), 128, 0, st>>>(nstrip, g->ts, s.b, g->zv,
+                                                                     g->dzv);
+        DG_CUDA(cudaGetLastError());
+        std::vector<int> bins(nstrip);
+        DG_CUDA(cudaMemcpyAsync(bins.data(), s.b.bin_id, nstrip * 4, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(d->Tdef, s.b.Tdef, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(d->dT, s.b.dT, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        for (int k = 0; k < NT; k++) {
+            DG_CUDA(cudaMemcpyAsync(Net::host_rs(d, k), s.b.rs + k * s.b.ld, nstrip * 8,
+                                    cudaMemcpyDeviceToHost, st));
+            DG_CUDA(cudaMemcpyAsync(Net::host_drs(d, k), s.b.drs + k * s.b.ld, nstrip * 8,
+                                    cudaMemcpyDeviceToHost, st));
+        }
+        DG_CUDA(cudaStreamSynchronize(st));
+        for (int c = 0; c < nstrip; c++) d->bin_id[c] = bins[c];
+        return 0;
+    }
+
+    /* calculate_rhs_<n>: temperature, rates, then per cell the RHS; returns
+     * 1 at the first cell holding a negative value, leaving that cell's and
+     * later cells' outputs untouched (C.template:489-521). */
+    static int rhs(double *input, double *out, int nstrip, int nchem, void *sdata)
+    {
+        Data *d = (Data *)sdata;
+        if (temperature(d, input, nstrip, nchem) != 0) return -1;
+        if (interpolate(d, nstrip) != 0) return -1;
+        StripDev s;
+        if (nstrip == 0) return 0;
+        if (strip_alloc(d, nstrip, nchem, N, s) != 0) return -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        DG_CUDA(cudaMemcpyAsync(s.b.Ts, d->Ts, nstrip * 8, cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < NT; k++)
+            DG_CUDA(cudaMemcpyAsync(s.b.rs + k * s.b.ld, Net::host_rs(d, k), nstrip * 8,
+                                    cudaMemcpyHostToDevice, st));
+        strip_rhs_kernel<Net><<<blocks(nstrip), 128, 0, st>>>(s.in, s.out, nstrip, N,
+                                                             d->current_z, s.b);
+        DG_CUDA(cudaGetLastError());
+        std::vector<int> flag(nstrip);
+        std::vector<double> h((size_t)nstrip * N);
+        DG_CUDA(cudaMemcpyAsync(flag.data(), s.b.flag, nstrip * 4, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(h.data(), s.out, (size_t)nstrip * N * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        int first = nstrip;
+        for (int c = 0; c < nstrip; c++)
+            if (flag[c]) {
+                first = c;
+                break;
+            }
+        memcpy(out, h.data(), (size_t)first * N * 8);
+        return first < nstrip ? 1 : 0;
+    }
+
+    /* calculate_jacobian_<n>: uses the rates and dT/dge held in data (set by
+     * the preceding RHS or interpolation call), as the reference does. */
+    static int jacobian(double *input, double *J, int nstrip, int nchem, void *sdata)
+    {
+        Data *d = (Data *)sdata;
+        StripDev s;
+        if (nstrip == 0) return 0;
+        if (strip_alloc(d, nstrip, nchem, N * N, s) != 0) return -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        DG_CUDA(cudaMemcpyAsync(s.in, input, (size_t)nstrip * N * 8, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(s.b.Ts, d->Ts, nstrip * 8, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(s.b.dTs_ge, Net::host_dTs_ge(d), nstrip * 8,
+                                cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < NT; k++)
+            DG_CUDA(cudaMemcpyAsync(s.b.rs + k * s.b.ld, Net::host_rs(d, k), nstrip * 8,
+                                    cudaMemcpyHostToDevice, st));
+        strip_jacobian_kernel<Net><<<blocks(nstrip), 128, 0, st>>>(s.in, s.out, nstrip, N,
+                                                                  d->current_z, s.b);
+        DG_CUDA(cudaGetLastError());
+        std::vector<int> flag(nstrip);
+        std::vector<double> h((size_t)nstrip * N * N);
+        DG_CUDA(cudaMemcpyAsync(flag.data(), s.b.flag, nstrip * 4, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(h.data(), s.out, h.size() * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        int first = nstrip;
+        for (int c = 0; c < nstrip; c++)
+            if (flag[c]) {
+                first = c;
+                fprintf(stderr, "JNegative[%d]\n", c);
+                break;
+            }
+        memcpy(J, h.data(), (size_t)first * N * N * 8);
+        return first < nstrip ? 1 : 0;
+    }
+
+    /* BE_chem_solve with this network's RHS and Jacobian: one Newton solve of
+     * a strip in lockstep (BE_chem_solve.C:79-241).  u, atol are updated as
+     * the reference updates them and data->Ts holds the last temperatures;
+     * the caller's scratch arrays u0, s, gu, Ju are not written. */
+    static int be_chem_solve(double *u, double dt, double *rtol, double *atol, int nstrip,
+                             int nchem, double *scaling, Data *d, double *, double *, double *,
+                             double *)
+    {
+        if (!d) {
+            set_error("BE_chem_solve: sdata is null");
+            return -1;
+        }
+        StripDev s;
+        if (nstrip == 0) return 0;
+        if (strip_alloc(d, nstrip, nchem, 3 * N, s) != 0) return -1;
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        if (load_z(d, d->current_z, st) != 0) return -1;
+        const size_t bytes = (size_t)nstrip * N * 8;
+        double *du = s.in, *drt = s.out, *dat = s.out + (size_t)nstrip * N,
+               *dsc = s.out + 2 * (size_t)nstrip * N;
+        DG_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(drt, rtol, bytes, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(dat, atol, bytes, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(dsc, scaling, bytes, cudaMemcpyHostToDevice, st));
+        TableSet ts = g->ts;
+        ts.z = d->current_z;
+        const int threads = ((nstrip + 31) / 32) * 32;
+        be_strip_kernel<Net><<<1, threads, 0, st>>>(du, dt, drt, dat, nstrip, dsc, ts,
+                                                    10, s.b.flag, s.b.Ts);
+        DG_CUDA(cudaGetLastError());
+        int ret = 1;
+        DG_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(atol, dat, bytes, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(d->Ts, s.b.Ts, nstrip * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(&ret, s.b.flag, 4, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        return ret;
+    }
+
+    /* Needs no data struct: uses a context-free temporary stream. */
+    static int electrons(double *input, int nstrip, int nchem)
+    {
+        if (nstrip <= 0) return 0;
+        if (nchem != N) {
+            set_error("%s: nchem %d != %d", Net::NAME, nchem, N);
+            return -1;
+        }
+        double *dbuf = nullptr;
+        const size_t bytes = (size_t)nstrip * N * 8;
+        DG_CUDA(cudaMalloc(&dbuf, bytes));
+        DG_CUDA(cudaMemcpy(dbuf, input, bytes, cudaMemcpyHostToDevice));
+        strip_electrons_kernel<Net><<<1, 1>>>(dbuf, nstrip, N);
+        DG_CUDA(cudaGetLastError());
+        DG_CUDA(cudaMemcpy(input, dbuf, bytes, cudaMemcpyDeviceToHost));
+        DG_CUDA(cudaFree(dbuf));
+        return 0;
+    }
+
+    static int temperature_from_mass_density(double *input, int nstrip, int nchem, double *T)
+    {
+        if (nstrip <= 0) return 0;
+        if (nchem != N) {
+            set_error("%s: nchem %d != %d", Net::NAME, nchem, N);
+            return -1;
+        }
+        double *dbuf = nullptr;
+        const size_t bytes = (size_t)nstrip * N * 8;
+        DG_CUDA(cudaMalloc(&dbuf, bytes + (size_t)nstrip * 8));
+        DG_CUDA(cudaMemcpy(dbuf, input, bytes, cudaMemcpyHostToDevice));
+        double *dT = dbuf + (size_t)nstrip * N;
+        strip_temperature_from_mass_kernel<Net><<<blocks(nstrip), 128>>>(dbuf, nstrip, N, dT);
+        DG_CUDA(cudaGetLastError());
+        DG_CUDA(cudaMemcpy(T, dT, (size_t)nstrip * 8, cudaMemcpyDeviceToHost));
+        DG_CUDA(cudaFree(dbuf));
+        return 0;
+    }
+};
+
+}  // namespace dg
+
+extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg)
+{
+    cfg->max_newton_sweeps = 10;
+    cfg->max_substeps = 50000;
+    cfg->dt_ratio_floor = 1e-15;
+    cfg->floor_value = 1e-25;
+    cfg->precision = DENGO_FP64;
+    cfg->schedule = DENGO_SCHED_AUTO;
+    cfg->block = 0;
+    cfg->grid = 0;
+}
+
+#endif

@@ -1,0 +1,402 @@
+/*
+ * The GB300 backward-Euler Newton engine: one cell per lane, the whole
+ * per-cell solve (temperature, table interpolation, RHS, Jacobian, scaled
+ * I - dt J, partial-pivot LU, Newton update and convergence vote, substep
+ * accept/reject and dt control) fused into one kernel pass.
+ *
+ * Semantics are those of the reference's generated driver called with one
+ * cell per strip (dims = 1), i.e. per-cell dt control:
+ *   BE_chem_solve / BE_Resid_Fun / BE_Resid_Jac / Gauss_Elim
+ *       dengo/solvers/BE_chem_solve.C:79-382
+ *   dengo_evolve_<name>
+ *       dengo/templates/rates_and_rate_tables.C.template:149-274
+ * including the in-place atol round trips, the fixed scaling vector, the
+ * floor at 1e-25 after an accepted substep (prev keeps the unfloored state),
+ * the 50000-substep cap (the last solved state is returned unaccepted) and
+ * the dt/dtf < 1e-15 stop.  The FP64 build performs the reference's IEEE
+ * operations in the reference's order (no FMA contraction); dg_log /
+ * dg_ipow stand in for glibc's log / pow.
+ *
+ * Lanes are refilled: when a lane's cell finishes it takes the next cell
+ * (static stride or an atomic work queue) while the other lanes of its warp
+ * continue, so a warp's lanes stay busy on a mix of stiff and easy cells.
+ */
+#ifndef DG_ENGINE_CUH
+#define DG_ENGINE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dg_math.h"
+#include "dengo_gb300.h"
+
+namespace dg {
+
+enum : int { ST_OK = 0, ST_MAX_SUBSTEPS = 1, ST_DT_UNDERFLOW = 2 };
+
+/* Rate/cooling tables on the device, bin-major: for bin b and table k the
+ * pair (r_k[b], r_k[b+1] - r_k[b]).  The difference is the reference's own
+ * subtraction (rates_and_rate_tables.C.template:406-408) done once. */
+struct TableSet {
+    const double2 *pairs;   /* [nbins][NT] */
+    const double *zvals;    /* [NT] values of the redshift tables at this call's z */
+    int nbins;              /* table length - 1 */
+    double lb, dbin, idbin; /* log(T_lo), bin width, 1/width (host-computed) */
+    double Tlo, Thi;
+    double z;               /* redshift of this call (only compton-like terms read it) */
+};
+
+/* Cell arrays: element (cell c, species s) at p[c*cs + s*ss]. */
+struct CellIO {
+    double *state;
+    double *atol;
+    const double *rtol;
+    double rtol_scalar;
+    const double *dtf;
+    double dtf_scalar;
+    double *dt;
+    double *ttot;
+    int *status;
+    int *substeps, *sweeps, *failures;
+    long long cs, ss;
+    long long ncells;
+};
+
+struct KernelCfg {
+    int max_sweeps;
+    int max_substeps;
+    double dt_ratio_floor;
+    double floor_value;
+};
+
+/* One double per thread in a [slots][BLOCK] shared-memory array: thread
+ * tid's slot i is p[i * BLOCK], so a warp's accesses are conflict-free. */
+template <int BLOCK>
+struct Slots {
+    double *p;
+    __device__ __forceinline__ double &operator[](int i) const { return p[i * BLOCK]; }
+};
+
+template <class Net, int BLOCK>
+struct Lane {
+    static constexpr int N = Net::N;
+    static constexpr int NT = Net::NT;
+    /* shared-memory slot map */
+    static constexpr int OFF_J = 0;
+    static constexpr int OFF_R = OFF_J + N * N;
+    static constexpr int OFF_PREV = OFF_R + NT;
+    static constexpr int OFF_SC = OFF_PREV + N;
+    static constexpr int OFF_INV = OFF_SC + N;
+    static constexpr int OFF_AT = OFF_INV + N;
+    static constexpr int OFF_RT = OFF_AT + N;
+    static constexpr int SLOTS = OFF_RT + N;
+    static constexpr size_t smem_bytes() { return sizeof(double) * SLOTS * BLOCK; }
+};
+
+/* Linear interpolation in log T (rates_and_rate_tables.C.template:372-411),
+ * values only: the solver never reads the T-derivatives. */
+template <class Net, int BLOCK>
+__device__ __forceinline__ void interpolate(const TableSet &ts, double logT, Slots<BLOCK> R)
+{
+    const int bin = (int)(ts.idbin * (logT - ts.lb));
+    const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+    const double t1 = (ts.lb + (bin) * ts.dbin);
+    const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+    const double Tdef = (logT - t1) / (t2 - t1);
+    const double2 *row = ts.pairs + (size_t)bc * Net::NT;
+#pragma unroll
+    for (int k = 0; k < Net::NT; k++) {
+        if (Net::zdep(k)) {
+            R[k] = ts.zvals[k];
+        } else {
+            const double2 pr = __ldg(row + k);
+            R[k] = pr.x + Tdef * pr.y;
+        }
+    }
+}
+
+/* Gauss_Elim (BE_chem_solve.C:330-382) on the scaled Jacobian held in
+ * shared memory, column-major A(i,j) = J[j*N + i]; x holds b on entry and
+ * the solution on exit. */
+template <int N, int BLOCK>
+__device__ __forceinline__ void gauss_elim(Slots<BLOCK> J, double (&x)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N - 1; k++) {
+        int p = k;
+        double best = fabs(J[k * N + k]);
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            const double a = fabs(J[k * N + i]);
+            if (a > best) {
+                best = a;
+                p = i;
+            }
+        }
+        if (p != k) {
+            for (int j = k; j < N; j++) {
+                const double t = J[j * N + k];
+                J[j * N + k] = J[j * N + p];
+                J[j * N + p] = t;
+            }
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                if (i == p) {
+                    const double t = x[k];
+                    x[k] = x[i];
+                    x[i] = t;
+                }
+            }
+        }
+        const double piv = J[k * N + k];
+#pragma unroll
+        for (int i = k + 1; i < N; i++) J[k * N + i] = J[k * N + i] / piv;
+#pragma unroll
+        for (int j = k + 1; j < N; j++) {
+            const double akj = J[j * N + k];
+#pragma unroll
+            for (int i = k + 1; i < N; i++) J[j * N + i] = J[j * N + i] - J[k * N + i] * akj;
+        }
+        const double xk = x[k];
+#pragma unroll
+        for (int i = k + 1; i < N; i++) x[i] = x[i] - J[k * N + i] * xk;
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
+        double xi = x[i];
+#pragma unroll
+        for (int j = i + 1; j < N; j++) xi = xi - J[j * N + i] * x[j];
+        x[i] = xi / J[i * N + i];
+    }
+}
+
+/* Stores one Jacobian entry already transformed as BE_Resid_Jac does:
+ * row scale 1/scale_eq, column scale scale_var, then -dt*J, +1 on the
+ * diagonal (BE_chem_solve.C:301-318). */
+template <int N, int BLOCK>
+struct JacPut {
+    Slots<BLOCK> J, INV, SC;
+    double mdt;
+    __device__ __forceinline__ void operator()(int q, int v, double jv) const
+    {
+        double a = jv * INV[q];
+        a = a * SC[v];
+        a = mdt * a;
+        if (q == v) a = a + 1.0;
+        J[v * N + q] = a;
+    }
+};
+
+/* Number-density conversion and electron consistency at the start of a
+ * cell (rates_and_rate_tables.C.template:158-170). */
+template <class Net>
+__device__ __forceinline__ void to_number_density(double (&y)[Net::N], double (&at)[Net::N])
+{
+    if (!Net::INPUT_IS_NUMBER) {
+#pragma unroll
+        for (int s = 0; s < Net::N; s++) {
+            if (s == Net::IGE) continue;
+            y[s] = y[s] / Net::unit(s);
+            at[s] = at[s] / Net::unit(s);
+        }
+    }
+}
+
+template <class Net, int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
+evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
+{
+    using L = Lane<Net, BLOCK>;
+    constexpr int N = Net::N;
+    extern __shared__ double dg_smem[];
+    const int tid = threadIdx.x;
+    double *base = dg_smem + tid;
+    const Slots<BLOCK> J{base + L::OFF_J * BLOCK};
+    const Slots<BLOCK> R{base + L::OFF_R * BLOCK};
+    const Slots<BLOCK> PREV{base + L::OFF_PREV * BLOCK};
+    const Slots<BLOCK> SC{base + L::OFF_SC * BLOCK};
+    const Slots<BLOCK> INV{base + L::OFF_INV * BLOCK};
+    const Slots<BLOCK> AT{base + L::OFF_AT * BLOCK};
+    const Slots<BLOCK> RT{base + L::OFF_RT * BLOCK};
+
+    const long long stride = (long long)gridDim.x * BLOCK;
+    long long cell = queue ? (long long)atomicAdd(queue, 1ull)
+                           : (long long)blockIdx.x * BLOCK + tid;
+
+    double u[N], u0[N], y[N];
+    double dtf = 0, dt = 0, ttot = 0;
+    int siter = 0, isweep = 0, nsweeps = 0, nfail = 0;
+    bool active = false;
+
+    /* ---- helpers as lambdas over the lane's state ---- */
+    auto substep_begin = [&]() {
+        /* BE_chem_solve.C:93-117 */
+#pragma unroll
+        for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
+#pragma unroll
+        for (int i = 0; i < N; i++) AT[i] = AT[i] * INV[i];
+#pragma unroll
+        for (int i = 0; i < N; i++) u0[i] = u[i];
+        isweep = 0;
+    };
+    auto cell_begin = [&]() -> bool {
+        double at[N];
+#pragma unroll
+        for (int s = 0; s < N; s++) {
+            const long long off = cell * io.cs + s * io.ss;
+            y[s] = io.state[off];
+            at[s] = io.atol[off];
+            RT[s] = io.rtol ? io.rtol[off] : io.rtol_scalar;
+        }
+        to_number_density<Net>(y, at);
+        Net::electrons(y);
+#pragma unroll
+        for (int s = 0; s < N; s++) AT[s] = at[s];
+        dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+        dt = io.dt ? io.dt[cell] : -1.0;
+        if (dt < 0) dt = dtf / 1e5;
+        ttot = 0;
+        siter = 0;
+        nsweeps = 0;
+        nfail = 0;
+#pragma unroll
+        for (int s = 0; s < N; s++) {
+            SC[s] = y[s];
+            PREV[s] = y[s];
+            INV[s] = 1.0 / y[s];
+        }
+        if (!(ttot < dtf)) return false;
+        substep_begin();
+        return true;
+    };
+    auto cell_end = [&](int status) {
+#pragma unroll
+        for (int s = 0; s < N; s++) {
+            double v = y[s], a = AT[s];
+            if (!Net::INPUT_IS_NUMBER && s != Net::IGE) {
+                v = v * Net::unit(s);
+                a = a * Net::unit(s);
+            }
+            const long long off = cell * io.cs + s * io.ss;
+            io.state[off] = v;
+            io.atol[off] = a;
+        }
+        if (io.dt) io.dt[cell] = dt;
+        if (io.ttot) io.ttot[cell] = ttot;
+        if (io.status) io.status[cell] = status;
+        if (io.substeps) io.substeps[cell] = siter;
+        if (io.sweeps) io.sweeps[cell] = nsweeps;
+        if (io.failures) io.failures[cell] = nfail;
+    };
+    auto fetch = [&]() {
+        while (cell < io.ncells) {
+            if (cell_begin()) {
+                active = true;
+                return;
+            }
+            cell_end(ST_OK);
+            cell = queue ? (long long)atomicAdd(queue, 1ull) : cell + stride;
+        }
+        active = false;
+    };
+
+    fetch();
+    while (active) {
+        /* ---------------- one Newton sweep ---------------- */
+        bool ok, unsolved = false, nan = false;
+        double T, Tge;
+        {
+            /* BE_Resid_Fun (BE_chem_solve.C:246-275) */
+#pragma unroll
+            for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
+            Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+            interpolate<Net, BLOCK>(ts, dg_log(T), R);
+            double f[N];
+            ok = Net::rhs(y, R, T, ts.z, f);
+            if (ok) {
+#pragma unroll
+                for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
+#pragma unroll
+                for (int i = 0; i < N; i++) f[i] = f[i] * INV[i];
+#pragma unroll
+                for (int i = 0; i < N; i++) f[i] = u[i] - u0[i] - dt * f[i];
+                /* BE_Resid_Jac (BE_chem_solve.C:280-321) */
+#pragma unroll
+                for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
+                JacPut<N, BLOCK> put{J, INV, SC, -dt};
+                ok = Net::jac(y, R, Tge, T, ts.z, put);
+                if (ok) {
+#pragma unroll
+                    for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
+                    gauss_elim<N, BLOCK>(J, f);
+                    /* Newton update and max-norm test (BE_chem_solve.C:173-206) */
+#pragma unroll
+                    for (int i = 0; i < N; i++) u[i] = u[i] - 1.0 * f[i];
+#pragma unroll
+                    for (int i = 0; i < N; i++) {
+                        if (fabs(f[i]) > (AT[i] + RT[i] * fabs(u[i]))) {
+                            unsolved = true;
+                            break;
+                        }
+                        if (u[i] != u[i]) {
+                            nan = true;
+                            break;
+                        }
+                    }
+                }
+            }
+        }
+        isweep++;
+        nsweeps++;
+        int rv = -1;
+        if (!ok || nan) rv = 1;
+        else if (!unsolved) rv = 0;
+        else if (isweep >= cfg.max_sweeps) rv = 1;
+        if (rv < 0) continue;
+
+        /* ---------- end of BE_chem_solve: unscale (BE_chem_solve.C:225-239) ---------- */
+#pragma unroll
+        for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
+#pragma unroll
+        for (int i = 0; i < N; i++) AT[i] = AT[i] * SC[i];
+        /* ---------- substep accept / reject (C.template:197-255) ---------- */
+        if (rv == 0) {
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                if (y[i] < 0) rv = 1;
+        }
+        int done = -1;
+        if (rv == 0) {
+            if (siter == cfg.max_substeps) {
+                done = ST_MAX_SUBSTEPS;
+            } else {
+                siter++;
+                ttot += dt;
+                const double grown = dt * 1.1, rest = dtf - ttot;
+                dt = grown < rest ? grown : rest;
+#pragma unroll
+                for (int i = 0; i < N; i++) {
+                    PREV[i] = y[i];
+                    if (y[i] < cfg.floor_value) y[i] = cfg.floor_value;
+                }
+                if (!(ttot < dtf)) done = ST_OK;
+            }
+        } else {
+            nfail++;
+            dt /= 2.0;
+#pragma unroll
+            for (int i = 0; i < N; i++) y[i] = PREV[i];
+            if (dt / dtf < cfg.dt_ratio_floor) done = ST_DT_UNDERFLOW;
+        }
+        if (done < 0) {
+            substep_begin();
+            continue;
+        }
+        cell_end(done);
+        cell = queue ? (long long)atomicAdd(queue, 1ull) : cell + stride;
+        fetch();
+    }
+}
+
+}  // namespace dg
+#endif

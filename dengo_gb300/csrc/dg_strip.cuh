@@ -1,0 +1,317 @@
+/*
+ * Kernels behind the reference's strip-wise entry points, one thread per
+ * cell of a strip (AoS input, input[cell*nchem + species]):
+ *   <n>_calculate_temperature  rates_and_rate_tables.C.template:309-350
+ *   <n>_interpolate_rates      rates_and_rate_tables.C.template:362-455
+ *   calculate_rhs_<n>          rates_and_rate_tables.C.template:460-522
+ *   calculate_jacobian_<n>     rates_and_rate_tables.C.template:527-599
+ *   ensure_electron_consistency  rates_and_rate_tables.C.template:604-630
+ *   temperature_from_mass_density  rates_and_rate_tables.C.template:635-668
+ * Per-strip quantities live in device arrays laid out like the reference's
+ * data struct fields: Ts[cell], rs[table][cell], ...
+ */
+#ifndef DG_STRIP_CUH
+#define DG_STRIP_CUH
+
+#include "dg_engine.cuh"
+
+namespace dg {
+
+struct StripBufs {
+    double *Ts, *logTs, *invTs, *dTs_ge, *Tdef, *dT;
+    double *rs, *drs;   /* [NT][ld] */
+    int *bin_id;
+    int *flag;          /* per cell: 1 if a species was negative */
+    long long ld;       /* leading dimension of rs/drs */
+};
+
+/* Column accessor over a [table][cell] array. */
+struct ColumnRates {
+    const double *p;
+    long long ld;
+    __device__ __forceinline__ double operator[](int k) const { return p[k * ld]; }
+};
+
+template <class Net>
+__device__ __forceinline__ void load_cell(const double *in, int nchem, int c, double (&y)[Net::N])
+{
+#pragma unroll
+    for (int s = 0; s < Net::N; s++) y[s] = in[(long long)c * nchem + s];
+}
+
+/* Table interpolation into a per-thread array (values only). */
+template <class Net>
+__device__ __forceinline__ void interpolate_local(const TableSet &ts, double logT, double *R)
+{
+    const int bin = (int)(ts.idbin * (logT - ts.lb));
+    const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+    const double t1 = (ts.lb + (bin) * ts.dbin);
+    const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+    const double Tdef = (logT - t1) / (t2 - t1);
+    const double2 *row = ts.pairs + (size_t)bc * Net::NT;
+    for (int k = 0; k < Net::NT; k++) {
+        if (Net::zdep(k)) {
+            R[k] = ts.zvals[k];
+        } else {
+            const double2 pr = row[k];
+            R[k] = pr.x + Tdef * pr.y;
+        }
+    }
+}
+
+template <class Net>
+__global__ void strip_temperature_kernel(const double *in, int nstrip, int nchem, TableSet ts,
+                                         StripBufs b)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nstrip) return;
+    double y[Net::N];
+    load_cell<Net>(in, nchem, c, y);
+    double T, Tge;
+    Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+    b.Ts[c] = T;
+    b.logTs[c] = dg_log(T);
+    b.invTs[c] = 1.0 / T;
+    b.dTs_ge[c] = Tge;
+}
+
+/* zv/dzv: values and z-derivatives of the redshift tables at this call's z
+ * (host-computed; zero when z is outside the tabulated range). */
+template <class Net>
+__global__ void strip_interpolate_kernel(int nstrip, TableSet ts, StripBufs b, const double *zv,
+                                         const double *dzv)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nstrip) return;
+    const double logT = b.logTs[c];
+    const int bin = (int)(ts.idbin * (logT - ts.lb));
+    const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+    const double t1 = (ts.lb + (bin) * ts.dbin);
+    const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+    const double Tdef = (logT - t1) / (t2 - t1);
+    const double dT = (t2 - t1);
+    b.bin_id[c] = bc;
+    b.Tdef[c] = Tdef;
+    b.dT[c] = dT;
+    const double invT = b.invTs[c];
+    const double2 *row = ts.pairs + (size_t)bc * Net::NT;
+    for (int k = 0; k < Net::NT; k++) {
+        double v, dv;
+        if (Net::zdep(k)) {
+            v = zv[k];
+            dv = dzv[k];
+        } else {
+            const double2 pr = row[k];
+            v = pr.x + Tdef * pr.y;
+            dv = pr.y;
+            dv = dv / dT;
+            dv = dv * invT;
+        }
+        b.rs[k * b.ld + c] = v;
+        b.drs[k * b.ld + c] = dv;
+    }
+}
+
+template <class Net>
+__global__ void strip_rhs_kernel(const double *in, double *out, int nstrip, int nchem,
+                                 double z, StripBufs b)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nstrip) return;
+    double y[Net::N], f[Net::N];
+    load_cell<Net>(in, nchem, c, y);
+    const ColumnRates R{b.rs + c, b.ld};
+    const bool ok = Net::rhs(y, R, b.Ts[c], z, f);
+    b.flag[c] = ok ? 0 : 1;
+    if (!ok) return;
+#pragma unroll
+    for (int s = 0; s < Net::N; s++) out[(long long)c * nchem + s] = f[s];
+}
+
+struct PlainPut {
+    double *J;
+    int N;
+    __device__ __forceinline__ void operator()(int q, int v, double jv) const { J[v * N + q] = jv; }
+};
+
+template <class Net>
+__global__ void strip_jacobian_kernel(const double *in, double *J, int nstrip, int nchem,
+                                      double z, StripBufs b)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nstrip) return;
+    double y[Net::N];
+    load_cell<Net>(in, nchem, c, y);
+    const ColumnRates R{b.rs + c, b.ld};
+    const PlainPut put{J + (long long)c * Net::N * Net::N, Net::N};
+    const bool ok = Net::jac(y, R, b.dTs_ge[c], b.Ts[c], z, put);
+    b.flag[c] = ok ? 0 : 1;
+}
+
+/* The reference accumulates total_e across the whole strip without
+ * resetting it per cell; reproduced by one thread walking the cells. */
+template <class Net>
+__global__ void strip_electrons_kernel(double *in, int nstrip, int nchem)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double total_e = 0.0;
+    for (int c = 0; c < nstrip; c++) {
+        double y[Net::N];
+        load_cell<Net>(in, nchem, c, y);
+        total_e = Net::electron_sum(y, total_e);
+        if (Net::IDE >= 0) in[(long long)c * nchem + Net::IDE] = total_e;
+    }
+}
+
+template <class Net>
+__global__ void strip_temperature_from_mass_kernel(const double *in, int nstrip, int nchem,
+                                                   double *T)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nstrip) return;
+    double y[Net::N];
+    load_cell<Net>(in, nchem, c, y);
+    T[c] = Net::temperature_from_mass_density(y);
+}
+
+/* Scaled Jacobian store into a per-thread array (BE_chem_solve.C:301-318). */
+template <int N>
+struct ScaledLocalPut {
+    double *J;
+    const double *inv, *sc;
+    double mdt;
+    __device__ __forceinline__ void operator()(int q, int v, double jv) const
+    {
+        double a = jv * inv[q];
+        a = a * sc[v];
+        a = mdt * a;
+        if (q == v) a = a + 1.0;
+        J[v * N + q] = a;
+    }
+};
+
+template <int N>
+__device__ void gauss_elim_local(double *A, double *x)
+{
+    for (int k = 0; k < N - 1; k++) {
+        int p = k;
+        for (int i = k + 1; i < N; i++)
+            if (fabs(A[k * N + i]) > fabs(A[k * N + p])) p = i;
+        for (int j = k; j < N; j++) {
+            const double t = A[j * N + k];
+            A[j * N + k] = A[j * N + p];
+            A[j * N + p] = t;
+        }
+        const double t = x[k];
+        x[k] = x[p];
+        x[p] = t;
+        for (int i = k + 1; i < N; i++) A[k * N + i] /= A[k * N + k];
+        for (int j = k + 1; j < N; j++)
+            for (int i = k + 1; i < N; i++) A[j * N + i] -= A[k * N + i] * A[j * N + k];
+        for (int i = k + 1; i < N; i++) x[i] -= A[k * N + i] * x[k];
+    }
+    for (int i = N - 1; i >= 0; i--) {
+        for (int j = i + 1; j < N; j++) x[i] -= A[j * N + i] * x[j];
+        x[i] /= A[i * N + i];
+    }
+}
+
+/* BE_chem_solve (BE_chem_solve.C:79-241) over one strip in lockstep: one
+ * block, one thread per cell.  All cells share the sweep loop; a negative
+ * value anywhere fails the strip at the RHS or Jacobian stage, a NaN stops
+ * the sweep at the first such cell in cell order (later cells keep their
+ * pre-update values), and the strip converges only when every cell passed
+ * the max-norm test.  Writes u and atol back as the reference does and the
+ * last temperature of each cell to Ts. */
+template <class Net>
+__global__ void __launch_bounds__(DENGO_MAX_NCELLS)
+be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstrip,
+                const double *scaling, TableSet ts, int max_sweeps, int *ret, double *Ts)
+{
+    constexpr int N = Net::N;
+    const int c = threadIdx.x;
+    const bool act = c < nstrip;
+    __shared__ int first_bad;
+    double us[N], u0[N], sc[N], inv[N], at[N], rt[N], y[N], g[N], upre[N];
+    double R[Net::NT];
+    double A[N * N];
+    if (act) {
+        for (int i = 0; i < N; i++) {
+            sc[i] = scaling[c * N + i];
+            inv[i] = 1.0 / sc[i];
+            us[i] = u[c * N + i] * inv[i];
+            at[i] = atol[c * N + i] * inv[i];
+            rt[i] = rtol[c * N + i];
+            u0[i] = us[i];
+        }
+    }
+    int rv = 1;
+    int fail_mode = 0; /* 0 none, 1 u = y*sc (RHS/Jacobian failure) */
+    for (int isweep = 0; isweep < max_sweeps; isweep++) {
+        bool ok = true;
+        double T = 0, Tge = 0;
+        if (act) {
+            for (int i = 0; i < N; i++) y[i] = us[i] * sc[i];
+            Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+            Ts[c] = T;
+            interpolate_local<Net>(ts, dg_log(T), R);
+            ok = Net::rhs(y, R, T, ts.z, g);
+        }
+        if (__syncthreads_or(act && !ok)) {
+            fail_mode = 1;
+            break;
+        }
+        if (act) {
+            for (int i = 0; i < N; i++) us[i] = y[i] * inv[i];
+            for (int i = 0; i < N; i++) g[i] = g[i] * inv[i];
+            for (int i = 0; i < N; i++) g[i] = us[i] - u0[i] - dt * g[i];
+            for (int i = 0; i < N; i++) y[i] = us[i] * sc[i];
+            const ScaledLocalPut<N> put{A, inv, sc, -dt};
+            ok = Net::jac(y, R, Tge, T, ts.z, put);
+        }
+        if (__syncthreads_or(act && !ok)) {
+            fail_mode = 1;
+            break;
+        }
+        bool unsolved = false, nan = false;
+        if (act) {
+            for (int i = 0; i < N; i++) us[i] = y[i] * inv[i];
+            gauss_elim_local<N>(A, g);
+            for (int i = 0; i < N; i++) upre[i] = us[i];
+            for (int i = 0; i < N; i++) us[i] -= 1.0 * g[i];
+            for (int i = 0; i < N; i++) {
+                if (fabs(g[i]) > (at[i] + rt[i] * fabs(us[i]))) {
+                    unsolved = true;
+                    break;
+                }
+                if (us[i] != us[i]) {
+                    nan = true;
+                    break;
+                }
+            }
+        }
+        if (c == 0) first_bad = nstrip;
+        __syncthreads();
+        if (act && nan) atomicMin(&first_bad, c);
+        __syncthreads();
+        if (first_bad < nstrip) {
+            if (act && c > first_bad)
+                for (int i = 0; i < N; i++) us[i] = upre[i];
+            rv = 1;
+            break;
+        }
+        const bool any_unsolved = __syncthreads_or(act && unsolved);
+        rv = any_unsolved ? 1 : 0;
+        if (!any_unsolved) break;
+    }
+    if (act) {
+        for (int i = 0; i < N; i++) {
+            u[c * N + i] = fail_mode ? y[i] * sc[i] : us[i] * sc[i];
+            atol[c * N + i] = at[i] * sc[i];
+        }
+    }
+    if (c == 0) *ret = fail_mode ? 1 : rv;
+}
+
+}  // namespace dg
+#endif

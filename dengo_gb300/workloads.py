@@ -1,0 +1,81 @@
+"""Seeded synthetic cell populations for the benchmark configurations.
+
+No public dataset exists for this solver; every workload is drawn here from
+``numpy.random.Generator(PCG64(seed))``.
+
+Primordial cells (``primordial_cells``):
+  * nH ~ logU(nH_lo, nH_hi) cm^-3, T ~ logU(T_lo, T_hi) K;
+  * He mass fraction Y = 0.24: n_He = Y / (4 (1 - Y)) nH;
+  * ionised fraction n(H+) = 1e-4 nH; n(H2) = 1e-6 nH;
+    n(H-) = n(H2+) = n(He++) = n(He+) = 1e-12 nH; neutral H and He take the
+    remainder of their nuclei;
+  * electrons from charge neutrality;
+  * ge [erg/g] from T through the solver's own T(ge) relation
+    (gamma = 5/3 for every species), so the first temperature evaluation
+    returns T;
+  * stored as the reference's mass densities rho_s = n_s w_s 1.67e-24 g/cm^3
+    (``input_is_number = False``), cells x species, species in state order;
+  * dtf = 0.1 t_ff with t_ff = sqrt(3 pi / (32 G rho)).
+  An optional unstable band puts a fraction of the cells at
+  T ~ logU(1e4, 1e5) K with nH ~ logU(1e3, nH_hi).
+"""
+
+import numpy as np
+
+KB = 1.3806504e-16
+MH = 1.67e-24
+G_NEWTON = 6.674e-8
+GAMMA = 5.0 / 3.0
+
+PRIMORDIAL_ORDER = ("H2_1", "H2_2", "H_1", "H_2", "H_m0", "He_1", "He_2", "He_3",
+                    "de", "ge")
+PRIMORDIAL_WEIGHTS = dict(H2_1=2.0, H2_2=2.0, H_1=1.00794, H_2=1.00794,
+                          H_m0=1.00794, He_1=4.002602, He_2=4.002602,
+                          He_3=4.002602, de=1.0)
+
+# Named configurations: (nH range, T range, unstable fraction).
+PRIMORDIAL_CONFIGS = {
+    "config1": dict(nH=(1.0, 1e6), T=(10.0, 1e8), unstable=0.0, seed=20241),
+    "config2": dict(nH=(1.0, 1e6), T=(10.0, 1e8), unstable=0.0, seed=20242),
+    "config3": dict(nH=(1e-3, 1e12), T=(10.0, 0.999e9), unstable=0.05, seed=20243),
+}
+
+
+def _logu(rng, lo, hi, n):
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+
+
+def primordial_cells(ncells, config="config1", seed=None, dt_factor=0.1):
+    """Return ``(state, dtf)``: state is (ncells, 10) float64 mass densities +
+    ge in state order, dtf is (ncells,) float64 seconds."""
+    cfg = PRIMORDIAL_CONFIGS[config]
+    rng = np.random.Generator(np.random.PCG64(cfg["seed"] if seed is None else seed))
+    nH = _logu(rng, *cfg["nH"], ncells)
+    T = _logu(rng, *cfg["T"], ncells)
+    if cfg["unstable"] > 0:
+        band = rng.uniform(size=ncells) < cfg["unstable"]
+        nb = int(band.sum())
+        T[band] = _logu(rng, 1e4, 1e5, nb)
+        nH[band] = _logu(rng, 1e3, cfg["nH"][1], nb)
+    Y = 0.24
+    nHe = Y / (4.0 * (1.0 - Y)) * nH
+    n = {}
+    n["H_2"] = 1e-4 * nH
+    n["H2_1"] = 1e-6 * nH
+    n["H_m0"] = 1e-12 * nH
+    n["H2_2"] = 1e-12 * nH
+    n["H_1"] = nH - n["H_2"] - n["H_m0"] - 2 * n["H2_1"] - 2 * n["H2_2"]
+    n["He_3"] = 1e-12 * nH
+    n["He_2"] = 1e-12 * nH
+    n["He_1"] = nHe - n["He_2"] - n["He_3"]
+    n["de"] = n["H_2"] - n["H_m0"] + n["H2_2"] + n["He_2"] + 2 * n["He_3"]
+    density = sum(PRIMORDIAL_WEIGHTS[s] * n[s] for s in PRIMORDIAL_ORDER
+                  if s not in ("de", "ge"))
+    gsum = sum(n[s] / (GAMMA - 1.0) for s in PRIMORDIAL_ORDER if s != "ge")
+    ge = T * KB * gsum / (density * MH)
+    state = np.empty((ncells, len(PRIMORDIAL_ORDER)))
+    for i, s in enumerate(PRIMORDIAL_ORDER):
+        state[:, i] = ge if s == "ge" else n[s] * PRIMORDIAL_WEIGHTS[s] * MH
+    rho = state[:, :-1].sum(axis=1)
+    tff = np.sqrt(3.0 * np.pi / (32.0 * G_NEWTON * rho))
+    return state, dt_factor * tff

@@ -1,0 +1,40 @@
+/* ORACLE -- test infrastructure; see hdf5.h. */
+#ifndef DGO_HDF5_HL_SHIM_H
+#define DGO_HDF5_HL_SHIM_H
+#include "hdf5.h"
+
+static inline herr_t H5LTread_dataset_double(hid_t id, const char *dset, double *buf)
+{
+    char p[1200];
+    snprintf(p, sizeof(p), "%s/%s.f64", dgo_shim_paths[id], dset[0] == '/' ? dset + 1 : dset);
+    FILE *f = fopen(p, "rb");
+    if (!f) { fprintf(stderr, "hdf5 shim: cannot open %s\n", p); return -1; }
+    size_t n = 0;
+    while (fread(buf + n, sizeof(double), 1, f) == 1) n++;
+    fclose(f);
+    return 0;
+}
+static inline herr_t H5LTget_dataset_info(hid_t id, const char *dset, hsize_t *dims,
+                                          void *a, void *b)
+{
+    char p[1200];
+    (void)a; (void)b;
+    snprintf(p, sizeof(p), "%s/%s.f64", dgo_shim_paths[id], dset[0] == '/' ? dset + 1 : dset);
+    FILE *f = fopen(p, "rb");
+    if (!f) return -1;
+    fseek(f, 0, SEEK_END);
+    *dims = (hsize_t)(ftell(f) / 8);
+    fclose(f);
+    return 0;
+}
+static inline herr_t H5LTmake_dataset_double(hid_t id, const char *dset, int rank,
+                                             const hsize_t *dims, const double *buf)
+{
+    (void)id; (void)dset; (void)rank; (void)dims; (void)buf; return 0;
+}
+static inline herr_t H5LTset_attribute_double(hid_t id, const char *obj, const char *attr,
+                                              const double *buf, size_t n)
+{
+    (void)id; (void)obj; (void)attr; (void)buf; (void)n; return 0;
+}
+#endif

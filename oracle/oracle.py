@@ -1,0 +1,138 @@
+"""ORACLE -- test infrastructure, not part of the product.
+
+Python access to the C restatement (be_oracle.c + gen/<name>_oracle.c) and,
+where it was built, to the reference's own solver (oracle/_ref).  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+P_D = C.POINTER(C.c_double)
+P_I = C.POINTER(C.c_int)
+P_L = C.POINTER(C.c_longlong)
+
+CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w"]
+
+
+class Config(C.Structure):
+    _fields_ = [("max_sweeps", C.c_int), ("max_substeps", C.c_int),
+                ("dt_ratio_floor", C.c_double), ("floor_value", C.c_double)]
+
+
+def build_oracle(name="primordial", force=False):
+    """Compile the C restatement for network ``name`` (gcc)."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(BUILD, "libdgo_%s.so" % name)
+    srcs = [os.path.join(HERE, "be_oracle.c"), os.path.join(HERE, "gen", "%s_oracle.c" % name)]
+    if force or not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out)
+                                               for s in srcs):
+        subprocess.check_call(["gcc"] + CFLAGS + srcs + ["-o", out, "-lm"])
+    return out
+
+
+def _dp(a):
+    return a.ctypes.data_as(P_D)
+
+
+class Oracle:
+    """The C restatement of the reference solver for one network."""
+
+    def __init__(self, name="primordial"):
+        self.name = name
+        self.lib = C.CDLL(build_oracle(name))
+        self.net_addr = C.addressof(C.c_char.in_dll(self.lib, "dgo_%s_network" % name))
+        self.lib.dgo_default_config.restype = Config
+        self.lib.dgo_evolve_cells.argtypes = [
+            C.c_void_p, C.POINTER(P_D), P_D, P_D, C.c_double, P_D, P_D, P_D, C.c_longlong,
+            C.POINTER(Config), P_D, P_I, P_L, P_L, P_L, C.c_int]
+        self.lib.dgo_evolve.argtypes = [C.c_void_p, C.c_void_p, C.c_double, P_D, C.c_double,
+                                        P_D, P_D, P_D, C.c_longlong, C.POINTER(Config),
+                                        C.c_void_p]
+        self.lib.dgo_evolve.restype = C.c_double
+        self.nt = getattr(self.lib, "dgo_%s_ntables" % name)()
+        ntab = getattr(self.lib, "dgo_%s_table_len" % name)
+        ntab.argtypes = [C.c_int]
+        self.table_len = [ntab(k) for k in range(self.nt)]
+
+    def config(self, max_sweeps=10, max_substeps=50000):
+        c = self.lib.dgo_default_config()
+        c.max_sweeps, c.max_substeps = max_sweeps, max_substeps
+        return c
+
+    def _tables(self, tables_in_order):
+        keep = [np.ascontiguousarray(t, np.float64) for t in tables_in_order]
+        return keep, (P_D * len(keep))(*[_dp(t) for t in keep])
+
+    def evolve_cells(self, tables_in_order, state, dtf, dt=None, z=-1.0, rtol=None, atol=None,
+                     nthreads=0, max_sweeps=10, max_substeps=50000):
+        """Per-cell reference semantics (dengo_evolve with dims = 1 per cell).
+
+        state: (cells, N) AoS mass densities + ge.  Returns a dict."""
+        st = np.ascontiguousarray(state, np.float64).copy()
+        n = st.shape[0]
+        rt = np.full_like(st, 1e-6) if rtol is None else np.ascontiguousarray(rtol, np.float64).copy()
+        at = (1e-6 * st) if atol is None else np.ascontiguousarray(atol, np.float64).copy()
+        dtf = np.broadcast_to(np.asarray(dtf, np.float64), (n,)).copy()
+        dt = np.full(n, -1.0) if dt is None else np.broadcast_to(np.asarray(dt, np.float64), (n,)).copy()
+        keep, tp = self._tables(tables_in_order)
+        ttot = np.zeros(n)
+        status = np.zeros(n, np.int32)
+        sub, sw, fl = (np.zeros(n, np.int64) for _ in range(3))
+        cfg = self.config(max_sweeps, max_substeps)
+        self.lib.dgo_evolve_cells(self.net_addr, tp, _dp(dtf), _dp(dt), float(z), _dp(st),
+                                  _dp(rt), _dp(at), n, C.byref(cfg), _dp(ttot),
+                                  status.ctypes.data_as(P_I), sub.ctypes.data_as(P_L),
+                                  sw.ctypes.data_as(P_L), fl.ctypes.data_as(P_L), int(nthreads))
+        return dict(state=st, atol=at, dt=dt, ttot=ttot, status=status, substeps=sub,
+                    sweeps=sw, failures=fl)
+
+
+class Reference:
+    """The reference's own generated solver, built by oracle/ref_build.py
+    (only where the reference checkout exists)."""
+
+    def __init__(self, name="primordial"):
+        path = os.path.join(REF, "libref_%s.so" % name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        os.environ.setdefault("DGO_REF_TABLE_DIR", os.path.join(REF, name))
+        self.lib = C.CDLL(path)
+        self.lib.ref_evolve_cells.argtypes = [P_D, P_D, C.c_double, P_D, P_D, P_D, C.c_longlong,
+                                              P_D, C.c_int]
+        self.lib.ref_setup.restype = C.c_void_p
+        self.lib.ref_rs.restype = P_D
+        self.lib.ref_rs.argtypes = [C.c_void_p, C.c_int]
+        self.lib.ref_Ts.restype = P_D
+        self.lib.ref_Ts.argtypes = [C.c_void_p]
+        self.lib.ref_dTs_ge.restype = P_D
+        self.lib.ref_dTs_ge.argtypes = [C.c_void_p]
+        for f in ("ref_rhs", "ref_jac"):
+            getattr(self.lib, f).argtypes = [P_D, P_D, C.c_int, C.c_int, C.c_void_p]
+        self.lib.ref_temperature.argtypes = [C.c_void_p, P_D, C.c_int, C.c_int]
+        self.lib.ref_interpolate.argtypes = [C.c_void_p, C.c_int]
+        self.lib.ref_electrons.argtypes = [P_D, C.c_int, C.c_int]
+        self.lib.ref_evolve.argtypes = [C.c_void_p, C.c_double, P_D, C.c_double, P_D, P_D, P_D,
+                                        C.c_longlong]
+        self.lib.ref_evolve.restype = C.c_double
+        self.lib.ref_BE_chem_solve.argtypes = [P_D, C.c_double, P_D, P_D, C.c_int, C.c_int, P_D,
+                                               C.c_void_p, P_D, P_D, P_D, P_D]
+        self.N = self.lib.ref_nchem()
+
+    def evolve_cells(self, state, dtf, dt=None, z=-1.0, rtol=None, atol=None, nthreads=0):
+        st = np.ascontiguousarray(state, np.float64).copy()
+        n = st.shape[0]
+        rt = np.full_like(st, 1e-6) if rtol is None else np.ascontiguousarray(rtol, np.float64).copy()
+        at = (1e-6 * st) if atol is None else np.ascontiguousarray(atol, np.float64).copy()
+        dtf = np.broadcast_to(np.asarray(dtf, np.float64), (n,)).copy()
+        dt = np.full(n, -1.0) if dt is None else np.broadcast_to(np.asarray(dt, np.float64), (n,)).copy()
+        ttot = np.zeros(n)
+        self.lib.ref_evolve_cells(_dp(dtf), _dp(dt), float(z), _dp(st), _dp(rt), _dp(at), n,
+                                  _dp(ttot), int(nthreads))
+        return dict(state=st, atol=at, dt=dt, ttot=ttot)

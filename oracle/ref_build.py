@@ -1,0 +1,209 @@
+"""ORACLE -- test infrastructure.  Builds the reference's own solver into
+``oracle/_ref/`` so the C restatement can be pinned against it.
+
+Recipe (runs only where the reference checkout exists):
+
+1. Import the reference package read-only from ``/root/reference`` with
+   compatibility shims that change no arithmetic:
+   * ``h5py`` is replaced by a writer of raw float64 files (the container has
+     no HDF5); ``docutils.utils.roman`` (imported, unused) is stubbed;
+   * the cooling equations' pre-rename species names (``HI``, ``HeII``, ...)
+     are aliased to the registered species (dengo/primordial_cooling.py vs
+     dengo/primordial_rates.py:36-43);
+   * ``CoolingAction.species`` concatenates lists instead of dict views
+     (reaction_classes.py:356, a Python-2 idiom);
+   * ``CoolingAction`` is given an order by name so ``write_solver`` can sort
+     it (chemical_network.py:314);
+   * temporaries are parsed with the species and table symbols in scope, so
+     ``galdl`` of ``gloverabel08`` refers to the species symbols
+     (reaction_classes.py:346-350).
+2. Build the primordial network (all reactions; all cooling actions except
+   ``compton``; 1024 bins over 1-1e9 K) and call the reference's
+   ``write_solver(..., ode_solver_source=None)`` into ``oracle/_ref/<name>/``:
+   the rendered ``<name>_solver.C/.h`` and the tables.
+3. Compile the rendered solver together with the reference's
+   ``dengo/solvers/BE_chem_solve.C`` (read where it lies), a small C harness
+   written here, and the header-only HDF5 stand-in in ``oracle/hdf5_shim/``:
+   ``g++ -O2 -ffp-contract=off -fopenmp -shared``.
+
+Output: ``oracle/_ref/libref_<name>.so`` exporting ``ref_*`` functions.
+"""
+
+import os
+import subprocess
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("DGO_REFERENCE_ROOT", "/root/reference")
+OUT = os.path.join(HERE, "_ref")
+
+ALIASES = dict(HI="H_1", HII="H_2", HM="H_m0", HeI="He_1", HeII="He_2",
+               HeIII="He_3", H2I="H2_1", H2II="H2_2")
+
+
+def _install_shims():
+    h5 = types.ModuleType("h5py")
+
+    class _File:
+        def __init__(self, path, mode="r"):
+            self.path = path
+            os.makedirs(path + ".d", exist_ok=True)
+
+        def create_dataset(self, name, data):
+            np.ascontiguousarray(data, dtype="<f8").tofile(
+                os.path.join(self.path + ".d", name.strip("/") + ".f64"))
+
+        def close(self):
+            pass
+
+    h5.File = _File
+    sys.modules["h5py"] = h5
+    du = types.ModuleType("docutils")
+    duu = types.ModuleType("docutils.utils")
+    dur = types.ModuleType("docutils.utils.roman")
+    du.utils, duu.roman = duu, dur
+    sys.modules.update({"docutils": du, "docutils.utils": duu,
+                        "docutils.utils.roman": dur})
+
+
+def _reference_primordial():
+    sys.path.insert(0, REF_ROOT)
+    _install_shims()
+    import sympy
+    import dengo.reaction_classes as rc
+    import dengo.chemical_network as cn
+    from dengo.primordial_rates import setup_primordial
+    setup_primordial()
+    for a, n in ALIASES.items():
+        rc.species_registry[a] = rc.species_registry[n]
+
+    def equation(self):
+        if self._eq is not None:
+            return self._eq
+        symbols = {n: s.symbol for n, s in rc.species_registry.items()}
+        ta = {n: sympy.Symbol("%s_%s[i]" % (self.name, n)) for n in self.tables}
+        tp = {n: sympy.Symbol(n) for n in self.temporaries}
+        self.table_symbols.update(ta)
+        self.temp_symbols.update(tp)
+        symbols.update(ta)
+        symbols.update(tp)
+        self._eq = eval(self._equation, symbols)
+        for n, e in self.temporaries.items():
+            scope = {k: s.symbol for k, s in rc.species_registry.items()}
+            scope.update(ta)
+            self._eq = self._eq.subs(n, sympy.sympify(e, locals=scope))
+        return self._eq
+
+    def species(self):
+        self.equation
+        bad = set(list(self.temp_symbols.values()) + list(self.table_symbols.values()))
+        return {rc.species_registry[str(s).replace("[i]", "")]
+                for s in self.equation.atoms(sympy.Symbol) if s not in bad}
+
+    rc.CoolingAction.equation = property(equation)
+    rc.CoolingAction.species = property(species)
+    rc.CoolingAction.__lt__ = lambda a, b: a.name < b.name
+    import dengo.primordial_cooling  # noqa: F401
+    net = cn.ChemicalNetwork()
+    for c in sorted(rc.cooling_registry):
+        if c != "compton":
+            net.add_cooling(c)
+    for r in sorted(rc.reaction_registry):
+        net.add_reaction(r)
+    net.init_temperature((1e0, 1e9), n_bins=1024)
+    return net
+
+
+HARNESS = r"""
+/* ORACLE -- test infrastructure: C entry points over the reference's
+ * rendered solver, written by oracle/ref_build.py. */
+#include "%(n)s_solver.h"
+#include <stddef.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+void %(n)s_calculate_temperature(%(n)s_data *, double *, int, int);
+void %(n)s_interpolate_rates(%(n)s_data *, int);
+static const size_t dgo_rs_off[] = { %(rs)s };
+extern "C" {
+void *ref_setup(void) { return %(n)s_setup_data(NULL, NULL); }
+void ref_free(void *d) { free(d); }
+int ref_nchem(void) { return NSPECIES; }
+double ref_evolve(void *d, double dtf, double *dt, double z, double *input,
+                  double *rtol, double *atol, long long dims)
+{ return dengo_evolve_%(n)s(dtf, *dt, z, input, rtol, atol, dims, (%(n)s_data *)d); }
+int ref_rhs(double *in, double *out, int ns, int nc, void *d)
+{ return calculate_rhs_%(n)s(in, out, ns, nc, d); }
+int ref_jac(double *in, double *out, int ns, int nc, void *d)
+{ return calculate_jacobian_%(n)s(in, out, ns, nc, d); }
+void ref_temperature(void *d, double *in, int ns, int nc)
+{ %(n)s_calculate_temperature((%(n)s_data *)d, in, ns, nc); }
+void ref_interpolate(void *d, int ns) { %(n)s_interpolate_rates((%(n)s_data *)d, ns); }
+const double *ref_Ts(void *d) { return ((%(n)s_data *)d)->Ts; }
+const double *ref_dTs_ge(void *d) { return ((%(n)s_data *)d)->dTs_ge; }
+void ref_electrons(double *in, int ns, int nc) { ensure_electron_consistency(in, ns, nc); }
+int ref_BE_chem_solve(double *u, double dt, double *rtol, double *atol, int ns, int nc,
+                      double *scaling, void *d, double *u0, double *s, double *gu, double *Ju)
+{ return BE_chem_solve(calculate_rhs_%(n)s, calculate_jacobian_%(n)s, u, dt, rtol, atol,
+                       ns, nc, scaling, d, u0, s, gu, Ju); }
+const double *ref_rs(void *d, int k) {
+    return (const double *)((const char *)d + dgo_rs_off[k]);
+}
+void ref_evolve_cells(const double *dtf, double *dt, double z, double *input, double *rtol,
+                      double *atol, long long ncells, double *ttot, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+        %(n)s_data *d = %(n)s_setup_data(NULL, NULL);
+        long long c;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+        for (c = 0; c < ncells; c++) {
+            double t = dt[c];
+            ttot[c] = dengo_evolve_%(n)s(dtf[c], t, z, input + c * NSPECIES,
+                                         rtol + c * NSPECIES, atol + c * NSPECIES, 1, d);
+            dt[c] = t;
+        }
+        free(d);
+    }
+}
+}
+"""
+
+
+def build(name="primordial"):
+    if name != "primordial":
+        raise ValueError("only the primordial network renders with the reference here")
+    if not os.path.isdir(os.path.join(REF_ROOT, "dengo")):
+        raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
+    net = _reference_primordial()
+    odir = os.path.join(OUT, name)
+    os.makedirs(odir, exist_ok=True)
+    net.write_solver(name, output_dir=odir, ode_solver_source=None)
+    # offsets of the rs_* scratch arrays, in reaction-then-cooling order
+    fields = ["rs_%s" % r for r in sorted(net.reactions)]
+    for c in sorted(net.cooling_actions):
+        fields += ["cs_%s_%s" % (c, t) for t in sorted(net.cooling_actions[c].tables)]
+    rs = ", ".join("offsetof(%s_data, %s)" % (name, f) for f in fields)
+    harness = os.path.join(odir, "harness.cpp")
+    with open(harness, "w") as f:
+        f.write(HARNESS % dict(n=name, rs=rs))
+    lib = os.path.join(OUT, "libref_%s.so" % name)
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w",
+           "-I", os.path.join(HERE, "hdf5_shim"), "-I", odir,
+           os.path.join(odir, "%s_solver.C" % name),
+           os.path.join(REF_ROOT, "dengo", "solvers", "BE_chem_solve.C"),
+           harness, "-o", lib, "-lm"]
+    subprocess.check_call(cmd)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build(*(sys.argv[1:] or ["primordial"])))

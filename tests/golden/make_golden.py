@@ -1,0 +1,159 @@
+"""Generates the golden vectors under tests/golden/ from the reference itself.
+
+Run where the reference checkout exists (it is read, never modified):
+
+    python tests/golden/make_golden.py
+
+1. Builds the reference's own primordial solver (oracle/ref_build.py: the
+   reference's templates rendered by its own ``write_solver``, compiled with
+   its ``BE_chem_solve.C``).
+2. Runs it on seeded inputs and stores inputs and outputs in
+   ``primordial_golden.npz``:
+   * ``evolve_*``: ``dengo_evolve_primordial`` called once per cell
+     (dims = 1) on config-1 and config-3 cells plus edge cases (dtf = 0,
+     a negative density, a zero density, a given initial dt, T at and above
+     the table's upper bound, T below its lower bound);
+   * ``strip_*``: calculate_temperature / interpolate_rates /
+     calculate_rhs / calculate_jacobian on a 32-cell strip of number
+     densities, and ensure_electron_consistency on that strip;
+   * ``be_*``: one ``BE_chem_solve`` over an 8-cell strip in lockstep;
+   * ``lock_*``: ``dengo_evolve_primordial`` over an 8-cell strip (dims = 8,
+     the reference's lockstep semantics);
+   * ``tables``: every rate and cooling table the reference wrote.
+3. Stores the reference's printed expressions (RHS rows, Jacobian entries,
+   T(ge), dT/dge, mass density) in ``primordial_expressions.json`` after
+   checking that each appears verbatim in the reference's rendered C.
+"""
+
+import ctypes as C
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from dengo_gb300.workloads import primordial_cells  # noqa: E402
+
+P_D = C.POINTER(C.c_double)
+
+
+def dp(a):
+    return a.ctypes.data_as(P_D)
+
+
+def edge_cells():
+    """Hand-made cells exercising the driver's special paths."""
+    base, dtf = primordial_cells(8, "config1", seed=777)
+    cells = base.copy()
+    dtfs = dtf.copy()
+    dts = np.full(8, -1.0)
+    dtfs[0] = 0.0                       # no substep at all
+    cells[1, 3] = -1e-30                # a negative H+ density
+    cells[2, 4] = 0.0                   # a zero H- density: scale 0 -> NaN
+    dts[3] = dtfs[3] / 37.0             # caller-given initial dt
+    cells[4, 9] *= 1e4                  # very hot: T clamps at the upper bound
+    cells[5, 9] *= 1e-6                 # very cold: T clamps at the lower bound
+    return cells, dtfs, dts
+
+
+def main():
+    import ref_build
+    from oracle import Reference
+    ref_build.build("primordial")
+    ref = Reference("primordial")
+    N = ref.N
+    out = {}
+
+    # -- per-cell evolve ----------------------------------------------------
+    for tag, cfg, n in (("c1", "config1", 64), ("c3", "config3", 64)):
+        st, dtf = primordial_cells(n, cfg)
+        r = ref.evolve_cells(st, dtf, nthreads=8)
+        out["evolve_%s_in" % tag] = st
+        out["evolve_%s_dtf" % tag] = dtf
+        for k in ("state", "atol", "dt", "ttot"):
+            out["evolve_%s_%s" % (tag, k)] = r[k]
+    st, dtf, dts = edge_cells()
+    r = ref.evolve_cells(st, dtf, dt=dts, nthreads=8)
+    out["evolve_edge_in"], out["evolve_edge_dtf"], out["evolve_edge_dt0"] = st, dtf, dts
+    for k in ("state", "atol", "dt", "ttot"):
+        out["evolve_edge_%s" % k] = r[k]
+
+    # -- strip functions ------------------------------------------------------
+    lib = ref.lib
+    d = lib.ref_setup()
+    st, _ = primordial_cells(32, "config1", seed=4242)
+    w = np.array([2.0, 2.0, 1.00794, 1.00794, 1.00794, 4.002602, 4.002602, 4.002602, 1.0, 0.0])
+    num = st.copy()
+    num[:, :9] /= w[:9] * 1.67e-24
+    out["strip_in"] = num.copy()
+    lib.ref_temperature(d, dp(num), 32, N)
+    out["strip_Ts"] = np.ctypeslib.as_array(lib.ref_Ts(d), (32,)).copy()
+    out["strip_dTs_ge"] = np.ctypeslib.as_array(lib.ref_dTs_ge(d), (32,)).copy()
+    lib.ref_interpolate(d, 32)
+    nt = 44
+    out["strip_rs"] = np.array([np.ctypeslib.as_array(lib.ref_rs(d, k), (32,)).copy()
+                                for k in range(nt)])
+    rhs = np.zeros_like(num)
+    out["strip_rhs_rv"] = np.array(lib.ref_rhs(dp(num), dp(rhs), 32, N, C.c_void_p(d)))
+    out["strip_rhs"] = rhs
+    jac = np.zeros((32, N, N))
+    out["strip_jac_rv"] = np.array(lib.ref_jac(dp(num), dp(jac), 32, N, C.c_void_p(d)))
+    out["strip_jac"] = jac
+    el = num.copy()
+    lib.ref_electrons(dp(el), 32, N)
+    out["strip_electrons"] = el
+
+    # -- BE_chem_solve over a strip (lockstep) -------------------------------
+    ns = 8
+    u = num[:ns].copy()
+    rtol = np.full_like(u, 1e-6)
+    atol = 1e-6 * u
+    scale = u.copy()
+    out["be_in"], out["be_atol_in"] = u.copy(), atol.copy()
+    out["be_dt"] = np.array(1e10)
+    scratch = [np.zeros(ns * N), np.zeros(N), np.zeros(ns * N), np.zeros(ns * N * N)]
+    rv = lib.ref_BE_chem_solve(dp(u), 1e10, dp(rtol), dp(atol), ns, N, dp(scale), C.c_void_p(d),
+                               *[dp(a) for a in scratch])
+    out["be_rv"], out["be_u"], out["be_atol"] = np.array(rv), u, atol
+
+    # -- dengo_evolve over a strip (lockstep dims = 8) -----------------------
+    st, dtf = primordial_cells(8, "config1", seed=99)
+    x = st.copy()
+    rt = np.full_like(x, 1e-6)
+    at = 1e-6 * x
+    dt = C.c_double(-1.0)
+    ttot = lib.ref_evolve(d, float(dtf.min()), C.byref(dt), -1.0, dp(x), dp(rt), dp(at), 8)
+    out["lock_in"], out["lock_dtf"] = st, np.array(dtf.min())
+    out["lock_state"], out["lock_atol"] = x, at
+    out["lock_ttot"], out["lock_dt"] = np.array(ttot), np.array(dt.value)
+
+    # -- tables ----------------------------------------------------------------
+    tdir = os.path.join(ROOT, "oracle", "_ref", "primordial", "primordial_tables.h5.d")
+    names = sorted(f[:-4] for f in os.listdir(tdir))
+    out["table_names"] = np.array(names)
+    out["tables"] = np.array([np.fromfile(os.path.join(tdir, f + ".f64")) for f in names])
+    np.savez_compressed(os.path.join(HERE, "primordial_golden.npz"), **out)
+
+    # -- expressions -----------------------------------------------------------
+    from dengo_gb300.codegen.spec import network_spec
+    from dengo_gb300.networks import primordial_network
+    spec = network_spec(primordial_network(), "primordial")
+    src = open(os.path.join(ROOT, "oracle", "_ref", "primordial", "primordial_solver.C")).read()
+    exprs = dict(rhs=spec.rhs_ref, jac=spec.jac_ref, T=spec.T_ref, Tge=spec.Tge_ref,
+                 density=spec.mass_density_ref, species=[s.name for s in spec.species],
+                 tables=[t.name for t in spec.tables])
+    for text in spec.rhs_ref + [e for col in spec.jac_ref for e in col] + \
+            [spec.T_ref, spec.Tge_ref, spec.mass_density_ref]:
+        assert text in src, "expression not found in the reference's rendered C: %s" % text
+    with open(os.path.join(HERE, "primordial_expressions.json"), "w") as f:
+        json.dump(exprs, f, indent=1)
+    print("wrote golden vectors to", HERE)
+
+
+if __name__ == "__main__":
+    main()

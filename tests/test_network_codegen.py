@@ -1,0 +1,109 @@
+"""Network API and code generation against the reference's expressions and
+tables (tests/golden/, produced from the reference's own rendering)."""
+import json
+import os
+import platform
+import tempfile
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def net():
+    from dengo_gb300.networks import primordial_network
+    return primordial_network()
+
+
+@pytest.fixture(scope="module")
+def spec(net):
+    from dengo_gb300.codegen.spec import network_spec
+    return network_spec(net, "primordial")
+
+
+@pytest.fixture(scope="module")
+def ref_exprs():
+    with open(os.path.join(ROOT, "tests", "golden", "primordial_expressions.json")) as f:
+        return json.load(f)
+
+
+def test_species_order(spec, ref_exprs):
+    assert [s.name for s in spec.species] == ref_exprs["species"]
+    assert [s.name for s in spec.species] == ["H2_1", "H2_2", "H_1", "H_2", "H_m0", "He_1",
+                                              "He_2", "He_3", "de", "ge"]
+
+
+def test_table_order(spec, ref_exprs):
+    assert [t.name for t in spec.tables] == ref_exprs["tables"]
+    assert len(spec.tables) == 44
+
+
+def test_rhs_and_jacobian_text_equal_reference(spec, ref_exprs):
+    assert spec.rhs_ref == ref_exprs["rhs"]
+    assert spec.jac_ref == ref_exprs["jac"]
+    assert spec.T_ref == ref_exprs["T"]
+    assert spec.Tge_ref == ref_exprs["Tge"]
+    assert spec.mass_density_ref == ref_exprs["density"]
+
+
+def test_ge_column_is_zero(spec):
+    # The reference's Jacobian has no rate-temperature terms (see
+    # reaction_classes.ReactionCoefficient).
+    ige = spec.ige
+    assert not any(spec.jac_nonzero[ige])
+    assert spec.nnz() == 54
+
+
+def test_device_text_has_same_operands(spec):
+    # The device printer only renames: strip "[i]", integer powers.
+    import re
+    for ref, dev in zip(spec.rhs_ref, spec.rhs_dev):
+        r = re.sub(r"pow\(([^,()]+), (\d)\)", r"dg_ipow<\2>(\1)", ref.replace("[i]", ""))
+        assert r.split("=", 1)[1] == dev.split("=", 1)[1]
+
+
+def test_tables_equal_reference(net, golden):
+    mine = net.rate_tables()
+    names = list(golden["table_names"])
+    for name, arr in mine.items():
+        ref = golden["tables"][names.index(name)]
+        if platform.machine() == "x86_64":
+            assert np.array_equal(arr.view(np.int64), ref.view(np.int64)), name
+        else:
+            assert np.allclose(arr, ref, rtol=1e-13, atol=0), name
+
+
+def test_generated_sources_up_to_date(net):
+    from dengo_gb300.codegen import render_solver
+    gen = os.path.join(ROOT, "dengo_gb300", "generated", "primordial")
+    with tempfile.TemporaryDirectory() as d:
+        for p in render_solver(net, "primordial", d):
+            with open(p) as f, open(os.path.join(gen, os.path.basename(p))) as g:
+                assert f.read() == g.read(), os.path.basename(p)
+
+
+def test_oracle_sources_up_to_date():
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gen_oracle
+    with open(os.path.join(ROOT, "oracle", "gen", "primordial_oracle.c")) as f:
+        assert f.read() == gen_oracle.render("primordial")
+
+
+def test_table_file_roundtrip(tmp_path):
+    from dengo_gb300.tablefile import read_table_file, write_table_file
+    d = {"a": np.arange(5.0), "b_c": np.array([1e-300, -0.0, np.inf])}
+    write_table_file(str(tmp_path / "t.dgt"), d)
+    r = read_table_file(str(tmp_path / "t.dgt"))
+    assert set(r) == {"a", "b_c"}
+    assert np.array_equal(r["b_c"].view(np.int64), d["b_c"].view(np.int64))
+
+
+def test_write_solver_writes_all_outputs(net, tmp_path):
+    init = {s: np.ones(3) for s in net.species_list()}
+    paths = net.write_solver("demo", output_dir=str(tmp_path), init_values=init)
+    names = sorted(os.path.basename(p) for p in paths)
+    assert names == ["demo_initial_conditions.dgt", "demo_solver.cu", "demo_solver.h",
+                     "demo_tables.dgt"]

@@ -1,0 +1,48 @@
+"""The oracle (C restatement) against the reference's own outputs.
+
+The golden vectors were produced by the reference's generated solver
+(tests/golden/make_golden.py).  On the machine that made them the oracle
+must agree bit for bit; elsewhere (another libm) to 1e-12 relative.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+BITWISE = platform.machine() == "x86_64"
+
+
+def _same(a, b, rtol=1e-12):
+    if BITWISE:
+        return np.array_equal(np.asarray(a).view(np.int64), np.asarray(b).view(np.int64))
+    with np.errstate(invalid="ignore"):
+        return np.allclose(a, b, rtol=rtol, atol=0, equal_nan=True)
+
+
+@pytest.mark.parametrize("tag", ["c1", "c3", "edge"])
+def test_oracle_matches_reference_per_cell(golden, tables_in_order, oracle, tag):
+    g = golden
+    dt0 = g.get("evolve_%s_dt0" % tag)
+    r = oracle.evolve_cells(tables_in_order, g["evolve_%s_in" % tag], g["evolve_%s_dtf" % tag],
+                            dt=dt0, nthreads=4)
+    for k in ("state", "atol", "dt", "ttot"):
+        assert _same(r[k], g["evolve_%s_%s" % (tag, k)]), k
+
+
+def test_oracle_statuses_cover_all_outcomes(golden, tables_in_order, oracle):
+    r = oracle.evolve_cells(tables_in_order, golden["evolve_c1_in"], golden["evolve_c1_dtf"],
+                            nthreads=4)
+    assert set(np.unique(r["status"])) == {0, 1, 2}
+    ok = r["status"] == 0
+    assert np.all(r["ttot"][ok] >= golden["evolve_c1_dtf"][ok])
+    assert np.all(r["substeps"][r["status"] == 1] == 50000)
+
+
+def test_edge_cases_behave_like_reference(golden, tables_in_order, oracle):
+    g = golden
+    r = oracle.evolve_cells(tables_in_order, g["evolve_edge_in"], g["evolve_edge_dtf"],
+                            dt=g["evolve_edge_dt0"], nthreads=1)
+    assert r["ttot"][0] == 0.0 and r["substeps"][0] == 0          # dtf = 0
+    assert r["status"][1] == 2                                     # negative density
+    assert r["status"][2] == 2                                     # zero density -> NaN
+    assert np.array_equal(r["state"][0], g["evolve_edge_in"][0])  # untouched state
