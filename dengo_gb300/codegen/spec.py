@@ -12,6 +12,7 @@ Orders follow the reference's generated code exactly:
   (rates_and_rate_tables.C.template:578-594).
 """
 
+import re
 from dataclasses import dataclass, field
 
 import sympy
@@ -58,6 +59,8 @@ class NetworkSpec:
     T_dev: str
     Tge_ref: str
     Tge_dev: str
+    T_dev_div: str       # T_dev with x/(gamma - 1.0) as dg_div(x, gm1, rgm1)
+    Tge_dev_div: str
     rhs_ref: list        # per species, "rhs[j] = ...;"
     rhs_dev: list        # per species, "f[k] = ...;"
     jac_ref: list        # [var][eq] "Joutput[j] = ...;"
@@ -87,6 +90,14 @@ class NetworkSpec:
 
     def nnz(self):
         return sum(sum(1 for v in col if v) for col in self.jac_nonzero)
+
+
+_GAMMA_DIV = re.compile(r"\b([A-Za-z_][A-Za-z0-9_]*)/\(gamma - 1\.0\)")
+
+
+def gamma_div(text):
+    """Rewrite ``x/(gamma - 1.0)`` as ``dg_div(x, gm1, rgm1)`` (same value)."""
+    return _GAMMA_DIV.sub(r"dg_div(\1, gm1, rgm1)", text)
 
 
 def _lit(v):
@@ -141,5 +152,6 @@ def network_spec(net, name):
         mass_density_ref=ccode_ref(md), mass_density_dev=ccode_device(md),
         T_ref=ccode_ref(T), T_dev=ccode_device(T),
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),
+        T_dev_div=gamma_div(ccode_device(T)), Tge_dev_div=gamma_div(ccode_device(Tg)),
         rhs_ref=rhs_ref, rhs_dev=rhs_dev,
         jac_ref=jac_ref, jac_dev=jac_dev, jac_nonzero=jac_nz)

@@ -65,7 +65,30 @@ struct Gpu {
     double z_loaded = NAN;
     char *d_buf = nullptr;
     size_t d_cap = 0;
+    int *order = nullptr;         /* cell order built from a cost hint */
+    long long order_cap = 0;
+    int *order_counts = nullptr;  /* [64]: bucket counts and offsets */
 };
+
+/* Builds g->order (longest first) from the per-cell cost hint on stream st. */
+inline int build_order(Gpu *g, const int *cost, long long n, cudaStream_t st)
+{
+    if (n > g->order_cap) {
+        if (g->order) cudaFree(g->order);
+        g->order = nullptr;
+        g->order_cap = 0;
+        DG_CUDA(cudaMalloc(&g->order, sizeof(int) * n));
+        g->order_cap = n;
+    }
+    if (!g->order_counts) DG_CUDA(cudaMalloc(&g->order_counts, sizeof(int) * 64));
+    DG_CUDA(cudaMemsetAsync(g->order_counts, 0, sizeof(int) * 64, st));
+    const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+    order_count_kernel<<<grid, 256, 0, st>>>(cost, n, g->order_counts);
+    order_scan_kernel<<<1, 1, 0, st>>>(g->order_counts, g->order_counts + 32);
+    order_scatter_kernel<<<grid, 256, 0, st>>>(cost, n, g->order_counts + 32, g->order);
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
 
 inline int ensure_device_buf(Gpu *g, size_t bytes)
 {
@@ -268,6 +291,8 @@ struct Api {
             cudaFreeHost(g->h_zv);
             cudaFree(g->queue);
             cudaFree(g->d_buf);
+            cudaFree(g->order);
+            cudaFree(g->order_counts);
             if (g->stream) cudaStreamDestroy(g->stream);
             delete g;
         }
@@ -318,7 +343,8 @@ struct Api {
             return -1;
         }
         Gpu *g = gpu(d);
-        cudaStream_t st = stream ? (cudaStream_t)stream : g->stream;
+        /* NULL is the default stream, as everywhere in CUDA */
+        cudaStream_t st = (cudaStream_t)stream;
         if (load_z(d, z, st) != 0) return -1;
         CellIO io{};
         io.state = b->state;
@@ -336,6 +362,11 @@ struct Api {
         io.cs = b->cell_stride;
         io.ss = b->species_stride;
         io.ncells = b->ncells;
+        io.order = nullptr;
+        if (b->cost_hint && b->ncells > 0) {
+            if (build_order(g, b->cost_hint, b->ncells, st) != 0) return -1;
+            io.order = g->order;
+        }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         g->ts.z = z;
         switch (cfg.block) {
@@ -380,6 +411,7 @@ struct Api {
         b.substeps = hb->substeps ? sub : nullptr;
         b.sweeps = hb->sweeps ? swp : nullptr;
         b.failures = hb->failures ? fai : nullptr;
+        b.cost_hint = nullptr;
         auto h2d = [&](void *dst, const void *src, size_t bytes) {
             return src ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
         };

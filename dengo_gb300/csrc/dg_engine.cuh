@@ -58,6 +58,7 @@ struct CellIO {
     double *ttot;
     int *status;
     int *substeps, *sweeps, *failures;
+    const int *order;       /* optional: the q-th cell taken is order[q] */
     long long cs, ss;
     long long ncells;
 };
@@ -170,13 +171,106 @@ __device__ __forceinline__ void gauss_elim(Slots<BLOCK> J, double (&x)[N])
     }
 }
 
+/* Gauss_Elim with the same result, fewer FP64 operations.
+ *
+ * Every entry the reference changes is computed with the reference's
+ * operations in the reference's order, except that
+ *   - a quotient by the pivot is formed as dg_div(a, piv, 1/piv), which is
+ *     the correctly rounded a/piv, i.e. the reference's division;
+ *   - an update a - m*b is skipped when m or b is an exact zero and the other
+ *     factor is finite: then m*b is a zero and a - (+-0) == a (only the sign
+ *     of an exactly-zero entry can differ, which no later comparison or
+ *     nonzero result depends on).
+ * The finiteness tests are per elimination step, so a row or multiplier set
+ * holding inf/NaN is updated densely, exactly as the reference does. */
+template <int N, int BLOCK>
+__device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
+{
+    double piv_v[N], piv_r[N];
+#pragma unroll
+    for (int k = 0; k < N - 1; k++) {
+        int p = k;
+        double best = fabs(J[k * N + k]);
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            const double a = fabs(J[k * N + i]);
+            if (a > best) {
+                best = a;
+                p = i;
+            }
+        }
+        if (p != k) {
+            for (int j = k; j < N; j++) {
+                const double t = J[j * N + k];
+                J[j * N + k] = J[j * N + p];
+                J[j * N + p] = t;
+            }
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                if (i == p) {
+                    const double t = x[k];
+                    x[k] = x[i];
+                    x[i] = t;
+                }
+            }
+        }
+        const double piv = J[k * N + k];
+        const double rp = 1.0 / piv;
+        piv_v[k] = piv;
+        piv_r[k] = rp;
+        double m[N], row[N];
+        bool mfin = true, rowfin = true;
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            m[i] = dg_div(J[k * N + i], piv, rp);
+            J[k * N + i] = m[i];
+            mfin = mfin && dg_finite(m[i]);
+        }
+#pragma unroll
+        for (int j = k + 1; j < N; j++) {
+            row[j] = J[j * N + k];
+            rowfin = rowfin && dg_finite(row[j]);
+        }
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            if (m[i] != 0.0 || !rowfin) {
+#pragma unroll
+                for (int j = k + 1; j < N; j++) {
+                    if (row[j] != 0.0 || !mfin) J[j * N + i] = J[j * N + i] - m[i] * row[j];
+                }
+            }
+        }
+        const double xk = x[k];
+        const bool xfin = dg_finite(xk);
+#pragma unroll
+        for (int i = k + 1; i < N; i++)
+            if (m[i] != 0.0 || !xfin) x[i] = x[i] - m[i] * xk;
+    }
+    piv_v[N - 1] = J[(N - 1) * N + (N - 1)];
+    piv_r[N - 1] = 1.0 / piv_v[N - 1];
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
+        double xi = x[i];
+#pragma unroll
+        for (int j = i + 1; j < N; j++) {
+            const double aij = J[j * N + i];
+            if (aij != 0.0 || !dg_finite(x[j])) xi = xi - aij * x[j];
+        }
+        x[i] = dg_div(xi, piv_v[i], piv_r[i]);
+    }
+}
+
 /* Stores one Jacobian entry already transformed as BE_Resid_Jac does:
  * row scale 1/scale_eq, column scale scale_var, then -dt*J, +1 on the
- * diagonal (BE_chem_solve.C:301-318). */
+ * diagonal (BE_chem_solve.C:301-318).  zero() stores a structural zero:
+ * when every scale is a positive finite number and dt > 0 the reference's
+ * ((0 * inv) * scale) * -dt is -0.0 (1.0 on the diagonal), written directly;
+ * otherwise (dense) the operations are carried out. */
 template <int N, int BLOCK>
 struct JacPut {
     Slots<BLOCK> J, INV, SC;
     double mdt;
+    bool dense;
     __device__ __forceinline__ void operator()(int q, int v, double jv) const
     {
         double a = jv * INV[q];
@@ -184,6 +278,11 @@ struct JacPut {
         a = mdt * a;
         if (q == v) a = a + 1.0;
         J[v * N + q] = a;
+    }
+    __device__ __forceinline__ void zero(int q, int v) const
+    {
+        if (dense) operator()(q, v, 0.0);
+        else J[v * N + q] = (q == v) ? 1.0 : -0.0;
     }
 };
 
@@ -220,8 +319,9 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
     const Slots<BLOCK> RT{base + L::OFF_RT * BLOCK};
 
     const long long stride = (long long)gridDim.x * BLOCK;
-    long long cell = queue ? (long long)atomicAdd(queue, 1ull)
-                           : (long long)blockIdx.x * BLOCK + tid;
+    long long qi = queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * BLOCK + tid;
+    long long cell = 0;
+    bool dense = false;   /* a scale is not a positive finite number */
 
     double u[N], u0[N], y[N];
     double dtf = 0, dt = 0, ttot = 0;
@@ -259,11 +359,13 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         siter = 0;
         nsweeps = 0;
         nfail = 0;
+        dense = false;
 #pragma unroll
         for (int s = 0; s < N; s++) {
             SC[s] = y[s];
             PREV[s] = y[s];
             INV[s] = 1.0 / y[s];
+            dense = dense || !(y[s] > 0.0 && dg_finite(y[s]));
         }
         if (!(ttot < dtf)) return false;
         substep_begin();
@@ -289,13 +391,14 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         if (io.failures) io.failures[cell] = nfail;
     };
     auto fetch = [&]() {
-        while (cell < io.ncells) {
+        while (qi < io.ncells) {
+            cell = io.order ? (long long)io.order[qi] : qi;
             if (cell_begin()) {
                 active = true;
                 return;
             }
             cell_end(ST_OK);
-            cell = queue ? (long long)atomicAdd(queue, 1ull) : cell + stride;
+            qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
         }
         active = false;
     };
@@ -323,12 +426,12 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 /* BE_Resid_Jac (BE_chem_solve.C:280-321) */
 #pragma unroll
                 for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
-                JacPut<N, BLOCK> put{J, INV, SC, -dt};
+                JacPut<N, BLOCK> put{J, INV, SC, -dt, dense || !(dt > 0.0)};
                 ok = Net::jac(y, R, Tge, T, ts.z, put);
                 if (ok) {
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
-                    gauss_elim<N, BLOCK>(J, f);
+                    gauss_elim_fast<N, BLOCK>(J, f);
                     /* Newton update and max-norm test (BE_chem_solve.C:173-206) */
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = u[i] - 1.0 * f[i];
@@ -393,7 +496,7 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
             continue;
         }
         cell_end(done);
-        cell = queue ? (long long)atomicAdd(queue, 1ull) : cell + stride;
+        qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
         fetch();
     }
 }

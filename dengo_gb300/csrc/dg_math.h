@@ -128,6 +128,38 @@ DG_HD double dg_log(double x)
     return s2 + low;
 }
 
+/* Binary exponent field of x (0 for zero/subnormal, 0x7FF for inf/NaN). */
+DG_HD int dg_expo(double x) { return (int)((dg_bits(x) >> 52) & 0x7FF); }
+
+DG_HD bool dg_finite(double x) { return dg_expo(x) != 0x7FF; }
+
+/* Divisor in the range where dg_div's fast path applies. */
+DG_HD bool dg_div_ok(double b)
+{
+    const int e = dg_expo(b);
+    return e >= 150 && e <= 1900;
+}
+
+/* a / b, correctly rounded, given rb = 1.0 / b (correctly rounded).
+ * Markstein's quotient theorem (P. Markstein, "Computation of elementary
+ * functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+ * 1990): with q = RN(a rb) and the exact remainder r = a - b q from one
+ * fma, RN(q + r rb) = RN(a/b), provided no intermediate leaves the normal
+ * range.  The exponent guard keeps |a|, |b| in [2^-873, 2^877] and their
+ * ratio within 2^800, which keeps q and r normal; every other operand
+ * (zero, subnormal, huge, inf, NaN) takes the plain division.  One reciprocal
+ * then serves all quotients by the same divisor at 3 FP64 operations each. */
+DG_HD double dg_div(double a, double b, double rb)
+{
+    const int ea = dg_expo(a), eb = dg_expo(b), d = ea - eb;
+    if (ea >= 150 && ea <= 1900 && eb >= 150 && eb <= 1900 && d >= -800 && d <= 800) {
+        const double q = a * rb;
+        const double r = dg_fma(-b, q, a);
+        return dg_fma(r, rb, q);
+    }
+    return a / b;
+}
+
 /* x^n, n >= 2: the exact power rounded once (up to ~2^-100 relative error
  * before that rounding). */
 template <int n>

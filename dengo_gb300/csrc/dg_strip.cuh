@@ -132,6 +132,7 @@ struct PlainPut {
     double *J;
     int N;
     __device__ __forceinline__ void operator()(int q, int v, double jv) const { J[v * N + q] = jv; }
+    __device__ __forceinline__ void zero(int q, int v) const { J[v * N + q] = 0.0; }
 };
 
 template <class Net>
@@ -174,6 +175,45 @@ __global__ void strip_temperature_from_mass_kernel(const double *in, int nstrip,
     T[c] = Net::temperature_from_mass_density(y);
 }
 
+/* Longest-first cell order from a per-cell cost hint (e.g. the sweeps the
+ * cell needed in the previous hydro step): 32 buckets by floor(log2(cost+1)),
+ * costliest bucket first; the order inside a bucket is arbitrary (results do
+ * not depend on it).  counts/offsets hold 32 ints each, zeroed by the caller. */
+__device__ __forceinline__ int cost_bucket(int c)
+{
+    const unsigned v = (unsigned)(c < 0 ? 0 : c) + 1u;
+    return __clz(v);   /* 31 - floor(log2 v): big costs get small buckets */
+}
+
+__global__ void order_count_kernel(const int *cost, long long n, int *counts)
+{
+    __shared__ int sc[32];
+    if (threadIdx.x < 32) sc[threadIdx.x] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&sc[cost_bucket(cost[i])], 1);
+    __syncthreads();
+    if (threadIdx.x < 32 && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
+}
+
+__global__ void order_scan_kernel(const int *counts, int *offsets)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int run = 0;
+    for (int b = 0; b < 32; b++) {
+        offsets[b] = run;
+        run += counts[b];
+    }
+}
+
+__global__ void order_scatter_kernel(const int *cost, long long n, int *offsets, int *order)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        order[atomicAdd(&offsets[cost_bucket(cost[i])], 1)] = (int)i;
+}
+
 /* Scaled Jacobian store into a per-thread array (BE_chem_solve.C:301-318). */
 template <int N>
 struct ScaledLocalPut {
@@ -188,6 +228,7 @@ struct ScaledLocalPut {
         if (q == v) a = a + 1.0;
         J[v * N + q] = a;
     }
+    __device__ __forceinline__ void zero(int q, int v) const { operator()(q, v, 0.0); }
 };
 
 template <int N>

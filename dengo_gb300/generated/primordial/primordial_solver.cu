@@ -227,6 +227,10 @@ struct Net {
         const double gamma = 5.e0/3.e0;
         const double gammaH2 = 7.e0/5.e0;
         (void)gammaH2;
+        /* x/(gamma - 1.0) is evaluated as dg_div(x, gm1, 1/gm1): the same
+         * correctly rounded quotient */
+        const double gm1 = gamma - 1.0;
+        const double rgm1 = 1.0 / gm1;
         const double H2_1 = y[0];
         const double H2_2 = y[1];
         const double H_1 = y[2];
@@ -238,14 +242,14 @@ struct Net {
         const double de = y[8];
         const double ge = y[9];
         const double density = 2.0*H2_1 + 2.0*H2_2 + 1.0079400000000001*H_1 + 1.0079400000000001*H_2 + 1.0079400000000001*H_m0 + 4.0026020000000004*He_1 + 4.0026020000000004*He_2 + 4.0026020000000004*He_3;
-        double Tv = density*ge*mh/(kb*(H2_1/(gamma - 1.0) + H2_2/(gamma - 1.0) + H_1/(gamma - 1.0) + H_2/(gamma - 1.0) + H_m0/(gamma - 1.0) + He_1/(gamma - 1.0) + He_2/(gamma - 1.0) + He_3/(gamma - 1.0) + de/(gamma - 1.0)));
+        double Tv = density*ge*mh/(kb*(dg_div(H2_1, gm1, rgm1) + dg_div(H2_2, gm1, rgm1) + dg_div(H_1, gm1, rgm1) + dg_div(H_2, gm1, rgm1) + dg_div(H_m0, gm1, rgm1) + dg_div(He_1, gm1, rgm1) + dg_div(He_2, gm1, rgm1) + dg_div(He_3, gm1, rgm1) + dg_div(de, gm1, rgm1)));
         if (Tv < Tlo) {
             Tv = Tlo;
         } else if (Tv > Thi) {
             Tv = Thi;
         }
         T = Tv;
-        Tge = density*mh/(kb*(H2_1/(gamma - 1.0) + H2_2/(gamma - 1.0) + H_1/(gamma - 1.0) + H_2/(gamma - 1.0) + H_m0/(gamma - 1.0) + He_1/(gamma - 1.0) + He_2/(gamma - 1.0) + He_3/(gamma - 1.0) + de/(gamma - 1.0)));
+        Tge = density*mh/(kb*(dg_div(H2_1, gm1, rgm1) + dg_div(H2_2, gm1, rgm1) + dg_div(H_1, gm1, rgm1) + dg_div(H_2, gm1, rgm1) + dg_div(H_m0, gm1, rgm1) + dg_div(He_1, gm1, rgm1) + dg_div(He_2, gm1, rgm1) + dg_div(He_3, gm1, rgm1) + dg_div(de, gm1, rgm1)));
     }
 
     /* rates_and_rate_tables.C.template:635-668 */
@@ -484,7 +488,8 @@ struct Net {
         const double zero_row = 0.0 / mdensity;  /* a structural zero of the ge row */
         const double zero_col = 0.0 * Tge;       /* a structural zero of the ge column */
         const double zero_both = zero_row * Tge;
-        (void)zero_row; (void)zero_col; (void)zero_both;
+        const double rmd = 1.0 / mdensity;
+        (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
         jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
         put(0, 0, jv);
@@ -494,13 +499,13 @@ struct Net {
         put(2, 0, jv);
         jv = -k11*H_2 + 2*k12*de;
         put(3, 0, jv);
-        put(4, 0, 0.0);
-        put(5, 0, 0.0);
-        put(6, 0, 0.0);
-        put(7, 0, 0.0);
-        put(8, 0, 0.0);
+        put.zero(4, 0);
+        put.zero(5, 0);
+        put.zero(6, 0);
+        put.zero(7, 0);
+        put.zero(8, 0);
         jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0);
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 0, jv);
         jv = k10*H_1 + k19*H_m0;
         put(0, 1, jv);
@@ -512,9 +517,9 @@ struct Net {
         put(3, 1, jv);
         jv = -k19*H_m0;
         put(4, 1, jv);
-        put(5, 1, 0.0);
-        put(6, 1, 0.0);
-        put(7, 1, 0.0);
+        put.zero(5, 1);
+        put.zero(6, 1);
+        put.zero(7, 1);
         jv = -k18*de;
         put(8, 1, jv);
         put(9, 1, zero_row);
@@ -528,13 +533,13 @@ struct Net {
         put(3, 2, jv);
         jv = k07*de - k08*H_m0 - k15*H_m0;
         put(4, 2, jv);
-        put(5, 2, 0.0);
-        put(6, 2, 0.0);
-        put(7, 2, 0.0);
+        put.zero(5, 2);
+        put.zero(6, 2);
+        put.zero(7, 2);
         jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
         put(8, 2, jv);
         jv = -H2_1*gloverabel08_gaHI*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H2_1*h2formation_h2mcool + 3*dg_ipow<2>(H_1)*h2formation_h2mheat - ceHI_ceHI*de - ciHI_ciHI*de;
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 2, jv);
         jv = -k11*H2_1;
         put(0, 3, jv);
@@ -546,13 +551,13 @@ struct Net {
         put(3, 3, jv);
         jv = -k16*H_m0 - k17*H_m0;
         put(4, 3, jv);
-        put(5, 3, 0.0);
-        put(6, 3, 0.0);
-        put(7, 3, 0.0);
+        put.zero(5, 3);
+        put.zero(6, 3);
+        put.zero(7, 3);
         jv = -k02*de + k17*H_m0;
         put(8, 3, jv);
         jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 3, jv);
         jv = k08*H_1 + k19*H2_2;
         put(0, 4, jv);
@@ -564,32 +569,32 @@ struct Net {
         put(3, 4, jv);
         jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
         put(4, 4, jv);
-        put(5, 4, 0.0);
-        put(6, 4, 0.0);
-        put(7, 4, 0.0);
+        put.zero(5, 4);
+        put.zero(6, 4);
+        put.zero(7, 4);
         jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
         put(8, 4, jv);
         put(9, 4, zero_row);
-        put(0, 5, 0.0);
-        put(1, 5, 0.0);
-        put(2, 5, 0.0);
-        put(3, 5, 0.0);
-        put(4, 5, 0.0);
+        put.zero(0, 5);
+        put.zero(1, 5);
+        put.zero(2, 5);
+        put.zero(3, 5);
+        put.zero(4, 5);
         jv = -k03*de;
         put(5, 5, jv);
         jv = k03*de;
         put(6, 5, jv);
-        put(7, 5, 0.0);
+        put.zero(7, 5);
         jv = k03*de;
         put(8, 5, jv);
         jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 5, jv);
-        put(0, 6, 0.0);
-        put(1, 6, 0.0);
-        put(2, 6, 0.0);
-        put(3, 6, 0.0);
-        put(4, 6, 0.0);
+        put.zero(0, 6);
+        put.zero(1, 6);
+        put.zero(2, 6);
+        put.zero(3, 6);
+        put.zero(4, 6);
         jv = k04*de;
         put(5, 6, jv);
         jv = -k04*de - k05*de;
@@ -599,14 +604,14 @@ struct Net {
         jv = -k04*de + k05*de;
         put(8, 6, jv);
         jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 6, jv);
-        put(0, 7, 0.0);
-        put(1, 7, 0.0);
-        put(2, 7, 0.0);
-        put(3, 7, 0.0);
-        put(4, 7, 0.0);
-        put(5, 7, 0.0);
+        put.zero(0, 7);
+        put.zero(1, 7);
+        put.zero(2, 7);
+        put.zero(3, 7);
+        put.zero(4, 7);
+        put.zero(5, 7);
         jv = k06*de;
         put(6, 7, jv);
         jv = -k06*de;
@@ -614,7 +619,7 @@ struct Net {
         jv = -k06*de;
         put(8, 7, jv);
         jv = -4.0*brem_brem*de - de*reHeIII_reHeIII;
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 7, jv);
         jv = -k12*H2_1;
         put(0, 8, jv);
@@ -635,7 +640,7 @@ struct Net {
         jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
         put(8, 8, jv);
         jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0*He_3);
-        jv /= mdensity;
+        jv = dg_div(jv, mdensity, rmd);
         put(9, 8, jv);
         put(0, 9, zero_col);
         put(1, 9, zero_col);

@@ -38,7 +38,7 @@ class CellBatch(C.Structure):
                 ("atol", C.c_void_p), ("rtol", C.c_void_p), ("rtol_scalar", C.c_double),
                 ("dtf", C.c_void_p), ("dtf_scalar", C.c_double), ("dt", C.c_void_p),
                 ("ttot", C.c_void_p), ("status", C.c_void_p), ("substeps", C.c_void_p),
-                ("sweeps", C.c_void_p), ("failures", C.c_void_p)]
+                ("sweeps", C.c_void_p), ("failures", C.c_void_p), ("cost_hint", C.c_void_p)]
 
 
 def _ptr(x):
@@ -172,11 +172,11 @@ class Solver:
     def solve_device(self, state, ncells, cell_stride, species_stride, atol, rtol=None,
                      rtol_scalar=1e-6, dtf=None, dtf_scalar=0.0, dt=None, ttot=None,
                      status=None, substeps=None, sweeps=None, failures=None, z=-1.0,
-                     config=None, stream=None):
+                     config=None, stream=None, cost_hint=None):
         """``<name>_solve_cells_device``: asynchronous on ``stream``."""
         b = CellBatch(ncells, cell_stride, species_stride, _ptr(state), _ptr(atol), _ptr(rtol),
                       rtol_scalar, _ptr(dtf), dtf_scalar, _ptr(dt), _ptr(ttot), _ptr(status),
-                      _ptr(substeps), _ptr(sweeps), _ptr(failures))
+                      _ptr(substeps), _ptr(sweeps), _ptr(failures), _ptr(cost_hint))
         cfg = config or self.default_config()
         if stream is not None and not isinstance(stream, int):
             stream = stream.cuda_stream

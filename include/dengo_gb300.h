@@ -101,7 +101,12 @@ void dengo_default_config(dengo_solver_config *cfg);
  * rtol: may be NULL, then rtol_scalar applies to every element.
  * dtf: per-cell target time, or NULL for dtf_scalar.
  * dt: per-cell initial step in / last step out (< 0 selects dtf/1e5), or NULL.
- * ttot, status, substeps, sweeps, failures: per-cell outputs, each may be NULL. */
+ * ttot, status, substeps, sweeps, failures: per-cell outputs, each may be NULL.
+ * cost_hint: optional per-cell estimate of the work (e.g. the sweeps array of
+ * the previous hydro step); cells are then started costliest first, which
+ * packs the stiff cells into full warps.  Results do not depend on it.
+ * <n>_solve_cells_device runs asynchronously on `stream` (a cudaStream_t;
+ * NULL is the default stream, as everywhere in CUDA). */
 typedef struct dengo_cell_batch {
     long long ncells;
     long long cell_stride;
@@ -118,6 +123,7 @@ typedef struct dengo_cell_batch {
     int *substeps;
     int *sweeps;
     int *failures;
+    const int *cost_hint;
 } dengo_cell_batch;
 
 typedef int (*rhs_f)(double *, double *, int, int, void *);

@@ -1,0 +1,59 @@
+"""The C-ABI libraries load without a GPU and export every entry point
+include/dengo_gb300.h declares (no compute call is made here)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(network):
+    text = open(os.path.join(ROOT, "include", "dengo_gb300.h")).read()
+    macro = text[text.index("#define DENGO_DECLARE_NETWORK"):]
+    macro = macro[:macro.index("/* The unprefixed")]
+    names = set(re.findall(r"\b(n##_\w+|\w+_##n|\w+##_##n)\s*\(", macro))
+    out = set()
+    for nm in names:
+        out.add(nm.replace("n##_", network + "_").replace("_##n", "_" + network)
+                .replace("##", ""))
+    out |= {"ensure_electron_consistency", "temperature_from_mass_density", "BE_chem_solve",
+            "dengo_default_config"}
+    return out
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    from dengo_gb300.build import build_network, library_path
+    p = library_path("primordial")
+    if not os.path.exists(p):
+        build_network("primordial")
+    return p
+
+
+def test_every_declared_symbol_is_exported(libpath):
+    want = declared("primordial")
+    assert "dengo_evolve_primordial" in want and "primordial_solve_cells_device" in want
+    nm = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True,
+                        text=True).stdout
+    have = {line.split()[-1] for line in nm.splitlines()}
+    missing = sorted(want - have)
+    assert not missing, missing
+
+
+def test_library_loads_without_gpu(libpath):
+    lib = C.CDLL(libpath)
+    lib.primordial_nspecies.restype = C.c_int
+    assert lib.primordial_nspecies() == 10
+    lib.primordial_ntables.restype = C.c_int
+    assert lib.primordial_ntables() == 44
+    lib.primordial_species_name.restype = C.c_char_p
+    assert lib.primordial_species_name(9) == b"ge"
+
+
+def test_runtime_fails_loudly_without_library(tmp_path):
+    from dengo_gb300.runtime import load_library
+    with pytest.raises(RuntimeError, match="not built"):
+        load_library("primordial", path=str(tmp_path / "missing.so"))
