@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--parity-sample", type=int, default=48)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--order", type=int, default=1, help="start the costliest cells first")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--warps-per-cell", type=int, default=1, choices=[1, 2, 4])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -99,6 +102,15 @@ class Clocks:
                     reasons.add(name)
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(rows[0][2]),
                 "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def temperatures(state):
+    """Gas temperature of each cell (mass densities + ge), gamma = 5/3."""
+    from dengo_gb300.workloads import KB, MH, PRIMORDIAL_ORDER, PRIMORDIAL_WEIGHTS
+    w = np.array([PRIMORDIAL_WEIGHTS[s] for s in PRIMORDIAL_ORDER[:-1]])
+    n = state[:, :-1] / (w * MH)
+    density = (n[:, :-1] * w[:-1]).sum(axis=1)
+    return density * state[:, -1] * MH / (KB * 1.5 * n.sum(axis=1))
 
 
 def measure_fp64_peak():
@@ -208,6 +220,8 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     cfg = Solver.default_config()
     cfg.schedule, cfg.block = args.schedule, args.block
+    cfg.precision = 1 if args.precision == "mixed" else 0
+    cfg.warps_per_cell = args.warps_per_cell
 
     def device_batch(st_host):
         st = torch.tensor(np.ascontiguousarray(st_host.T), device=dev)   # SoA: [species][cell]
@@ -234,6 +248,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     del wst, wat
 
+    t_hint = torch.tensor(np.minimum(temperatures(state0), 2e9).astype(np.int32), device=dev)
     ok_count = torch.zeros((), dtype=torch.int64, device=dev)
     sweep_sum = torch.zeros((), dtype=torch.int64, device=dev)
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -251,8 +266,11 @@ def run_ours(args):
         flush.zero_()
         torch.mul(st, 1e-6, out=at)
         ev0[k].record(stream)
+        # longest-first order: the previous step's sweep counts, or for the
+        # first step the initial temperature (the stiff cells are the hot ones)
         solver.solve_device(st, n, 1, n, at, rtol_scalar=1e-6, dtf=d_dtf, status=status,
-                            sweeps=sweeps, config=cfg, stream=stream)
+                            sweeps=sweeps, config=cfg, stream=stream,
+                            cost_hint=(t_hint if k == 0 else sweeps) if args.order else None)
         ev1[k].record(stream)
         ok_count += (status == 0).sum()
         sweep_sum += sweeps.sum(dtype=torch.int64)
@@ -305,14 +323,19 @@ def run_ours(args):
     peak = measure_fp64_peak()
     achieved = flops / (total_ms / 1e3) / 1e12
     line = {
-        "metric": "converged cell-steps/s (primordial, per-cell BE Newton, FP64 plain path)",
+        "metric": "converged cell-steps/s (primordial, per-cell BE Newton, %s path)"
+                  % ("FP64 plain" if args.precision == "fp64" else "mixed FP32-LU"),
         "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64 residual + f32 LU",
+        "data": "synthetic (seeded)",
         "config": {"workload": "primordial network, %d cells per GPU drawn from the 128^3 "
                                "configuration's distributions, %d consecutive hydro steps, "
                                "state resident on the device" % (n, args.steps),
-                   "cells_per_gpu": n, "precision": "fp64", "schedule": args.schedule,
+                   "cells_per_gpu": n, "precision": args.precision, "schedule": args.schedule,
+                   "order": "costliest first" if args.order else "input order",
+                   "warps_per_cell": args.warps_per_cell,
                    "l2": "flushed (256 MB write) before every step",
                    "warmup": "%d steps over a %d-cell copy" % (args.warmup, wn)},
         "wall_s": wall, "step_ms": step_ms, "gpu_launches": args.steps,

@@ -66,6 +66,11 @@ class NetworkSpec:
     jac_ref: list        # [var][eq] "Joutput[j] = ...;"
     jac_dev: list        # [var][eq] device statement or None for a structural zero
     jac_nonzero: list = field(default_factory=list)   # [var][eq] bool
+    # Work split of one Newton sweep over NP cooperating warps: part index of
+    # every RHS row and every Jacobian entry, {NP: ...}, balanced by sympy
+    # operation count (longest-first greedy).
+    rhs_part: dict = field(default_factory=dict)      # {NP: [part per row]}
+    jac_part: dict = field(default_factory=dict)      # {NP: [var][eq] part}
 
     @property
     def N(self):
@@ -100,6 +105,18 @@ def gamma_div(text):
     return _GAMMA_DIV.sub(r"dg_div(\1, gm1, rgm1)", text)
 
 
+def balance(costs, nparts):
+    """Part index for each item: longest-first greedy onto the least-loaded
+    part (ties to the lowest part), so parts carry similar operation counts."""
+    load = [0.0] * nparts
+    part = [0] * len(costs)
+    for i in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        p = min(range(nparts), key=lambda k: (load[k], k))
+        part[i] = p
+        load[p] += costs[i]
+    return part
+
+
 def _lit(v):
     """The text Jinja prints for a Python number (``str``), as the reference's
     templates do for weights, charges and bounds."""
@@ -126,7 +143,8 @@ def network_spec(net, name):
         e = net.rhs_expression(s)
         rhs_ref.append(ccode_ref(e, assign_to=sympy.Symbol("rhs[j]")))
         rhs_dev.append(ccode_device(e, assign_to=sympy.Symbol("f[%d]" % i)))
-    jac_ref, jac_dev, jac_nz = [], [], []
+    rhs_cost = [float(sympy.count_ops(net.rhs_expression(s))) + 1.0 for s in ordered]
+    jac_ref, jac_dev, jac_nz, jac_cost = [], [], [], []
     for v, s1 in enumerate(ordered):
         cr, cd, cn = [], [], []
         for q, s2 in enumerate(ordered):
@@ -135,9 +153,16 @@ def network_spec(net, name):
             nz = not (e == 0)
             cn.append(nz)
             cd.append(ccode_device(e, assign_to=sympy.Symbol("jv")) if nz else None)
+            jac_cost.append(float(sympy.count_ops(e)) + 4.0 if nz else 0.5)
         jac_ref.append(cr)
         jac_dev.append(cd)
         jac_nz.append(cn)
+    N = len(ordered)
+    rhs_part, jac_part = {}, {}
+    for npart in (1, 2, 4):
+        rhs_part[npart] = balance(rhs_cost, npart)
+        flat = balance(jac_cost, npart)
+        jac_part[npart] = [flat[v * N:(v + 1) * N] for v in range(N)]
     md = net.mass_density_expression()
     T = net.temperature_expression(False)
     Tg = net.temperature_expression(True)
@@ -154,4 +179,5 @@ def network_spec(net, name):
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),
         T_dev_div=gamma_div(ccode_device(T)), Tge_dev_div=gamma_div(ccode_device(Tg)),
         rhs_ref=rhs_ref, rhs_dev=rhs_dev,
-        jac_ref=jac_ref, jac_dev=jac_dev, jac_nonzero=jac_nz)
+        jac_ref=jac_ref, jac_dev=jac_dev, jac_nonzero=jac_nz,
+        rhs_part=rhs_part, jac_part=jac_part)

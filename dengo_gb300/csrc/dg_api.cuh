@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "dg_engine.cuh"
+#include "dg_split.cuh"
 #include "dg_strip.cuh"
 #include "dg_tablefile.h"
 
@@ -300,12 +301,12 @@ struct Api {
     }
 
     /* ---------------- the solver ---------------- */
-    template <int BLOCK>
+    template <int BLOCK, bool MIXED>
     static int launch(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
                       cudaStream_t st)
     {
-        auto kern = evolve_fp64_kernel<Net, BLOCK>;
-        const size_t smem = Lane<Net, BLOCK>::smem_bytes();
+        auto kern = evolve_kernel<Net, BLOCK, MIXED>;
+        const size_t smem = Lane<Net, BLOCK, MIXED>::smem_bytes();
         DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         if (io.ncells <= 0) return 0;
         const long long need = (io.ncells + BLOCK - 1) / BLOCK;
@@ -328,6 +329,35 @@ struct Api {
         return 0;
     }
 
+    /* The split engine: 32 cells per CTA, NP warps per cell (dg_split.cuh). */
+    template <int NP, bool MIXED>
+    static int launch_split(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
+                            cudaStream_t st)
+    {
+        auto kern = evolve_split_kernel<Net, NP, MIXED>;
+        const size_t smem = SplitLayout<Net, NP, MIXED>::bytes();
+        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (io.ncells <= 0) return 0;
+        const long long need = (io.ncells + 31) / 32;
+        unsigned long long *queue = nullptr;
+        if (schedule == DENGO_SCHED_PER_THREAD) {
+            grid = (int)need;
+        } else {
+            int per_sm = 0;
+            DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * NP, smem));
+            if (per_sm < 1) per_sm = 1;
+            const long long full = (long long)g->nsm * per_sm;
+            if (grid <= 0) grid = (int)(need < full ? need : full);
+            if (schedule != DENGO_SCHED_STRIDE) {
+                queue = g->queue;
+                DG_CUDA(cudaMemsetAsync(queue, 0, sizeof(*queue), st));
+            }
+        }
+        kern<<<grid, 32 * NP, smem, st>>>(io, g->ts, kc, queue);
+        DG_CUDA(cudaGetLastError());
+        return 0;
+    }
+
     static int solve_device(Data *d, const dengo_cell_batch *b, double z,
                             const dengo_solver_config *cfg_in, void *stream)
     {
@@ -338,8 +368,8 @@ struct Api {
         dengo_solver_config cfg;
         if (cfg_in) cfg = *cfg_in;
         else dengo_default_config(&cfg);
-        if (cfg.precision != DENGO_FP64) {
-            set_error("%s_solve_cells_device: precision %d not built", Net::NAME, cfg.precision);
+        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED) {
+            set_error("%s_solve_cells_device: unknown precision %d", Net::NAME, cfg.precision);
             return -1;
         }
         Gpu *g = gpu(d);
@@ -369,10 +399,23 @@ struct Api {
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         g->ts.z = z;
+        const bool mixed = cfg.precision == DENGO_MIXED;
+        if (cfg.warps_per_cell == 2)
+            return mixed ? launch_split<2, true>(g, io, kc, cfg.schedule, cfg.grid, st)
+                         : launch_split<2, false>(g, io, kc, cfg.schedule, cfg.grid, st);
+        if (cfg.warps_per_cell == 4)
+            return mixed ? launch_split<4, true>(g, io, kc, cfg.schedule, cfg.grid, st)
+                         : launch_split<4, false>(g, io, kc, cfg.schedule, cfg.grid, st);
         switch (cfg.block) {
-        case 32: return launch<32>(g, io, kc, cfg.schedule, cfg.grid, st);
-        case 128: return launch<128>(g, io, kc, cfg.schedule, cfg.grid, st);
-        default: return launch<64>(g, io, kc, cfg.schedule, cfg.grid, st);
+        case 32:
+            return mixed ? launch<32, true>(g, io, kc, cfg.schedule, cfg.grid, st)
+                         : launch<32, false>(g, io, kc, cfg.schedule, cfg.grid, st);
+        case 128:
+            return mixed ? launch<128, true>(g, io, kc, cfg.schedule, cfg.grid, st)
+                         : launch<128, false>(g, io, kc, cfg.schedule, cfg.grid, st);
+        default:
+            return mixed ? launch<64, true>(g, io, kc, cfg.schedule, cfg.grid, st)
+                         : launch<64, false>(g, io, kc, cfg.schedule, cfg.grid, st);
         }
     }
 
@@ -741,6 +784,7 @@ extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg)
     cfg->schedule = DENGO_SCHED_AUTO;
     cfg->block = 0;
     cfg->grid = 0;
+    cfg->warps_per_cell = 1;
 }
 
 #endif

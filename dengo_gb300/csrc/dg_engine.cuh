@@ -78,13 +78,14 @@ struct Slots {
     __device__ __forceinline__ double &operator[](int i) const { return p[i * BLOCK]; }
 };
 
-template <class Net, int BLOCK>
+template <class Net, int BLOCK, bool MIXED = false>
 struct Lane {
     static constexpr int N = Net::N;
     static constexpr int NT = Net::NT;
-    /* shared-memory slot map */
+    /* shared-memory slot map, in doubles per thread; the mixed path keeps
+     * the matrix in FP32 (half the slots) */
     static constexpr int OFF_J = 0;
-    static constexpr int OFF_R = OFF_J + N * N;
+    static constexpr int OFF_R = OFF_J + (MIXED ? (N * N + 1) / 2 : N * N);
     static constexpr int OFF_PREV = OFF_R + NT;
     static constexpr int OFF_SC = OFF_PREV + N;
     static constexpr int OFF_INV = OFF_SC + N;
@@ -190,11 +191,11 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
 #pragma unroll
     for (int k = 0; k < N - 1; k++) {
         int p = k;
-        double best = fabs(J[k * N + k]);
+        double best = J[k * N + k];
 #pragma unroll
         for (int i = k + 1; i < N; i++) {
-            const double a = fabs(J[k * N + i]);
-            if (a > best) {
+            const double a = J[k * N + i];
+            if (dg_abs_gt(a, best)) {   /* fabs(a) > fabs(best) */
                 best = a;
                 p = i;
             }
@@ -219,12 +220,11 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
         piv_v[k] = piv;
         piv_r[k] = rp;
         double m[N], row[N];
-        bool mfin = true, rowfin = true;
+        bool rowfin = true;
 #pragma unroll
         for (int i = k + 1; i < N; i++) {
             m[i] = dg_div(J[k * N + i], piv, rp);
             J[k * N + i] = m[i];
-            mfin = mfin && dg_finite(m[i]);
         }
 #pragma unroll
         for (int j = k + 1; j < N; j++) {
@@ -233,10 +233,11 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
         }
 #pragma unroll
         for (int i = k + 1; i < N; i++) {
-            if (m[i] != 0.0 || !rowfin) {
+            const bool mf = dg_finite(m[i]);
+            if (dg_nonzero(m[i]) || !rowfin) {
 #pragma unroll
                 for (int j = k + 1; j < N; j++) {
-                    if (row[j] != 0.0 || !mfin) J[j * N + i] = J[j * N + i] - m[i] * row[j];
+                    if (dg_nonzero(row[j]) || !mf) J[j * N + i] = J[j * N + i] - m[i] * row[j];
                 }
             }
         }
@@ -244,7 +245,7 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
         const bool xfin = dg_finite(xk);
 #pragma unroll
         for (int i = k + 1; i < N; i++)
-            if (m[i] != 0.0 || !xfin) x[i] = x[i] - m[i] * xk;
+            if (dg_nonzero(m[i]) || !xfin) x[i] = x[i] - m[i] * xk;
     }
     piv_v[N - 1] = J[(N - 1) * N + (N - 1)];
     piv_r[N - 1] = 1.0 / piv_v[N - 1];
@@ -254,11 +255,94 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
 #pragma unroll
         for (int j = i + 1; j < N; j++) {
             const double aij = J[j * N + i];
-            if (aij != 0.0 || !dg_finite(x[j])) xi = xi - aij * x[j];
+            if (dg_nonzero(aij) || !dg_finite(x[j])) xi = xi - aij * x[j];
         }
         x[i] = dg_div(xi, piv_v[i], piv_r[i]);
     }
 }
+
+/* FP32 storage of the scaled matrix for the mixed-precision path. */
+template <int BLOCK>
+struct SlotsF {
+    float *p;
+    __device__ __forceinline__ float &operator[](int i) const { return p[i * BLOCK]; }
+};
+
+/* Partial-pivot LU and solve in FP32 (mixed precision): the same algorithm
+ * as Gauss_Elim, on the FP32 copy of the scaled I - dt J.  x: FP32 right-hand
+ * side in, FP32 Newton update out. */
+template <int N, int BLOCK>
+__device__ __forceinline__ void gauss_elim_f32(SlotsF<BLOCK> J, float (&x)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N - 1; k++) {
+        int p = k;
+        float best = fabsf(J[k * N + k]);
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            const float a = fabsf(J[k * N + i]);
+            if (a > best) {
+                best = a;
+                p = i;
+            }
+        }
+        if (p != k) {
+            for (int j = k; j < N; j++) {
+                const float t = J[j * N + k];
+                J[j * N + k] = J[j * N + p];
+                J[j * N + p] = t;
+            }
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                if (i == p) {
+                    const float t = x[k];
+                    x[k] = x[i];
+                    x[i] = t;
+                }
+            }
+        }
+        const float rp = 1.0f / J[k * N + k];
+        float m[N], row[N];
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            m[i] = J[k * N + i] * rp;
+            J[k * N + i] = m[i];
+        }
+#pragma unroll
+        for (int j = k + 1; j < N; j++) row[j] = J[j * N + k];
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+#pragma unroll
+            for (int j = k + 1; j < N; j++) J[j * N + i] = fmaf(-m[i], row[j], J[j * N + i]);
+            x[i] = fmaf(-m[i], x[k], x[i]);
+        }
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
+        float xi = x[i];
+#pragma unroll
+        for (int j = i + 1; j < N; j++) xi = fmaf(-J[j * N + i], x[j], xi);
+        x[i] = xi / J[i * N + i];
+    }
+}
+
+/* Scaled Jacobian store for the mixed path: the FP64 value of the reference's
+ * transformation, rounded to FP32. */
+template <int N, int BLOCK>
+struct JacPutF {
+    SlotsF<BLOCK> J;
+    Slots<BLOCK> INV, SC;
+    double mdt;
+    __device__ __forceinline__ void operator()(int q, int v, double jv) const
+    {
+        double a = jv * INV[q];
+        a = a * SC[v];
+        a = mdt * a;
+        if (q == v) a = a + 1.0;
+        J[v * N + q] = (float)a;
+    }
+    __device__ __forceinline__ void zero(int q, int v) const { J[v * N + q] = (q == v) ? 1.0f : 0.0f; }
+};
 
 /* Stores one Jacobian entry already transformed as BE_Resid_Jac does:
  * row scale 1/scale_eq, column scale scale_var, then -dt*J, +1 on the
@@ -301,16 +385,22 @@ __device__ __forceinline__ void to_number_density(double (&y)[Net::N], double (&
     }
 }
 
-template <class Net, int BLOCK>
+/* MIXED = false: the reference's FP64 arithmetic throughout (bit-faithful).
+ * MIXED = true: the scaled I - dt J is rounded to FP32 and factored in FP32;
+ * temperature, rates, RHS, residual, the Newton update and its convergence
+ * test stay FP64, so each Newton sweep refines the FP32 solve against the FP64
+ * residual. */
+template <class Net, int BLOCK, bool MIXED>
 __global__ void __launch_bounds__(BLOCK)
-evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
+evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 {
-    using L = Lane<Net, BLOCK>;
+    using L = Lane<Net, BLOCK, MIXED>;
     constexpr int N = Net::N;
     extern __shared__ double dg_smem[];
     const int tid = threadIdx.x;
     double *base = dg_smem + tid;
     const Slots<BLOCK> J{base + L::OFF_J * BLOCK};
+    const SlotsF<BLOCK> JF{(float *)(dg_smem + L::OFF_J * BLOCK) + tid};
     const Slots<BLOCK> R{base + L::OFF_R * BLOCK};
     const Slots<BLOCK> PREV{base + L::OFF_PREV * BLOCK};
     const Slots<BLOCK> SC{base + L::OFF_SC * BLOCK};
@@ -426,22 +516,37 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 /* BE_Resid_Jac (BE_chem_solve.C:280-321) */
 #pragma unroll
                 for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
-                JacPut<N, BLOCK> put{J, INV, SC, -dt, dense || !(dt > 0.0)};
-                ok = Net::jac(y, R, Tge, T, ts.z, put);
+                if (MIXED) {
+                    JacPutF<N, BLOCK> put{JF, INV, SC, -dt};
+                    ok = Net::jac(y, R, Tge, T, ts.z, put);
+                } else {
+                    JacPut<N, BLOCK> put{J, INV, SC, -dt, dense || !(dt > 0.0)};
+                    ok = Net::jac(y, R, Tge, T, ts.z, put);
+                }
                 if (ok) {
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
-                    gauss_elim_fast<N, BLOCK>(J, f);
+                    if (MIXED) {
+                        float xs[N];
+#pragma unroll
+                        for (int i = 0; i < N; i++) xs[i] = (float)f[i];
+                        gauss_elim_f32<N, BLOCK>(JF, xs);
+#pragma unroll
+                        for (int i = 0; i < N; i++) f[i] = (double)xs[i];
+                    } else {
+                        gauss_elim_fast<N, BLOCK>(J, f);
+                    }
                     /* Newton update and max-norm test (BE_chem_solve.C:173-206) */
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = u[i] - 1.0 * f[i];
 #pragma unroll
                     for (int i = 0; i < N; i++) {
-                        if (fabs(f[i]) > (AT[i] + RT[i] * fabs(u[i]))) {
+                        /* fabs(s) > atol + rtol*fabs(u), then the NaN test */
+                        if (dg_abs_gt_val(f[i], AT[i] + RT[i] * fabs(u[i]))) {
                             unsolved = true;
                             break;
                         }
-                        if (u[i] != u[i]) {
+                        if (dg_isnan(u[i])) {
                             nan = true;
                             break;
                         }
@@ -466,7 +571,7 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         if (rv == 0) {
 #pragma unroll
             for (int i = 0; i < N; i++)
-                if (y[i] < 0) rv = 1;
+                if (dg_lt0(y[i])) rv = 1;
         }
         int done = -1;
         if (rv == 0) {
@@ -480,7 +585,7 @@ evolve_fp64_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
 #pragma unroll
                 for (int i = 0; i < N; i++) {
                     PREV[i] = y[i];
-                    if (y[i] < cfg.floor_value) y[i] = cfg.floor_value;
+                    if (dg_lt_pos(y[i], cfg.floor_value)) y[i] = cfg.floor_value;
                 }
                 if (!(ttot < dtf)) done = ST_OK;
             }

@@ -133,6 +133,50 @@ DG_HD int dg_expo(double x) { return (int)((dg_bits(x) >> 52) & 0x7FF); }
 
 DG_HD bool dg_finite(double x) { return dg_expo(x) != 0x7FF; }
 
+/* IEEE comparisons evaluated on the bit patterns, with the results of the C
+ * operators in every case (NaN, infinities, signed zeros).  On GB300 a
+ * floating-point compare occupies the scarce FP64 pipe; these run on the
+ * integer pipes.  Shifting the bits left by one drops the sign and orders
+ * magnitudes as unsigned integers; NaN is any magnitude above infinity's. */
+#define DG_INF2 0xFFE0000000000000ull
+
+DG_HD bool dg_isnan(double x) { return (dg_bits(x) << 1) > DG_INF2; }
+
+/* x != 0.0 */
+DG_HD bool dg_nonzero(double x) { return (dg_bits(x) << 1) != 0; }
+
+/* x < 0.0 */
+DG_HD bool dg_lt0(double x)
+{
+    const uint64_t b = dg_bits(x), m = b << 1;
+    return (b >> 63) && m != 0 && m <= DG_INF2;
+}
+
+/* fabs(a) > fabs(b) */
+DG_HD bool dg_abs_gt(double a, double b)
+{
+    const uint64_t x = dg_bits(a) << 1, y = dg_bits(b) << 1;
+    return x <= DG_INF2 && y <= DG_INF2 && x > y;
+}
+
+/* fabs(s) > t */
+DG_HD bool dg_abs_gt_val(double s, double t)
+{
+    const uint64_t x = dg_bits(s) << 1, tb = dg_bits(t), y = tb << 1;
+    if (x > DG_INF2 || y > DG_INF2) return false;
+    if (tb >> 63) return y != 0 || x != 0;   /* t <= -0: true unless s and t are zeros */
+    return x > y;
+}
+
+/* y < c for c > 0 */
+DG_HD bool dg_lt_pos(double y, double c)
+{
+    const uint64_t b = dg_bits(y);
+    if ((b << 1) > DG_INF2) return false;
+    if (b >> 63) return true;
+    return b < dg_bits(c);
+}
+
 /* Divisor in the range where dg_div's fast path applies. */
 DG_HD bool dg_div_ok(double b)
 {

@@ -56,3 +56,64 @@ extern "C" int dg_measure_fma_peak(int fp64, int iters, double *tflops)
 {
     return fp64 ? measure<double>(iters, tflops) : measure<float>(iters, tflops);
 }
+
+/* FP64 issue model: `chains` independent dependent-FMA chains per thread,
+ * `warps` warps per SM (one block per SM).  Returns cycles per FMA per warp
+ * (clock64 inside the kernel, averaged over warps). */
+template <int CH>
+__global__ void fma_lat(double *out, long long *cyc, int iters, int active_lanes)
+{
+    if ((int)(threadIdx.x & 31) >= active_lanes) return;
+    double x[CH];
+#pragma unroll
+    for (int c = 0; c < CH; c++) x[c] = threadIdx.x + c;
+    const double a = 0.999999, b = 1e-7;
+    const long long t0 = clock64();
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < CH; c++) x[c] = fma(x[c], a, b);
+    }
+    const long long t1 = clock64();
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < CH; c++) s += x[c];
+    if (s == -1.2345) out[0] = s;
+    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)cyc, (unsigned long long)(t1 - t0));
+}
+
+extern "C" int dg_measure_fma_latency_lanes(int chains, int warps, int iters, int lanes,
+                                            double *cycles_per_fma);
+
+extern "C" int dg_measure_fma_latency(int chains, int warps, int iters, double *cycles_per_fma)
+{
+    return dg_measure_fma_latency_lanes(chains, warps, iters, 32, cycles_per_fma);
+}
+
+/* As above with only `lanes` active lanes per warp. */
+extern "C" int dg_measure_fma_latency_lanes(int chains, int warps, int iters, int lanes,
+                                            double *cycles_per_fma)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    double *out;
+    long long *cyc;
+    cudaMalloc(&out, 8);
+    cudaMalloc(&cyc, 8);
+    cudaMemset(cyc, 0, 8);
+    const int threads = 32 * warps;
+    switch (chains) {
+    case 1: fma_lat<1><<<nsm, threads>>>(out, cyc, iters, lanes); break;
+    case 2: fma_lat<2><<<nsm, threads>>>(out, cyc, iters, lanes); break;
+    case 4: fma_lat<4><<<nsm, threads>>>(out, cyc, iters, lanes); break;
+    default: fma_lat<8><<<nsm, threads>>>(out, cyc, iters, lanes); chains = 8; break;
+    }
+    long long h = 0;
+    cudaMemcpy(&h, cyc, 8, cudaMemcpyDeviceToHost);
+    const cudaError_t e = cudaGetLastError();
+    cudaFree(out);
+    cudaFree(cyc);
+    if (e != cudaSuccess) return -1;
+    *cycles_per_fma = (double)h / ((double)nsm * warps) / ((double)iters * chains);
+    return 0;
+}

@@ -1,0 +1,404 @@
+/*
+ * Split engine: 32 cells per CTA, one per lane, and the Newton sweep of each
+ * cell divided over NP cooperating warps (NP = 2 or 4), which the scheduler
+ * places on different SM sub-partitions and hence different FP64 units.
+ *
+ * On GB300 each sub-partition's FP64 unit accepts one warp instruction every
+ * ~64 cycles whatever the number of active lanes, so a cell's sweep costs
+ * about (FP64 instructions on its path) x 64 cycles.  The stiffest cells need
+ * 10^5 sequential sweeps and set the length of a hydro step; splitting a sweep
+ * over NP warps shortens that path by up to NP while each FP64 warp
+ * instruction still serves 32 cells.
+ *
+ * Work split of one sweep (barriers between phases):
+ *   warp 0        substep bookkeeping, T(ge), log T, bin; residual; pivot
+ *                 search and row swap; back substitution; Newton update and
+ *                 convergence test; cell refill (work queue)
+ *   all warps     table interpolation (tables k = w mod NP), RHS rows and
+ *                 Jacobian entries of part w (generated partition balanced by
+ *                 operation count), multipliers and row updates of the LU
+ *                 for rows i = w mod NP
+ * Every value is computed with exactly the operations of the single-lane
+ * engine (dg_engine.cuh), so results are bit-identical to it and hence to the
+ * reference.  Per-cell state lives in shared memory as [slot][32] doubles.
+ */
+#ifndef DG_SPLIT_CUH
+#define DG_SPLIT_CUH
+
+#include "dg_engine.cuh"
+
+namespace dg {
+
+template <class Net, int NP, bool MIXED>
+struct SplitLayout {
+    static constexpr int N = Net::N;
+    static constexpr int NT = Net::NT;
+    static constexpr int J = 0;                                   /* matrix */
+    static constexpr int R = J + (MIXED ? (N * N + 1) / 2 : N * N);  /* rates */
+    static constexpr int Y = R + NT;      /* unscaled state seen by RHS/Jacobian */
+    static constexpr int G = Y + N;       /* RHS, residual, Newton update */
+    static constexpr int U = G + N;
+    static constexpr int U0 = U + N;
+    static constexpr int SC = U0 + N;
+    static constexpr int INV = SC + N;
+    static constexpr int AT = INV + N;
+    static constexpr int RT = AT + N;
+    static constexpr int PREV = RT + N;
+    static constexpr int SCAL = PREV + N;  /* T, Tge, Tdef, -dt, piv, 1/piv */
+    static constexpr int SLOTS = SCAL + 6;
+    static constexpr size_t bytes()
+    {
+        /* doubles + per-cell ints: bin, flags[4] */
+        return sizeof(double) * SLOTS * 32 + sizeof(int) * 8 * 32 + 64;
+    }
+};
+
+/* per-cell int flags */
+enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6 };
+
+template <class Net, int NP, bool MIXED>
+__global__ void __launch_bounds__(32 * NP)
+evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
+{
+    using L = SplitLayout<Net, NP, MIXED>;
+    constexpr int N = Net::N;
+    extern __shared__ double dg_smem[];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    double *cellbase = dg_smem + l;
+    const Slots<32> J{cellbase + L::J * 32}, R{cellbase + L::R * 32}, Y{cellbase + L::Y * 32},
+        G{cellbase + L::G * 32}, U{cellbase + L::U * 32}, U0{cellbase + L::U0 * 32},
+        SC{cellbase + L::SC * 32}, INV{cellbase + L::INV * 32}, AT{cellbase + L::AT * 32},
+        RT{cellbase + L::RT * 32}, PREV{cellbase + L::PREV * 32}, S{cellbase + L::SCAL * 32};
+    const SlotsF<32> JF{(float *)(dg_smem + L::J * 32) + l};
+    int *iflags = (int *)(dg_smem + L::SLOTS * 32);
+    auto F = [&](int f) -> int & { return iflags[f * 32 + l]; };
+    __shared__ int s_any;
+
+    /* warp-0 control state of this lane's cell */
+    long long qi = 0, cell = 0;
+    double dtf = 0, dt = 0, ttot = 0;
+    int siter = 0, isweep = 0, nsweeps = 0, nfail = 0;
+    bool active = false, dense = false;
+    const long long stride = (long long)gridDim.x * 32;
+    if (w == 0) qi = queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * 32 + l;
+
+    auto substep_begin = [&]() {
+        for (int i = 0; i < N; i++) {
+            const double v = Y[i] * INV[i];
+            U[i] = v;
+            U0[i] = v;
+            AT[i] = AT[i] * INV[i];
+        }
+        isweep = 0;
+    };
+    auto cell_begin = [&]() -> bool {
+        double y[N], at[N];
+        for (int s = 0; s < N; s++) {
+            const long long off = cell * io.cs + s * io.ss;
+            y[s] = io.state[off];
+            at[s] = io.atol[off];
+            RT[s] = io.rtol ? io.rtol[off] : io.rtol_scalar;
+        }
+        to_number_density<Net>(y, at);
+        Net::electrons(y);
+        dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+        dt = io.dt ? io.dt[cell] : -1.0;
+        if (dt < 0) dt = dtf / 1e5;
+        ttot = 0;
+        siter = nsweeps = nfail = 0;
+        dense = false;
+        for (int s = 0; s < N; s++) {
+            AT[s] = at[s];
+            Y[s] = y[s];
+            SC[s] = y[s];
+            PREV[s] = y[s];
+            INV[s] = 1.0 / y[s];
+            dense = dense || !(y[s] > 0.0 && dg_finite(y[s]));
+        }
+        if (!(ttot < dtf)) return false;
+        substep_begin();
+        return true;
+    };
+    auto cell_end = [&](int status) {
+        for (int s = 0; s < N; s++) {
+            double v = Y[s], a = AT[s];
+            if (!Net::INPUT_IS_NUMBER && s != Net::IGE) {
+                v = v * Net::unit(s);
+                a = a * Net::unit(s);
+            }
+            const long long off = cell * io.cs + s * io.ss;
+            io.state[off] = v;
+            io.atol[off] = a;
+        }
+        if (io.dt) io.dt[cell] = dt;
+        if (io.ttot) io.ttot[cell] = ttot;
+        if (io.status) io.status[cell] = status;
+        if (io.substeps) io.substeps[cell] = siter;
+        if (io.sweeps) io.sweeps[cell] = nsweeps;
+        if (io.failures) io.failures[cell] = nfail;
+    };
+    auto fetch = [&]() {
+        while (qi < io.ncells) {
+            cell = io.order ? (long long)io.order[qi] : qi;
+            if (cell_begin()) {
+                active = true;
+                return;
+            }
+            cell_end(ST_OK);
+            qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
+        }
+        active = false;
+    };
+
+    if (w == 0) {
+        fetch();
+        F(F_ACT) = active;
+    }
+    for (;;) {
+        /* ---- P0 (warp 0): unscale, temperature, bin ---- */
+        if (w == 0) {
+            const unsigned anyact = __ballot_sync(0xffffffffu, active);
+            if (l == 0) s_any = anyact != 0;
+            if (active) {
+                double y[N];
+                for (int i = 0; i < N; i++) {
+                    y[i] = U[i] * SC[i];
+                    Y[i] = y[i];
+                }
+                double T, Tge;
+                Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+                const double logT = dg_log(T);
+                const int bin = (int)(ts.idbin * (logT - ts.lb));
+                const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+                const double t1 = (ts.lb + (bin) * ts.dbin);
+                const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+                S[0] = T;
+                S[1] = Tge;
+                S[2] = (logT - t1) / (t2 - t1);
+                S[3] = -dt;
+                F(F_BIN) = bc;
+                F(F_DENSE) = dense || !(dt > 0.0);
+            }
+            F(F_OKR) = 1;
+            F(F_OKJ) = 1;
+        }
+        __syncthreads();
+        if (!s_any) break;
+        const bool act = F(F_ACT) != 0;
+        /* ---- P1 (all warps): interpolation, tables k = w mod NP ---- */
+        if (act) {
+            const double Tdef = S[2];
+            const double2 *row = ts.pairs + (size_t)F(F_BIN) * Net::NT;
+            for (int k = w; k < Net::NT; k += NP) {
+                if (Net::zdep(k)) {
+                    R[k] = ts.zvals[k];
+                } else {
+                    const double2 pr = __ldg(row + k);
+                    R[k] = pr.x + Tdef * pr.y;
+                }
+            }
+        }
+        __syncthreads();
+        /* ---- P2 (all warps): RHS rows of part w ---- */
+        if (act) {
+            double y[N], f[N];
+            for (int i = 0; i < N; i++) y[i] = Y[i];
+            bool ok = true;
+            switch (w) {
+            case 0: ok = Net::template rhs<NP, 0>(y, R, S[0], ts.z, f); break;
+            case 1: ok = Net::template rhs<NP, 1 % NP>(y, R, S[0], ts.z, f); break;
+            case 2: ok = Net::template rhs<NP, 2 % NP>(y, R, S[0], ts.z, f); break;
+            default: ok = Net::template rhs<NP, 3 % NP>(y, R, S[0], ts.z, f); break;
+            }
+            if (ok) {
+                for (int i = 0; i < N; i++)
+                    if (Net::rhs_row_part(NP, i) == w) G[i] = f[i];
+            } else {
+                atomicAnd(&F(F_OKR), 0);
+            }
+        }
+        __syncthreads();
+        /* ---- P3 (warp 0): residual g = u - u0 - dt f (scaled), y for the Jacobian ---- */
+        if (w == 0 && act && F(F_OKR)) {
+            for (int i = 0; i < N; i++) {
+                const double u = Y[i] * INV[i];
+                double g = G[i] * INV[i];
+                g = u - U0[i] - dt * g;
+                G[i] = g;
+                U[i] = u;
+                Y[i] = u * SC[i];
+            }
+        }
+        __syncthreads();
+        /* ---- P4 (all warps): Jacobian entries of part w, scaled ---- */
+        const bool do_j = act && F(F_OKR);
+        if (do_j) {
+            double y[N];
+            for (int i = 0; i < N; i++) y[i] = Y[i];
+            bool ok = true;
+            if (MIXED) {
+                const JacPutF<N, 32> put{JF, INV, SC, S[3]};
+                switch (w) {
+                case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
+                case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                }
+            } else {
+                const JacPut<N, 32> put{J, INV, SC, S[3], F(F_DENSE) != 0};
+                switch (w) {
+                case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
+                case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                }
+            }
+            if (!ok) atomicAnd(&F(F_OKJ), 0);
+        }
+        __syncthreads();
+        const bool do_lu = do_j && F(F_OKJ);
+        if (w == 0 && do_lu) {
+            for (int i = 0; i < N; i++) U[i] = Y[i] * INV[i];
+        }
+        /* ---- P5: LU.  FP64: pivot (warp 0) then row updates (all warps);
+         *      mixed: the whole FP32 factorisation on warp 0 ---- */
+        if (MIXED) {
+            if (w == 0 && do_lu) {
+                float xs[N];
+                for (int i = 0; i < N; i++) xs[i] = (float)G[i];
+                gauss_elim_f32<N, 32>(JF, xs);
+                for (int i = 0; i < N; i++) G[i] = (double)xs[i];
+            }
+        } else {
+            for (int k = 0; k < N - 1; k++) {
+                __syncthreads();
+                if (w == 0 && do_lu) {
+                    int p = k;
+                    double best = J[k * N + k];
+                    for (int i = k + 1; i < N; i++) {
+                        const double a = J[k * N + i];
+                        if (dg_abs_gt(a, best)) {
+                            best = a;
+                            p = i;
+                        }
+                    }
+                    if (p != k) {
+                        for (int j = k; j < N; j++) {
+                            const double t = J[j * N + k];
+                            J[j * N + k] = J[j * N + p];
+                            J[j * N + p] = t;
+                        }
+                        const double t = G[k];
+                        G[k] = G[p];
+                        G[p] = t;
+                    }
+                    const double piv = J[k * N + k];
+                    S[4] = piv;
+                    S[5] = 1.0 / piv;
+                }
+                __syncthreads();
+                if (do_lu) {
+                    const double piv = S[4], rp = S[5];
+                    bool rowfin = true;
+                    for (int j = k + 1; j < N; j++) rowfin = rowfin && dg_finite(J[j * N + k]);
+                    const double xk = G[k];
+                    const bool xfin = dg_finite(xk);
+                    for (int i = k + 1 + ((w - (k + 1) % NP + NP) % NP); i < N; i += NP) {
+                        const double m = dg_div(J[k * N + i], piv, rp);
+                        J[k * N + i] = m;
+                        const bool mf = dg_finite(m);
+                        if (dg_nonzero(m) || !rowfin) {
+                            for (int j = k + 1; j < N; j++) {
+                                const double akj = J[j * N + k];
+                                if (dg_nonzero(akj) || !mf) J[j * N + i] = J[j * N + i] - m * akj;
+                            }
+                        }
+                        if (dg_nonzero(m) || !xfin) G[i] = G[i] - m * xk;
+                    }
+                }
+            }
+            __syncthreads();
+            if (w == 0 && do_lu) {
+                /* back substitution; the pivots are the final diagonal */
+                for (int i = N - 1; i >= 0; i--) {
+                    double xi = G[i];
+                    for (int j = i + 1; j < N; j++) {
+                        const double aij = J[j * N + i];
+                        const double xj = G[j];
+                        if (dg_nonzero(aij) || !dg_finite(xj)) xi = xi - aij * xj;
+                    }
+                    const double piv = J[i * N + i];
+                    G[i] = dg_div(xi, piv, 1.0 / piv);
+                }
+            }
+        }
+        __syncthreads();
+        /* ---- P6 (warp 0): Newton update, convergence, substep control ---- */
+        if (w == 0 && act) {
+            bool ok = F(F_OKR) && F(F_OKJ), unsolved = false, nan = false;
+            if (ok) {
+                for (int i = 0; i < N; i++) U[i] = U[i] - 1.0 * G[i];
+                for (int i = 0; i < N; i++) {
+                    if (dg_abs_gt_val(G[i], AT[i] + RT[i] * fabs(U[i]))) {
+                        unsolved = true;
+                        break;
+                    }
+                    if (dg_isnan(U[i])) {
+                        nan = true;
+                        break;
+                    }
+                }
+            }
+            isweep++;
+            nsweeps++;
+            int rv = -1;
+            if (!ok || nan) rv = 1;
+            else if (!unsolved) rv = 0;
+            else if (isweep >= cfg.max_sweeps) rv = 1;
+            if (rv >= 0) {
+                double y[N];
+                for (int i = 0; i < N; i++) {
+                    y[i] = U[i] * SC[i];
+                    AT[i] = AT[i] * SC[i];
+                }
+                if (rv == 0)
+                    for (int i = 0; i < N; i++)
+                        if (dg_lt0(y[i])) rv = 1;
+                int done = -1;
+                if (rv == 0) {
+                    if (siter == cfg.max_substeps) {
+                        done = ST_MAX_SUBSTEPS;
+                    } else {
+                        siter++;
+                        ttot += dt;
+                        const double grown = dt * 1.1, rest = dtf - ttot;
+                        dt = grown < rest ? grown : rest;
+                        for (int i = 0; i < N; i++) {
+                            PREV[i] = y[i];
+                            if (dg_lt_pos(y[i], cfg.floor_value)) y[i] = cfg.floor_value;
+                        }
+                        if (!(ttot < dtf)) done = ST_OK;
+                    }
+                } else {
+                    nfail++;
+                    dt /= 2.0;
+                    for (int i = 0; i < N; i++) y[i] = PREV[i];
+                    if (dt / dtf < cfg.dt_ratio_floor) done = ST_DT_UNDERFLOW;
+                }
+                for (int i = 0; i < N; i++) Y[i] = y[i];
+                if (done < 0) {
+                    substep_begin();
+                } else {
+                    cell_end(done);
+                    qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
+                    fetch();
+                }
+            }
+            F(F_ACT) = active;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dg
+#endif

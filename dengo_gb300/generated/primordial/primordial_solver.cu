@@ -308,7 +308,22 @@ struct Net {
 
     /* calculate_rhs (rates_and_rate_tables.C.template:489-520) for one cell;
      * false when a value is negative. */
-    template <class RT>
+    /* Part of a Newton sweep's work assigned to cooperating warp P of NP:
+     * pick<NP>(part with 1, 2, 4 warps) for one row or entry. */
+    __host__ __device__ static constexpr int pick(int np, int p1, int p2, int p4)
+    {
+        return np == 1 ? p1 : (np == 2 ? p2 : p4);
+    }
+
+    /* the part of NP that computes RHS row q */
+    __host__ __device__ static constexpr int rhs_row_part(int np, int q)
+    {
+        return q == 0 ? pick(np, 0, 0, 3) : q == 1 ? pick(np, 0, 1, 3) : q == 2 ? pick(np, 0, 1, 1) : q == 3 ? pick(np, 0, 0, 3) : q == 4 ? pick(np, 0, 1, 2) : q == 5 ? pick(np, 0, 0, 2) : q == 6 ? pick(np, 0, 0, 1) : q == 7 ? pick(np, 0, 1, 0) : q == 8 ? pick(np, 0, 1, 2) : q == 9 ? pick(np, 0, 0, 0) : 0;
+    }
+
+    /* NP/P select the rows computed by warp P of NP cooperating warps (all
+     * rows by default); rows of other parts are left untouched. */
+    template <int NP = 1, int P = 0, class RT>
     __device__ __forceinline__ static bool rhs(const double (&y)[N], const RT &R, double T, double z,
                                                double (&f)[N])
     {
@@ -317,32 +332,32 @@ struct Net {
         (void)T; (void)z;
         const double H2_1 = y[0];
         mdensity += H2_1;
-        if (H2_1 < 0.0) return false;
+        if (dg_lt0(H2_1)) return false;   /* H2_1 < 0.0 */
         const double H2_2 = y[1];
         mdensity += H2_2;
-        if (H2_2 < 0.0) return false;
+        if (dg_lt0(H2_2)) return false;   /* H2_2 < 0.0 */
         const double H_1 = y[2];
         mdensity += H_1;
-        if (H_1 < 0.0) return false;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
         const double H_2 = y[3];
         mdensity += H_2;
-        if (H_2 < 0.0) return false;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
         const double H_m0 = y[4];
         mdensity += H_m0;
-        if (H_m0 < 0.0) return false;
+        if (dg_lt0(H_m0)) return false;   /* H_m0 < 0.0 */
         const double He_1 = y[5];
         mdensity += He_1;
-        if (He_1 < 0.0) return false;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
         const double He_2 = y[6];
         mdensity += He_2;
-        if (He_2 < 0.0) return false;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
         const double He_3 = y[7];
         mdensity += He_3;
-        if (He_3 < 0.0) return false;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
         const double de = y[8];
-        if (de < 0.0) return false;
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
         const double ge = y[9];
-        if (ge < 0.0) return false;
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
         mdensity *= mh;
         const double k01 = R[0];
         const double k02 = R[1];
@@ -388,24 +403,44 @@ struct Net {
         const double reHeII1_reHeII1 = R[41];
         const double reHeII2_reHeII2 = R[42];
         const double reHeIII_reHeIII = R[43];
-        f[0] = k08*H_1*H_m0 + k10*H2_2*H_1 - k11*H2_1*H_2 - k12*H2_1*de - k13*H2_1*H_1 + k19*H2_2*H_m0 + k21*H2_1*dg_ipow<2>(H_1) + k22*dg_ipow<3>(H_1) - k23*dg_ipow<2>(H2_1);
-        f[1] = k09*H_1*H_2 - k10*H2_2*H_1 + k11*H2_1*H_2 + k17*H_2*H_m0 - k18*H2_2*de - k19*H2_2*H_m0;
-        f[2] = -k01*H_1*de + k02*H_2*de - k07*H_1*de - k08*H_1*H_m0 - k09*H_1*H_2 - k10*H2_2*H_1 + k11*H2_1*H_2 + 2*k13*H2_1*H_1 + k14*H_m0*de + k15*H_1*H_m0 + 2*k16*H_2*H_m0 + 2*k18*H2_2*de + k19*H2_2*H_m0 - 2*k21*H2_1*dg_ipow<2>(H_1) - 2*k22*dg_ipow<3>(H_1) + 2*k23*dg_ipow<2>(H2_1);
-        f[3] = k01*H_1*de - k02*H_2*de - k09*H_1*H_2 + k10*H2_2*H_1 - k11*H2_1*H_2 + 2*k12*H2_1*de - k16*H_2*H_m0 - k17*H_2*H_m0;
-        f[4] = k07*H_1*de - k08*H_1*H_m0 - k14*H_m0*de - k15*H_1*H_m0 - k16*H_2*H_m0 - k17*H_2*H_m0 - k19*H2_2*H_m0;
-        f[5] = -k03*He_1*de + k04*He_2*de;
-        f[6] = k03*He_1*de - k04*He_2*de - k05*He_2*de + k06*He_3*de;
-        f[7] = k05*He_2*de - k06*He_3*de;
-        f[8] = k01*H_1*de - k02*H_2*de + k03*He_1*de - k04*He_2*de + k05*He_2*de - k06*He_3*de - k07*H_1*de + k08*H_1*H_m0 + k14*H_m0*de + k15*H_1*H_m0 + k17*H_2*H_m0 - k18*H2_2*de;
-        f[9] = -H2_1*H_1*h2formation_h2mcool - H2_1*gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0) + dg_ipow<3>(H_1)*h2formation_h2mheat - H_1*ceHI_ceHI*de - H_1*ciHI_ciHI*de - H_2*de*reHII_reHII - He_1*ciHeI_ciHeI*de - He_2*ceHeII_ceHeII*de - He_2*ceHeI_ceHeI*dg_ipow<2>(de) - He_2*ciHeII_ciHeII*de - He_2*ciHeIS_ciHeIS*dg_ipow<2>(de) - He_2*de*reHeII1_reHeII1 - He_2*de*reHeII2_reHeII2 - He_3*de*reHeIII_reHeIII - brem_brem*de*(H_2 + He_2 + 4.0*He_3);
-        f[9] /= mdensity;
+        if (pick(NP, 0, 0, 3) == P) {
+            f[0] = k08*H_1*H_m0 + k10*H2_2*H_1 - k11*H2_1*H_2 - k12*H2_1*de - k13*H2_1*H_1 + k19*H2_2*H_m0 + k21*H2_1*dg_ipow<2>(H_1) + k22*dg_ipow<3>(H_1) - k23*dg_ipow<2>(H2_1);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            f[1] = k09*H_1*H_2 - k10*H2_2*H_1 + k11*H2_1*H_2 + k17*H_2*H_m0 - k18*H2_2*de - k19*H2_2*H_m0;
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            f[2] = -k01*H_1*de + k02*H_2*de - k07*H_1*de - k08*H_1*H_m0 - k09*H_1*H_2 - k10*H2_2*H_1 + k11*H2_1*H_2 + 2*k13*H2_1*H_1 + k14*H_m0*de + k15*H_1*H_m0 + 2*k16*H_2*H_m0 + 2*k18*H2_2*de + k19*H2_2*H_m0 - 2*k21*H2_1*dg_ipow<2>(H_1) - 2*k22*dg_ipow<3>(H_1) + 2*k23*dg_ipow<2>(H2_1);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            f[3] = k01*H_1*de - k02*H_2*de - k09*H_1*H_2 + k10*H2_2*H_1 - k11*H2_1*H_2 + 2*k12*H2_1*de - k16*H_2*H_m0 - k17*H_2*H_m0;
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            f[4] = k07*H_1*de - k08*H_1*H_m0 - k14*H_m0*de - k15*H_1*H_m0 - k16*H_2*H_m0 - k17*H_2*H_m0 - k19*H2_2*H_m0;
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            f[5] = -k03*He_1*de + k04*He_2*de;
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            f[6] = k03*He_1*de - k04*He_2*de - k05*He_2*de + k06*He_3*de;
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            f[7] = k05*He_2*de - k06*He_3*de;
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            f[8] = k01*H_1*de - k02*H_2*de + k03*He_1*de - k04*He_2*de + k05*He_2*de - k06*He_3*de - k07*H_1*de + k08*H_1*H_m0 + k14*H_m0*de + k15*H_1*H_m0 + k17*H_2*H_m0 - k18*H2_2*de;
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            f[9] = -H2_1*H_1*h2formation_h2mcool - H2_1*gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0) + dg_ipow<3>(H_1)*h2formation_h2mheat - H_1*ceHI_ceHI*de - H_1*ciHI_ciHI*de - H_2*de*reHII_reHII - He_1*ciHeI_ciHeI*de - He_2*ceHeII_ceHeII*de - He_2*ceHeI_ceHeI*dg_ipow<2>(de) - He_2*ciHeII_ciHeII*de - He_2*ciHeIS_ciHeIS*dg_ipow<2>(de) - He_2*de*reHeII1_reHeII1 - He_2*de*reHeII2_reHeII2 - He_3*de*reHeIII_reHeIII - brem_brem*de*(H_2 + He_2 + 4.0*He_3);
+            f[9] /= mdensity;
+        }
         return true;
     }
 
     /* calculate_jacobian (rates_and_rate_tables.C.template:556-595) for one
      * cell: put(eq, var, d rhs_eq / d var) for every entry; 54 of
      * 100 entries are structurally nonzero. */
-    template <class RT, class Put>
+    template <int NP = 1, int P = 0, class RT, class Put>
     __device__ __forceinline__ static bool jac(const double (&y)[N], const RT &R, double Tge, double T,
                                                double z, const Put &put)
     {
@@ -414,32 +449,32 @@ struct Net {
         (void)T; (void)z;
         const double H2_1 = y[0];
         mdensity += H2_1;
-        if (H2_1 < 0.0) return false;
+        if (dg_lt0(H2_1)) return false;   /* H2_1 < 0.0 */
         const double H2_2 = y[1];
         mdensity += H2_2;
-        if (H2_2 < 0.0) return false;
+        if (dg_lt0(H2_2)) return false;   /* H2_2 < 0.0 */
         const double H_1 = y[2];
         mdensity += H_1;
-        if (H_1 < 0.0) return false;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
         const double H_2 = y[3];
         mdensity += H_2;
-        if (H_2 < 0.0) return false;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
         const double H_m0 = y[4];
         mdensity += H_m0;
-        if (H_m0 < 0.0) return false;
+        if (dg_lt0(H_m0)) return false;   /* H_m0 < 0.0 */
         const double He_1 = y[5];
         mdensity += He_1;
-        if (He_1 < 0.0) return false;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
         const double He_2 = y[6];
         mdensity += He_2;
-        if (He_2 < 0.0) return false;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
         const double He_3 = y[7];
         mdensity += He_3;
-        if (He_3 < 0.0) return false;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
         const double de = y[8];
-        if (de < 0.0) return false;
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
         const double ge = y[9];
-        if (ge < 0.0) return false;
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
         mdensity *= mh;
         const double k01 = R[0];
         const double k02 = R[1];
@@ -491,167 +526,367 @@ struct Net {
         const double rmd = 1.0 / mdensity;
         (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
-        jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
-        put(0, 0, jv);
-        jv = k11*H_2;
-        put(1, 0, jv);
-        jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
-        put(2, 0, jv);
-        jv = -k11*H_2 + 2*k12*de;
-        put(3, 0, jv);
-        put.zero(4, 0);
-        put.zero(5, 0);
-        put.zero(6, 0);
-        put.zero(7, 0);
-        put.zero(8, 0);
-        jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0);
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 0, jv);
-        jv = k10*H_1 + k19*H_m0;
-        put(0, 1, jv);
-        jv = -k10*H_1 - k18*de - k19*H_m0;
-        put(1, 1, jv);
-        jv = -k10*H_1 + 2*k18*de + k19*H_m0;
-        put(2, 1, jv);
-        jv = k10*H_1;
-        put(3, 1, jv);
-        jv = -k19*H_m0;
-        put(4, 1, jv);
-        put.zero(5, 1);
-        put.zero(6, 1);
-        put.zero(7, 1);
-        jv = -k18*de;
-        put(8, 1, jv);
-        put(9, 1, zero_row);
-        jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
-        put(0, 2, jv);
-        jv = k09*H_2 - k10*H2_2;
-        put(1, 2, jv);
-        jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
-        put(2, 2, jv);
-        jv = k01*de - k09*H_2 + k10*H2_2;
-        put(3, 2, jv);
-        jv = k07*de - k08*H_m0 - k15*H_m0;
-        put(4, 2, jv);
-        put.zero(5, 2);
-        put.zero(6, 2);
-        put.zero(7, 2);
-        jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
-        put(8, 2, jv);
-        jv = -H2_1*gloverabel08_gaHI*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H2_1*h2formation_h2mcool + 3*dg_ipow<2>(H_1)*h2formation_h2mheat - ceHI_ceHI*de - ciHI_ciHI*de;
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 2, jv);
-        jv = -k11*H2_1;
-        put(0, 3, jv);
-        jv = k09*H_1 + k11*H2_1 + k17*H_m0;
-        put(1, 3, jv);
-        jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
-        put(2, 3, jv);
-        jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
-        put(3, 3, jv);
-        jv = -k16*H_m0 - k17*H_m0;
-        put(4, 3, jv);
-        put.zero(5, 3);
-        put.zero(6, 3);
-        put.zero(7, 3);
-        jv = -k02*de + k17*H_m0;
-        put(8, 3, jv);
-        jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 3, jv);
-        jv = k08*H_1 + k19*H2_2;
-        put(0, 4, jv);
-        jv = k17*H_2 - k19*H2_2;
-        put(1, 4, jv);
-        jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
-        put(2, 4, jv);
-        jv = -k16*H_2 - k17*H_2;
-        put(3, 4, jv);
-        jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
-        put(4, 4, jv);
-        put.zero(5, 4);
-        put.zero(6, 4);
-        put.zero(7, 4);
-        jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
-        put(8, 4, jv);
-        put(9, 4, zero_row);
-        put.zero(0, 5);
-        put.zero(1, 5);
-        put.zero(2, 5);
-        put.zero(3, 5);
-        put.zero(4, 5);
-        jv = -k03*de;
-        put(5, 5, jv);
-        jv = k03*de;
-        put(6, 5, jv);
-        put.zero(7, 5);
-        jv = k03*de;
-        put(8, 5, jv);
-        jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 5, jv);
-        put.zero(0, 6);
-        put.zero(1, 6);
-        put.zero(2, 6);
-        put.zero(3, 6);
-        put.zero(4, 6);
-        jv = k04*de;
-        put(5, 6, jv);
-        jv = -k04*de - k05*de;
-        put(6, 6, jv);
-        jv = k05*de;
-        put(7, 6, jv);
-        jv = -k04*de + k05*de;
-        put(8, 6, jv);
-        jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 6, jv);
-        put.zero(0, 7);
-        put.zero(1, 7);
-        put.zero(2, 7);
-        put.zero(3, 7);
-        put.zero(4, 7);
-        put.zero(5, 7);
-        jv = k06*de;
-        put(6, 7, jv);
-        jv = -k06*de;
-        put(7, 7, jv);
-        jv = -k06*de;
-        put(8, 7, jv);
-        jv = -4.0*brem_brem*de - de*reHeIII_reHeIII;
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 7, jv);
-        jv = -k12*H2_1;
-        put(0, 8, jv);
-        jv = -k18*H2_2;
-        put(1, 8, jv);
-        jv = -k01*H_1 + k02*H_2 - k07*H_1 + k14*H_m0 + 2*k18*H2_2;
-        put(2, 8, jv);
-        jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
-        put(3, 8, jv);
-        jv = k07*H_1 - k14*H_m0;
-        put(4, 8, jv);
-        jv = -k03*He_1 + k04*He_2;
-        put(5, 8, jv);
-        jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
-        put(6, 8, jv);
-        jv = k05*He_2 - k06*He_3;
-        put(7, 8, jv);
-        jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
-        put(8, 8, jv);
-        jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0*He_3);
-        jv = dg_div(jv, mdensity, rmd);
-        put(9, 8, jv);
-        put(0, 9, zero_col);
-        put(1, 9, zero_col);
-        put(2, 9, zero_col);
-        put(3, 9, zero_col);
-        put(4, 9, zero_col);
-        put(5, 9, zero_col);
-        put(6, 9, zero_col);
-        put(7, 9, zero_col);
-        put(8, 9, zero_col);
-        put(9, 9, zero_both);
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
+            put(0, 0, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k11*H_2;
+            put(1, 0, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
+            put(2, 0, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -k11*H_2 + 2*k12*de;
+            put(3, 0, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(5, 0);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(7, 0);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(8, 0);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0);
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 0, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k10*H_1 + k19*H_m0;
+            put(0, 1, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -k10*H_1 - k18*de - k19*H_m0;
+            put(1, 1, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -k10*H_1 + 2*k18*de + k19*H_m0;
+            put(2, 1, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k10*H_1;
+            put(3, 1, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -k19*H_m0;
+            put(4, 1, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(5, 1);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 1);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(7, 1);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k18*de;
+            put(8, 1, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put(9, 1, zero_row);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
+            put(0, 2, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = k09*H_2 - k10*H2_2;
+            put(1, 2, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
+            put(2, 2, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k01*de - k09*H_2 + k10*H2_2;
+            put(3, 2, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k07*de - k08*H_m0 - k15*H_m0;
+            put(4, 2, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 2);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 2);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 2);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
+            put(8, 2, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -H2_1*gloverabel08_gaHI*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H2_1*h2formation_h2mcool + 3*dg_ipow<2>(H_1)*h2formation_h2mheat - ceHI_ceHI*de - ciHI_ciHI*de;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 2, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k11*H2_1;
+            put(0, 3, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = k09*H_1 + k11*H2_1 + k17*H_m0;
+            put(1, 3, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
+            put(2, 3, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
+            put(3, 3, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k16*H_m0 - k17*H_m0;
+            put(4, 3, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(5, 3);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(6, 3);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(7, 3);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -k02*de + k17*H_m0;
+            put(8, 3, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 3, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k08*H_1 + k19*H2_2;
+            put(0, 4, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = k17*H_2 - k19*H2_2;
+            put(1, 4, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
+            put(2, 4, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k16*H_2 - k17*H_2;
+            put(3, 4, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
+            put(4, 4, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 4);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(6, 4);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(7, 4);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
+            put(8, 4, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put(9, 4, zero_row);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 5);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 5);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(3, 5);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(4, 5);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k03*de;
+            put(5, 5, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k03*de;
+            put(6, 5, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = k03*de;
+            put(8, 5, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 5, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(0, 6);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(1, 6);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(2, 6);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(3, 6);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(4, 6);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = k04*de;
+            put(5, 6, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k04*de - k05*de;
+            put(6, 6, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k05*de;
+            put(7, 6, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -k04*de + k05*de;
+            put(8, 6, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(0, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(1, 7);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(2, 7);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(3, 7);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 7);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k06*de;
+            put(6, 7, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k06*de;
+            put(7, 7, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k06*de;
+            put(8, 7, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -4.0*brem_brem*de - de*reHeIII_reHeIII;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 7, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k12*H2_1;
+            put(0, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k18*H2_2;
+            put(1, 8, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -k01*H_1 + k02*H_2 - k07*H_1 + k14*H_m0 + 2*k18*H2_2;
+            put(2, 8, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
+            put(3, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k07*H_1 - k14*H_m0;
+            put(4, 8, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -k03*He_1 + k04*He_2;
+            put(5, 8, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
+            put(6, 8, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = k05*He_2 - k06*He_3;
+            put(7, 8, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
+            put(8, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0*He_3);
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put(0, 9, zero_col);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put(1, 9, zero_col);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put(2, 9, zero_col);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put(3, 9, zero_col);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put(4, 9, zero_col);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put(5, 9, zero_col);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put(6, 9, zero_col);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put(7, 9, zero_col);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put(8, 9, zero_col);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put(9, 9, zero_both);
+        }
         return true;
     }
 };

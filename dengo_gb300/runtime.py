@@ -28,7 +28,7 @@ class SolverConfig(C.Structure):
     _fields_ = [("max_newton_sweeps", C.c_int), ("max_substeps", C.c_int),
                 ("dt_ratio_floor", C.c_double), ("floor_value", C.c_double),
                 ("precision", C.c_int), ("schedule", C.c_int),
-                ("block", C.c_int), ("grid", C.c_int)]
+                ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int)]
 
 
 class CellBatch(C.Structure):
@@ -150,6 +150,7 @@ class Solver:
         cfg.max_newton_sweeps, cfg.max_substeps = 10, 50000
         cfg.dt_ratio_floor, cfg.floor_value = 1e-15, 1e-25
         cfg.precision, cfg.schedule, cfg.block, cfg.grid = DENGO_FP64, SCHED_AUTO, 0, 0
+        cfg.warps_per_cell = 1
         return cfg
 
     # ---- reference-shaped host entry points ----------------------------

@@ -86,6 +86,8 @@ typedef struct dengo_solver_config {
     int schedule;              /* enum dengo_schedule  */
     int block;                 /* threads per block, 0 = tuned default */
     int grid;                  /* blocks, 0 = tuned default             */
+    int warps_per_cell;        /* warps sharing each cell's sweep: 1, 2 or
+                                  4 (32 cells per group of warps); 0 = tuned */
 } dengo_solver_config;
 
 void dengo_default_config(dengo_solver_config *cfg);

@@ -94,3 +94,42 @@ def test_integer_powers(lib):
         exact4 = Fraction(x) ** 4
         assert abs(Fraction(lib.h_pow4(x)) - exact4) <= Fraction(math.ulp(lib.h_pow4(x))) / 2
     assert misround3 / len(xs) < 5e-3
+
+
+CMP_SRC = r'''
+#include "dg_math.h"
+extern "C" int h_cmp(double a, double b) {
+    int r = 0;
+    r |= (dg_isnan(a) == (a != a)) << 0;
+    r |= (dg_nonzero(a) == (a != 0.0)) << 1;
+    r |= (dg_lt0(a) == (a < 0.0)) << 2;
+    r |= (dg_abs_gt(a, b) == (fabs(a) > fabs(b))) << 3;
+    r |= (dg_abs_gt_val(a, b) == (fabs(a) > b)) << 4;
+    r |= (b > 0 ? (dg_lt_pos(a, b) == (a < b)) : 1) << 5;
+    r |= (dg_finite(a) == (bool)isfinite(a)) << 6;
+    return r;
+}
+'''
+
+
+def test_integer_comparisons_match_ieee(tmp_path):
+    """The bit-pattern comparisons used on the device agree with the C
+    operators on every class of value (zeros of both signs, subnormals,
+    normals, infinities, NaNs)."""
+    src = tmp_path / "c.cpp"
+    src.write_text(CMP_SRC)
+    so = tmp_path / "c.so"
+    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                           "-I", os.path.join(ROOT, "dengo_gb300", "csrc"), str(src),
+                           "-o", str(so)])
+    L = C.CDLL(str(so))
+    L.h_cmp.restype = C.c_int
+    L.h_cmp.argtypes = [C.c_double, C.c_double]
+    special = [0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1e-25, -1e-25, 1.0, -1.0,
+               1.5, 1e308, -1e308, math.inf, -math.inf, math.nan, -math.nan]
+    rng = np.random.default_rng(5)
+    rand = list(np.ldexp(rng.uniform(-2, 2, 300), rng.integers(-1074, 1024, 300)))
+    vals = special + [float(v) for v in rand]
+    for a in vals:
+        for b in special + [float(v) for v in rand[:40]]:
+            assert L.h_cmp(a, b) == 0x7F, (a, b, bin(L.h_cmp(a, b)))

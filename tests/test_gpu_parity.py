@@ -130,6 +130,70 @@ def test_layouts_and_schedules_bit_identical(solver):
         assert np.array_equal(got[1], base[1]) and np.array_equal(got[2], base[2])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_split_engine_bit_identical(solver, golden, precision):
+    """2 and 4 warps per cell give the single-lane engine's exact bits."""
+    import torch
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(200, "config3", seed=77)
+    state = np.concatenate([state, golden["evolve_edge_in"]])
+    dtf = np.concatenate([dtf, golden["evolve_edge_dtf"]])
+    dt0 = np.concatenate([np.full(200, -1.0), golden["evolve_edge_dt0"]])
+    n = len(dtf)
+    outs = []
+    for wpc in (1, 2, 4):
+        st = torch.tensor(state.T.copy(), device="cuda")
+        at = st * 1e-6
+        status = torch.zeros(n, dtype=torch.int32, device="cuda")
+        sweeps = torch.zeros(n, dtype=torch.int32, device="cuda")
+        dt = torch.tensor(dt0, device="cuda")
+        cfg = Solver.default_config()
+        cfg.precision, cfg.warps_per_cell = precision, wpc
+        solver.solve_device(st, n, 1, n, at, dtf=torch.tensor(dtf, device="cuda"), dt=dt,
+                            status=status, sweeps=sweeps, config=cfg,
+                            stream=torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        outs.append([x.cpu().numpy() for x in (st, at, dt, status, sweeps)])
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+
+
+def test_cost_hint_order_does_not_change_results(solver):
+    import torch
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(500, "config3", seed=9)
+    outs = []
+    for hint in (None, np.random.default_rng(0).integers(0, 10**6, 500).astype(np.int32)):
+        st = torch.tensor(state.T.copy(), device="cuda")
+        at = st * 1e-6
+        status = torch.zeros(500, dtype=torch.int32, device="cuda")
+        h = None if hint is None else torch.tensor(hint, device="cuda")
+        solver.solve_device(st, 500, 1, 500, at, dtf=torch.tensor(dtf, device="cuda"),
+                            status=status, stream=torch.cuda.current_stream(), cost_hint=h)
+        torch.cuda.synchronize()
+        outs.append((st.cpu().numpy(), status.cpu().numpy()))
+    assert np.array_equal(outs[0][0].view(np.int64), outs[1][0].view(np.int64))
+    assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_mixed_precision_within_1e6_of_oracle(solver, oracle):
+    """Mixed path (FP32 LU, FP64 residual): converged cells within 1e-6
+    relative of the FP64 oracle (the spec bar for this path)."""
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(96, "config1", seed=404)
+    cfg = Solver.default_config()
+    cfg.precision = 1
+    out = solver.solve_host(state, dtf, rtol=1e-6, config=cfg)
+    ref = oracle.evolve_cells(solver._tables, state, dtf, nthreads=0)
+    ok = (ref["status"] == 0) & (out["status"] == 0)
+    assert ok.sum() >= 0.9 * (ref["status"] == 0).sum()
+    err = rel_err(out["state"][ok], ref["state"][ok])
+    assert err.max(initial=0.0) <= 1e-6, err.max()
+
+
 def test_batch_invariance(solver):
     """A cell's result does not depend on the cells solved beside it."""
     from dengo_gb300.workloads import primordial_cells
