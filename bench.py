@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--order", type=int, default=1, help="start the costliest cells first")
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    p.add_argument("--warps-per-cell", type=int, default=1, choices=[1, 2, 4])
+    p.add_argument("--warps-per-cell", type=int, default=4, choices=[1, 2, 4])
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
