@@ -2,7 +2,8 @@
 
 Each shipped network's generated sources live in
 ``dengo_gb300/generated/<name>/``; ``build_network`` compiles
-``<name>_solver.cu`` into ``lib<name>_solver.so`` next to it.  The FP64
+``<name>_solver.cu`` -- once for the entry points and once per engine variant,
+in parallel -- into ``lib<name>_solver.so`` next to it.  The FP64
 engine must not contract multiply-adds (``--fmad=false``) to reproduce the
 reference's arithmetic; deliberate FMAs are written as intrinsics.
 """
@@ -11,6 +12,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 from concurrent.futures import ThreadPoolExecutor
 
 PKG = os.path.dirname(os.path.abspath(__file__))
@@ -21,7 +23,7 @@ GENERATED = os.path.join(PKG, "generated")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-shared", "-Xcompiler", "-ffp-contract=off"]
+              "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc():
@@ -39,31 +41,71 @@ def library_path(name):
     return os.path.join(network_dir(name), "lib%s_solver.so" % name)
 
 
-def build_network(name, src_dir=None, out=None, verbose=False, extra=()):
-    src_dir = src_dir or network_dir(name)
-    out = out or os.path.join(src_dir, "lib%s_solver.so" % name)
-    src = os.path.join(src_dir, "%s_solver.cu" % name)
-    cmd = [nvcc()] + ARCH_FLAGS + NVCC_FLAGS + list(extra) + [
-        "-I", INCLUDE, "-I", CSRC, "-I", src_dir, src, "-o", out]
+def _run(cmd, what, verbose):
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
         print(" ".join(cmd))
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (name, res.stdout, res.stderr))
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (what, res.stdout, res.stderr))
     if verbose:
         sys.stderr.write(res.stderr)
-    return out
+
+
+class _NetworkBuild:
+    """The translation units of one network library: the entry points
+    (-DDG_SPLIT_KERNELS) and one unit per engine variant
+    (-DDG_KERNEL_PART=k), linked into lib<name>_solver.so."""
+
+    def __init__(self, name, src_dir, out, tmp, verbose, extra):
+        from .codegen import ENGINE_VARIANTS
+        self.name, self.out, self.verbose = name, out, verbose
+        src = os.path.join(src_dir, "%s_solver.cu" % name)
+        base = [nvcc()] + (["-Xptxas=-v"] if verbose else []) + ARCH_FLAGS + NVCC_FLAGS + \
+            list(extra) + ["-I", INCLUDE, "-I", CSRC, "-I", src_dir, "-c", src]
+        defs = ["-DDG_SPLIT_KERNELS"] + ["-DDG_KERNEL_PART=%d" % k
+                                         for k in range(len(ENGINE_VARIANTS))]
+        self.objs = [os.path.join(tmp, "%s_%d.o" % (name, i)) for i in range(len(defs))]
+        self.compiles = [base + [d, "-o", o] for d, o in zip(defs, self.objs)]
+
+    def compile(self, i):
+        _run(self.compiles[i], "%s (unit %d)" % (self.name, i), self.verbose)
+
+    def link(self):
+        _run([nvcc()] + ARCH_FLAGS + ["-shared", "-Xcompiler", "-fPIC"] + self.objs +
+             ["-o", self.out], "%s (link)" % self.name, self.verbose)
+        return self.out
+
+
+def _build(builds, extra_jobs=(), verbose=False):
+    with tempfile.TemporaryDirectory(prefix="dg_build_") as tmp:
+        nb = [b(tmp) for b in builds]
+        units = [(b, i) for b in nb for i in range(len(b.compiles))]
+        workers = max(2, min(len(units) + len(extra_jobs), os.cpu_count() or 4))
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            extra = [ex.submit(j) for j in extra_jobs]
+            for f in [ex.submit(b.compile, i) for b, i in units]:
+                f.result()
+            outs = [f.result() for f in [ex.submit(b.link) for b in nb]]
+            return outs + [f.result() for f in extra]
+
+
+def build_network(name, src_dir=None, out=None, verbose=False, extra=()):
+    """lib<name>_solver.so from generated/<name>/<name>_solver.cu (its units
+    compiled in parallel)."""
+    src_dir = src_dir or network_dir(name)
+    out = out or os.path.join(src_dir, "lib%s_solver.so" % name)
+    return _build([lambda tmp: _NetworkBuild(name, src_dir, out, tmp, verbose, extra)],
+                  verbose=verbose)[0]
 
 
 def build_all(names=None, verbose=False):
     """Every CUDA library of the package: one per shipped network plus the
-    peak microbenchmark, compiled in parallel."""
+    peak microbenchmark, all translation units compiled in parallel."""
     from .networks import SHIPPED_NETWORKS
     names = list(names or SHIPPED_NETWORKS)
-    jobs = [lambda n=n: build_network(n, verbose=verbose) for n in names] + [build_peak]
-    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        return [f.result() for f in [ex.submit(j) for j in jobs]]
+    builds = [lambda tmp, n=n: _NetworkBuild(n, network_dir(n), library_path(n), tmp, verbose, ())
+              for n in names]
+    return _build(builds, extra_jobs=[build_peak], verbose=verbose)
 
 
 def generate(name):

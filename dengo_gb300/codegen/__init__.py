@@ -32,6 +32,12 @@ def _env():
                               keep_trailing_newline=True, undefined=jinja2.StrictUndefined)
 
 
+# The engine kernels one network library holds, one translation unit each in
+# the package build: (launcher, BLOCK or warps per cell, mixed precision).
+ENGINE_VARIANTS = [("launch_lane", b, m) for b in (32, 64, 128) for m in ("false", "true")] + \
+                  [("launch_split", w, m) for w in (2, 4) for m in ("false", "true")]
+
+
 def render_solver(net, name, output_dir, family="rates_and_rate_tables"):
     if family not in FAMILIES:
         raise KeyError("unknown solver template family %r (known: %s)"
@@ -40,7 +46,7 @@ def render_solver(net, name, output_dir, family="rates_and_rate_tables"):
     env = _env()
     paths = []
     for suffix, tname in FAMILIES[family]:
-        text = env.get_template(tname).render(s=spec, n=name)
+        text = env.get_template(tname).render(s=spec, n=name, variants=ENGINE_VARIANTS)
         path = os.path.join(output_dir, "%s_solver%s" % (name, suffix))
         with open(path, "w") as f:
             f.write(text)

@@ -96,6 +96,10 @@ class NetworkSpec:
     def nnz(self):
         return sum(sum(1 for v in col if v) for col in self.jac_nonzero)
 
+    def jac_col_mask(self, var):
+        """Bit q set when d rhs_q / d y_var is structurally nonzero."""
+        return sum(1 << q for q, v in enumerate(self.jac_nonzero[var]) if v)
+
 
 _GAMMA_DIV = re.compile(r"\b([A-Za-z_][A-Za-z0-9_]*)/\(gamma - 1\.0\)")
 

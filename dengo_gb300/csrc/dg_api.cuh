@@ -71,7 +71,20 @@ struct Gpu {
     int *order_counts = nullptr;  /* [64]: bucket counts and offsets */
 };
 
-/* Builds g->order (longest first) from the per-cell cost hint on stream st. */
+/* Writes order[0..n) (longest first) from the per-cell cost hint on stream
+ * st; counts: 64 ints of scratch (bucket counts, then offsets). */
+inline int launch_order(const int *cost, long long n, int *counts, int *order, cudaStream_t st)
+{
+    DG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * 64, st));
+    const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+    order_count_kernel<<<grid, 256, 0, st>>>(cost, n, counts);
+    order_scan_kernel<<<1, 1, 0, st>>>(counts, counts + 32);
+    order_scatter_kernel<<<grid, 256, 0, st>>>(cost, n, counts + 32, order);
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+/* Builds g->order from the cost hint, growing the context's buffers. */
 inline int build_order(Gpu *g, const int *cost, long long n, cudaStream_t st)
 {
     if (n > g->order_cap) {
@@ -82,13 +95,30 @@ inline int build_order(Gpu *g, const int *cost, long long n, cudaStream_t st)
         g->order_cap = n;
     }
     if (!g->order_counts) DG_CUDA(cudaMalloc(&g->order_counts, sizeof(int) * 64));
-    DG_CUDA(cudaMemsetAsync(g->order_counts, 0, sizeof(int) * 64, st));
-    const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-    order_count_kernel<<<grid, 256, 0, st>>>(cost, n, g->order_counts);
-    order_scan_kernel<<<1, 1, 0, st>>>(g->order_counts, g->order_counts + 32);
-    order_scatter_kernel<<<grid, 256, 0, st>>>(cost, n, g->order_counts + 32, g->order);
-    DG_CUDA(cudaGetLastError());
-    return 0;
+    return launch_order(cost, n, g->order_counts, g->order, st);
+}
+
+/* The kernel's view of a caller's batch. */
+inline CellIO cell_io(const dengo_cell_batch *b)
+{
+    CellIO io{};
+    io.state = b->state;
+    io.atol = b->atol;
+    io.rtol = b->rtol;
+    io.rtol_scalar = b->rtol_scalar;
+    io.dtf = b->dtf;
+    io.dtf_scalar = b->dtf_scalar;
+    io.dt = b->dt;
+    io.ttot = b->ttot;
+    io.status = b->status;
+    io.substeps = b->substeps;
+    io.sweeps = b->sweeps;
+    io.failures = b->failures;
+    io.cs = b->cell_stride;
+    io.ss = b->species_stride;
+    io.ncells = b->ncells;
+    io.order = nullptr;
+    return io;
 }
 
 inline int ensure_device_buf(Gpu *g, size_t bytes)
@@ -122,6 +152,133 @@ inline size_t carve_size(std::initializer_list<size_t> bytes)
     size_t s = 0;
     for (size_t b : bytes) s = ((s + 255) & ~(size_t)255) + b;
     return s + 256;
+}
+
+/* ---------------- engine launches ----------------
+ * One function per engine variant.  The package build compiles each variant's
+ * kernel in a translation unit of its own (the generated solver file with
+ * -DDG_KERNEL_PART=k) and declares the others extern in the entry points'
+ * unit, so one network's kernels compile in parallel; compiled as a single
+ * unit the file instantiates them all.  queue: the work-queue counter used by
+ * DENGO_SCHED_QUEUE and DENGO_SCHED_AUTO. */
+#define DG_LAUNCH_ARGS \
+    ::dg::Gpu *, const ::dg::CellIO &, const ::dg::KernelCfg &, int, int, cudaStream_t, unsigned long long *
+
+/* Opt a kernel into its dynamic shared memory once per device (bit `dev` of
+ * `done`), so that launches inside a stream capture record only the launch
+ * and its queue reset. */
+template <class K>
+inline int smem_attribute_once(K kern, size_t smem, unsigned long long &done)
+{
+    int dev = 0;
+    DG_CUDA(cudaGetDevice(&dev));
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(done & bit)) {
+        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        done |= bit;
+    }
+    return 0;
+}
+
+/* Grid of a persistent launch: as many CTAs as fit on the device at once
+ * (occupancy), fewer when the cells do not fill them. */
+template <class K>
+inline int persistent_grid(const Gpu *g, K kern, int threads, size_t smem, long long need, int grid,
+                           int *err)
+{
+    int per_sm = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) {
+        set_error("cudaOccupancyMaxActiveBlocksPerMultiprocessor failed: %s", cudaGetErrorString(e));
+        *err = (int)e;
+        return 0;
+    }
+    if (per_sm < 1) per_sm = 1;
+    const long long full = (long long)g->nsm * per_sm;
+    return grid > 0 ? grid : (int)(need < full ? need : full);
+}
+
+/* The single-lane engine (dg_engine.cuh), BLOCK cells per CTA. */
+template <class Net, int BLOCK, bool MIXED>
+int launch_lane(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
+                cudaStream_t st, unsigned long long *queue)
+{
+    auto kern = evolve_kernel<Net, BLOCK, MIXED>;
+    const size_t smem = Lane<Net, BLOCK, MIXED>::smem_bytes();
+    static unsigned long long attr_done = 0;
+    if (int e = smem_attribute_once(kern, smem, attr_done)) return e;
+    if (io.ncells <= 0) return 0;
+    const long long need = (io.ncells + BLOCK - 1) / BLOCK;
+    unsigned long long *q = nullptr;
+    if (schedule == DENGO_SCHED_PER_THREAD) {
+        grid = (int)need;
+    } else {
+        int err = 0;
+        grid = persistent_grid(g, kern, BLOCK, smem, need, grid, &err);
+        if (err) return err;
+        if (schedule != DENGO_SCHED_STRIDE) {
+            q = queue;
+            DG_CUDA(cudaMemsetAsync(q, 0, sizeof(*q), st));
+        }
+    }
+    kern<<<grid, BLOCK, smem, st>>>(io, g->ts, kc, q);
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+/* The split engine (dg_split.cuh): 32 cells per CTA, NP warps per cell. */
+template <class Net, int NP, bool MIXED>
+int launch_split(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
+                 cudaStream_t st, unsigned long long *queue)
+{
+    auto kern = evolve_split_kernel<Net, NP, MIXED>;
+    const size_t smem = SplitLayout<Net, NP, MIXED>::bytes();
+    static unsigned long long attr_done = 0;
+    if (int e = smem_attribute_once(kern, smem, attr_done)) return e;
+    if (io.ncells <= 0) return 0;
+    const long long need = (io.ncells + 31) / 32;
+    unsigned long long *q = nullptr;
+    if (schedule == DENGO_SCHED_PER_THREAD) {
+        grid = (int)need;
+    } else {
+        int err = 0;
+        grid = persistent_grid(g, kern, 32 * NP, smem, need, grid, &err);
+        if (err) return err;
+        if (schedule != DENGO_SCHED_STRIDE) {
+            q = queue;
+            DG_CUDA(cudaMemsetAsync(q, 0, sizeof(*q), st));
+        }
+    }
+    kern<<<grid, 32 * NP, smem, st>>>(io, g->ts, kc, q);
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+/* The variant a configuration selects: warps_per_cell 2 or 4 runs the split
+ * engine, anything else the single-lane engine with block 32, 64 or 128. */
+template <class Net>
+int launch_engine(Gpu *g, const CellIO &io, const KernelCfg &kc, const dengo_solver_config &cfg,
+                  cudaStream_t st, unsigned long long *queue)
+{
+    const bool mixed = cfg.precision == DENGO_MIXED;
+    const int sch = cfg.schedule, gr = cfg.grid;
+    if (cfg.warps_per_cell == 2)
+        return mixed ? launch_split<Net, 2, true>(g, io, kc, sch, gr, st, queue)
+                     : launch_split<Net, 2, false>(g, io, kc, sch, gr, st, queue);
+    if (cfg.warps_per_cell == 4)
+        return mixed ? launch_split<Net, 4, true>(g, io, kc, sch, gr, st, queue)
+                     : launch_split<Net, 4, false>(g, io, kc, sch, gr, st, queue);
+    switch (cfg.block) {
+    case 32:
+        return mixed ? launch_lane<Net, 32, true>(g, io, kc, sch, gr, st, queue)
+                     : launch_lane<Net, 32, false>(g, io, kc, sch, gr, st, queue);
+    case 128:
+        return mixed ? launch_lane<Net, 128, true>(g, io, kc, sch, gr, st, queue)
+                     : launch_lane<Net, 128, false>(g, io, kc, sch, gr, st, queue);
+    default:
+        return mixed ? launch_lane<Net, 64, true>(g, io, kc, sch, gr, st, queue)
+                     : launch_lane<Net, 64, false>(g, io, kc, sch, gr, st, queue);
+    }
 }
 
 template <class Net>
@@ -301,63 +458,6 @@ struct Api {
     }
 
     /* ---------------- the solver ---------------- */
-    template <int BLOCK, bool MIXED>
-    static int launch(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
-                      cudaStream_t st)
-    {
-        auto kern = evolve_kernel<Net, BLOCK, MIXED>;
-        const size_t smem = Lane<Net, BLOCK, MIXED>::smem_bytes();
-        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        if (io.ncells <= 0) return 0;
-        const long long need = (io.ncells + BLOCK - 1) / BLOCK;
-        unsigned long long *queue = nullptr;
-        if (schedule == DENGO_SCHED_PER_THREAD) {
-            grid = (int)need;
-        } else {
-            int per_sm = 0;
-            DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
-            if (per_sm < 1) per_sm = 1;
-            const long long full = (long long)g->nsm * per_sm;
-            if (grid <= 0) grid = (int)(need < full ? need : full);
-            if (schedule != DENGO_SCHED_STRIDE) {
-                queue = g->queue;
-                DG_CUDA(cudaMemsetAsync(queue, 0, sizeof(*queue), st));
-            }
-        }
-        kern<<<grid, BLOCK, smem, st>>>(io, g->ts, kc, queue);
-        DG_CUDA(cudaGetLastError());
-        return 0;
-    }
-
-    /* The split engine: 32 cells per CTA, NP warps per cell (dg_split.cuh). */
-    template <int NP, bool MIXED>
-    static int launch_split(Gpu *g, const CellIO &io, const KernelCfg &kc, int schedule, int grid,
-                            cudaStream_t st)
-    {
-        auto kern = evolve_split_kernel<Net, NP, MIXED>;
-        const size_t smem = SplitLayout<Net, NP, MIXED>::bytes();
-        DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        if (io.ncells <= 0) return 0;
-        const long long need = (io.ncells + 31) / 32;
-        unsigned long long *queue = nullptr;
-        if (schedule == DENGO_SCHED_PER_THREAD) {
-            grid = (int)need;
-        } else {
-            int per_sm = 0;
-            DG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * NP, smem));
-            if (per_sm < 1) per_sm = 1;
-            const long long full = (long long)g->nsm * per_sm;
-            if (grid <= 0) grid = (int)(need < full ? need : full);
-            if (schedule != DENGO_SCHED_STRIDE) {
-                queue = g->queue;
-                DG_CUDA(cudaMemsetAsync(queue, 0, sizeof(*queue), st));
-            }
-        }
-        kern<<<grid, 32 * NP, smem, st>>>(io, g->ts, kc, queue);
-        DG_CUDA(cudaGetLastError());
-        return 0;
-    }
-
     static int solve_device(Data *d, const dengo_cell_batch *b, double z,
                             const dengo_solver_config *cfg_in, void *stream)
     {
@@ -376,47 +476,14 @@ struct Api {
         /* NULL is the default stream, as everywhere in CUDA */
         cudaStream_t st = (cudaStream_t)stream;
         if (load_z(d, z, st) != 0) return -1;
-        CellIO io{};
-        io.state = b->state;
-        io.atol = b->atol;
-        io.rtol = b->rtol;
-        io.rtol_scalar = b->rtol_scalar;
-        io.dtf = b->dtf;
-        io.dtf_scalar = b->dtf_scalar;
-        io.dt = b->dt;
-        io.ttot = b->ttot;
-        io.status = b->status;
-        io.substeps = b->substeps;
-        io.sweeps = b->sweeps;
-        io.failures = b->failures;
-        io.cs = b->cell_stride;
-        io.ss = b->species_stride;
-        io.ncells = b->ncells;
-        io.order = nullptr;
+        CellIO io = cell_io(b);
         if (b->cost_hint && b->ncells > 0) {
             if (build_order(g, b->cost_hint, b->ncells, st) != 0) return -1;
             io.order = g->order;
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         g->ts.z = z;
-        const bool mixed = cfg.precision == DENGO_MIXED;
-        if (cfg.warps_per_cell == 2)
-            return mixed ? launch_split<2, true>(g, io, kc, cfg.schedule, cfg.grid, st)
-                         : launch_split<2, false>(g, io, kc, cfg.schedule, cfg.grid, st);
-        if (cfg.warps_per_cell == 4)
-            return mixed ? launch_split<4, true>(g, io, kc, cfg.schedule, cfg.grid, st)
-                         : launch_split<4, false>(g, io, kc, cfg.schedule, cfg.grid, st);
-        switch (cfg.block) {
-        case 32:
-            return mixed ? launch<32, true>(g, io, kc, cfg.schedule, cfg.grid, st)
-                         : launch<32, false>(g, io, kc, cfg.schedule, cfg.grid, st);
-        case 128:
-            return mixed ? launch<128, true>(g, io, kc, cfg.schedule, cfg.grid, st)
-                         : launch<128, false>(g, io, kc, cfg.schedule, cfg.grid, st);
-        default:
-            return mixed ? launch<64, true>(g, io, kc, cfg.schedule, cfg.grid, st)
-                         : launch<64, false>(g, io, kc, cfg.schedule, cfg.grid, st);
-        }
+        return launch_engine<Net>(g, io, kc, cfg, st, g->queue);
     }
 
     /* <n>_solve_cells_host: the batch's pointers are host pointers.  The
@@ -731,6 +798,76 @@ struct Api {
         DG_CUDA(cudaMemcpyAsync(&ret, s.b.flag, 4, cudaMemcpyDeviceToHost, st));
         DG_CUDA(cudaStreamSynchronize(st));
         return ret;
+    }
+
+    /* <n>_run_strip: the Cython driver run_<n> on one strip (number
+     * densities after its mass-to-number conversion; host arrays).  Returns
+     * the iterations taken, or -1 with the error message set.  The
+     * trajectory pointers may be null. */
+    static int run_strip(Data *d, double tf, int niter, double z, double *input, double *rtol,
+                         double *atol, int nstrip, double *ttot, double *dt, double *traj,
+                         double *traj_T, unsigned char *traj_ok, double *traj_t, double *traj_dt)
+    {
+        if (!d || !input || !rtol || !atol || !ttot || !dt) {
+            set_error("%s_run_strip: null argument", Net::NAME);
+            return -1;
+        }
+        if (nstrip <= 0 || nstrip > DENGO_MAX_NCELLS || niter <= 0) {
+            set_error("%s_run_strip: nstrip %d outside [1, %d] or niter %d < 1", Net::NAME, nstrip,
+                      DENGO_MAX_NCELLS, niter);
+            return -1;
+        }
+        Gpu *g = gpu(d);
+        cudaStream_t st = g->stream;
+        d->current_z = z;
+        if (load_z(d, z, st) != 0) return -1;
+        const size_t cells = (size_t)nstrip * N, it = (size_t)niter;
+        const bool want = traj || traj_T || traj_ok || traj_t || traj_dt;
+        if (ensure_device_buf(g, carve_size({3 * cells * 8, 3 * 8, 64, want ? it * cells * 8 : 0,
+                                             want ? it * nstrip * 8 : 0, want ? it : 0,
+                                             want ? 2 * it * 8 : 0})) != 0)
+            return -1;
+        Carve cv{g->d_buf};
+        double *din = cv.take<double>(cells), *drt = cv.take<double>(cells),
+               *dat = cv.take<double>(cells), *dsc = cv.take<double>(3);
+        RunOut o{};
+        o.ttot = dsc;
+        o.dt = dsc + 1;
+        o.iters = cv.take<int>(16);
+        if (want) {
+            o.traj = traj ? cv.take<double>(it * cells) : nullptr;
+            o.traj_T = traj_T ? cv.take<double>(it * nstrip) : nullptr;
+            o.traj_ok = traj_ok ? cv.take<unsigned char>(it) : nullptr;
+            o.traj_t = traj_t ? cv.take<double>(it) : nullptr;
+            o.traj_dt = traj_dt ? cv.take<double>(it) : nullptr;
+            if (o.traj) DG_CUDA(cudaMemsetAsync(o.traj, 0, it * cells * 8, st));
+            if (o.traj_T) DG_CUDA(cudaMemsetAsync(o.traj_T, 0, it * nstrip * 8, st));
+            if (o.traj_ok) DG_CUDA(cudaMemsetAsync(o.traj_ok, 0, it, st));
+            if (o.traj_t) DG_CUDA(cudaMemsetAsync(o.traj_t, 0, it * 8, st));
+            if (o.traj_dt) DG_CUDA(cudaMemsetAsync(o.traj_dt, 0, it * 8, st));
+        }
+        DG_CUDA(cudaMemcpyAsync(din, input, cells * 8, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(drt, rtol, cells * 8, cudaMemcpyHostToDevice, st));
+        DG_CUDA(cudaMemcpyAsync(dat, atol, cells * 8, cudaMemcpyHostToDevice, st));
+        TableSet ts = g->ts;
+        ts.z = z;
+        const int threads = ((nstrip + 31) / 32) * 32;
+        run_strip_kernel<Net><<<1, threads, 0, st>>>(din, drt, dat, nstrip, tf, niter, ts, 10, o);
+        DG_CUDA(cudaGetLastError());
+        int iters = 0;
+        DG_CUDA(cudaMemcpyAsync(input, din, cells * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(atol, dat, cells * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(ttot, o.ttot, 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(dt, o.dt, 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaMemcpyAsync(&iters, o.iters, 4, cudaMemcpyDeviceToHost, st));
+        if (traj) DG_CUDA(cudaMemcpyAsync(traj, o.traj, it * cells * 8, cudaMemcpyDeviceToHost, st));
+        if (traj_T)
+            DG_CUDA(cudaMemcpyAsync(traj_T, o.traj_T, it * nstrip * 8, cudaMemcpyDeviceToHost, st));
+        if (traj_ok) DG_CUDA(cudaMemcpyAsync(traj_ok, o.traj_ok, it, cudaMemcpyDeviceToHost, st));
+        if (traj_t) DG_CUDA(cudaMemcpyAsync(traj_t, o.traj_t, it * 8, cudaMemcpyDeviceToHost, st));
+        if (traj_dt) DG_CUDA(cudaMemcpyAsync(traj_dt, o.traj_dt, it * 8, cudaMemcpyDeviceToHost, st));
+        DG_CUDA(cudaStreamSynchronize(st));
+        return iters;
     }
 
     /* Needs no data struct: uses a context-free temporary stream. */

@@ -28,6 +28,8 @@
 #include <stdint.h>
 
 #include "dg_math.h"
+#include "dg_slots.cuh"
+#include "dg_mixed.cuh"
 #include "dengo_gb300.h"
 
 namespace dg {
@@ -70,22 +72,15 @@ struct KernelCfg {
     double floor_value;
 };
 
-/* One double per thread in a [slots][BLOCK] shared-memory array: thread
- * tid's slot i is p[i * BLOCK], so a warp's accesses are conflict-free. */
-template <int BLOCK>
-struct Slots {
-    double *p;
-    __device__ __forceinline__ double &operator[](int i) const { return p[i * BLOCK]; }
-};
-
 template <class Net, int BLOCK, bool MIXED = false>
 struct Lane {
     static constexpr int N = Net::N;
     static constexpr int NT = Net::NT;
-    /* shared-memory slot map, in doubles per thread; the mixed path keeps
-     * the matrix in FP32 (half the slots) */
+    /* shared-memory slot map, in doubles per thread; the mixed path adds
+     * the FP32 factors (half a slot per entry) after the FP64 matrix */
     static constexpr int OFF_J = 0;
-    static constexpr int OFF_R = OFF_J + (MIXED ? (N * N + 1) / 2 : N * N);
+    static constexpr int OFF_JF = OFF_J + N * N;
+    static constexpr int OFF_R = OFF_JF + (MIXED ? (N * N + 1) / 2 : 0);
     static constexpr int OFF_PREV = OFF_R + NT;
     static constexpr int OFF_SC = OFF_PREV + N;
     static constexpr int OFF_INV = OFF_SC + N;
@@ -261,89 +256,6 @@ __device__ __forceinline__ void gauss_elim_fast(Slots<BLOCK> J, double (&x)[N])
     }
 }
 
-/* FP32 storage of the scaled matrix for the mixed-precision path. */
-template <int BLOCK>
-struct SlotsF {
-    float *p;
-    __device__ __forceinline__ float &operator[](int i) const { return p[i * BLOCK]; }
-};
-
-/* Partial-pivot LU and solve in FP32 (mixed precision): the same algorithm
- * as Gauss_Elim, on the FP32 copy of the scaled I - dt J.  x: FP32 right-hand
- * side in, FP32 Newton update out. */
-template <int N, int BLOCK>
-__device__ __forceinline__ void gauss_elim_f32(SlotsF<BLOCK> J, float (&x)[N])
-{
-#pragma unroll
-    for (int k = 0; k < N - 1; k++) {
-        int p = k;
-        float best = fabsf(J[k * N + k]);
-#pragma unroll
-        for (int i = k + 1; i < N; i++) {
-            const float a = fabsf(J[k * N + i]);
-            if (a > best) {
-                best = a;
-                p = i;
-            }
-        }
-        if (p != k) {
-            for (int j = k; j < N; j++) {
-                const float t = J[j * N + k];
-                J[j * N + k] = J[j * N + p];
-                J[j * N + p] = t;
-            }
-#pragma unroll
-            for (int i = k + 1; i < N; i++) {
-                if (i == p) {
-                    const float t = x[k];
-                    x[k] = x[i];
-                    x[i] = t;
-                }
-            }
-        }
-        const float rp = 1.0f / J[k * N + k];
-        float m[N], row[N];
-#pragma unroll
-        for (int i = k + 1; i < N; i++) {
-            m[i] = J[k * N + i] * rp;
-            J[k * N + i] = m[i];
-        }
-#pragma unroll
-        for (int j = k + 1; j < N; j++) row[j] = J[j * N + k];
-#pragma unroll
-        for (int i = k + 1; i < N; i++) {
-#pragma unroll
-            for (int j = k + 1; j < N; j++) J[j * N + i] = fmaf(-m[i], row[j], J[j * N + i]);
-            x[i] = fmaf(-m[i], x[k], x[i]);
-        }
-    }
-#pragma unroll
-    for (int i = N - 1; i >= 0; i--) {
-        float xi = x[i];
-#pragma unroll
-        for (int j = i + 1; j < N; j++) xi = fmaf(-J[j * N + i], x[j], xi);
-        x[i] = xi / J[i * N + i];
-    }
-}
-
-/* Scaled Jacobian store for the mixed path: the FP64 value of the reference's
- * transformation, rounded to FP32. */
-template <int N, int BLOCK>
-struct JacPutF {
-    SlotsF<BLOCK> J;
-    Slots<BLOCK> INV, SC;
-    double mdt;
-    __device__ __forceinline__ void operator()(int q, int v, double jv) const
-    {
-        double a = jv * INV[q];
-        a = a * SC[v];
-        a = mdt * a;
-        if (q == v) a = a + 1.0;
-        J[v * N + q] = (float)a;
-    }
-    __device__ __forceinline__ void zero(int q, int v) const { J[v * N + q] = (q == v) ? 1.0f : 0.0f; }
-};
-
 /* Stores one Jacobian entry already transformed as BE_Resid_Jac does:
  * row scale 1/scale_eq, column scale scale_var, then -dt*J, +1 on the
  * diagonal (BE_chem_solve.C:301-318).  zero() stores a structural zero:
@@ -386,10 +298,11 @@ __device__ __forceinline__ void to_number_density(double (&y)[Net::N], double (&
 }
 
 /* MIXED = false: the reference's FP64 arithmetic throughout (bit-faithful).
- * MIXED = true: the scaled I - dt J is rounded to FP32 and factored in FP32;
- * temperature, rates, RHS, residual, the Newton update and its convergence
- * test stay FP64, so each Newton sweep refines the FP32 solve against the FP64
- * residual. */
+ * MIXED = true: the Newton system is solved by MixedSolve (equilibrated FP32
+ * LU + FP64 iterative refinement, dg_mixed.cuh), falling back to the FP64
+ * elimination for a cell whose matrix holds inf/NaN or whose scales are not
+ * all positive and finite; temperature, rates, RHS, Jacobian, residual and
+ * the Newton update and its convergence test stay FP64. */
 template <class Net, int BLOCK, bool MIXED>
 __global__ void __launch_bounds__(BLOCK)
 evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
@@ -400,7 +313,7 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
     const int tid = threadIdx.x;
     double *base = dg_smem + tid;
     const Slots<BLOCK> J{base + L::OFF_J * BLOCK};
-    const SlotsF<BLOCK> JF{(float *)(dg_smem + L::OFF_J * BLOCK) + tid};
+    const SlotsF<BLOCK> JF{(float *)(dg_smem + L::OFF_JF * BLOCK) + tid};
     const Slots<BLOCK> R{base + L::OFF_R * BLOCK};
     const Slots<BLOCK> PREV{base + L::OFF_PREV * BLOCK};
     const Slots<BLOCK> SC{base + L::OFF_SC * BLOCK};
@@ -516,26 +429,24 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
                 /* BE_Resid_Jac (BE_chem_solve.C:280-321) */
 #pragma unroll
                 for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
-                if (MIXED) {
-                    JacPutF<N, BLOCK> put{JF, INV, SC, -dt};
-                    ok = Net::jac(y, R, Tge, T, ts.z, put);
-                } else {
-                    JacPut<N, BLOCK> put{J, INV, SC, -dt, dense || !(dt > 0.0)};
+                const bool dense_j = dense || !(dt > 0.0);
+                {
+                    JacPut<N, BLOCK> put{J, INV, SC, -dt, dense_j};
                     ok = Net::jac(y, R, Tge, T, ts.z, put);
                 }
                 if (ok) {
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
-                    if (MIXED) {
-                        float xs[N];
+                    bool solved = false;
+                    if (MIXED && !dense_j) {
+                        double xs[N];
+                        solved = MixedSolve<Net, BLOCK>{J, JF}(f, xs);
+                        if (solved) {
 #pragma unroll
-                        for (int i = 0; i < N; i++) xs[i] = (float)f[i];
-                        gauss_elim_f32<N, BLOCK>(JF, xs);
-#pragma unroll
-                        for (int i = 0; i < N; i++) f[i] = (double)xs[i];
-                    } else {
-                        gauss_elim_fast<N, BLOCK>(J, f);
+                            for (int i = 0; i < N; i++) f[i] = xs[i];
+                        }
                     }
+                    if (!solved) gauss_elim_fast<N, BLOCK>(J, f);
                     /* Newton update and max-norm test (BE_chem_solve.C:173-206) */
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = u[i] - 1.0 * f[i];

@@ -33,9 +33,14 @@ template <class Net, int NP, bool MIXED>
 struct SplitLayout {
     static constexpr int N = Net::N;
     static constexpr int NT = Net::NT;
-    static constexpr int J = 0;                                   /* matrix */
-    static constexpr int R = J + (MIXED ? (N * N + 1) / 2 : N * N);  /* rates */
-    static constexpr int Y = R + NT;      /* unscaled state seen by RHS/Jacobian */
+    static constexpr int J = 0;           /* FP64 matrix */
+    /* The rates are dead once the Jacobian is built, so the mixed path's
+     * FP32 factors and refined solution share their region. */
+    static constexpr int R = J + N * N;   /* rates */
+    static constexpr int JF = R;          /* mixed: FP32 factors */
+    static constexpr int X = JF + (N * N + 1) / 2;   /* mixed: refined solution */
+    static constexpr int RSZ = MIXED ? (NT > X + N - R ? NT : X + N - R) : NT;
+    static constexpr int Y = R + RSZ;     /* unscaled state seen by RHS/Jacobian */
     static constexpr int G = Y + N;       /* RHS, residual, Newton update */
     static constexpr int U = G + N;
     static constexpr int U0 = U + N;
@@ -46,18 +51,21 @@ struct SplitLayout {
     static constexpr int PREV = RT + N;
     static constexpr int SCAL = PREV + N;  /* T, Tge, Tdef, -dt, piv, 1/piv */
     static constexpr int SLOTS = SCAL + 6;
-    static constexpr size_t bytes()
-    {
-        /* doubles + per-cell ints: bin, flags[4] */
-        return sizeof(double) * SLOTS * 32 + sizeof(int) * 8 * 32 + 64;
-    }
+    static constexpr int NFLAGS = 10;
+    /* per-cell ints after the doubles: NFLAGS flags, then (mixed) the row
+     * and column scale exponents and the FP32 pivots, N each */
+    static constexpr int NINTS = NFLAGS + (MIXED ? 3 * N : 0);
+    static constexpr size_t bytes() { return sizeof(double) * SLOTS * 32 + sizeof(int) * NINTS * 32 + 64; }
 };
 
-/* per-cell int flags */
-enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6 };
+/* per-cell int flags; F_MIX: 0 FP64 elimination, 1 refining, 2 refined */
+enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6,
+             F_MIX = 7, F_EPREV = 8 };
 
+/* The mixed variant is held to the register budget of three 4-warp CTAs per
+ * SM, the occupancy its shared memory allows for the 10-species network. */
 template <class Net, int NP, bool MIXED>
-__global__ void __launch_bounds__(32 * NP)
+__global__ void __launch_bounds__(32 * NP, MIXED ? 3 : 1)
 evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 {
     using L = SplitLayout<Net, NP, MIXED>;
@@ -69,9 +77,12 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         G{cellbase + L::G * 32}, U{cellbase + L::U * 32}, U0{cellbase + L::U0 * 32},
         SC{cellbase + L::SC * 32}, INV{cellbase + L::INV * 32}, AT{cellbase + L::AT * 32},
         RT{cellbase + L::RT * 32}, PREV{cellbase + L::PREV * 32}, S{cellbase + L::SCAL * 32};
-    const SlotsF<32> JF{(float *)(dg_smem + L::J * 32) + l};
+    const SlotsF<32> JF{(float *)(dg_smem + L::JF * 32) + l};
     int *iflags = (int *)(dg_smem + L::SLOTS * 32);
     auto F = [&](int f) -> int & { return iflags[f * 32 + l]; };
+    /* mixed: s (row exponents), t (column exponents), FP32 pivots */
+    auto MI = [&](int k) -> int & { return iflags[(L::NFLAGS + k) * 32 + l]; };
+    const Slots<32> X{cellbase + L::X * 32};
     __shared__ int s_any;
 
     /* warp-0 control state of this lane's cell */
@@ -236,22 +247,12 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             double y[N];
             for (int i = 0; i < N; i++) y[i] = Y[i];
             bool ok = true;
-            if (MIXED) {
-                const JacPutF<N, 32> put{JF, INV, SC, S[3]};
-                switch (w) {
-                case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
-                case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                }
-            } else {
-                const JacPut<N, 32> put{J, INV, SC, S[3], F(F_DENSE) != 0};
-                switch (w) {
-                case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
-                case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
-                }
+            const JacPut<N, 32> put{J, INV, SC, S[3], F(F_DENSE) != 0};
+            switch (w) {
+            case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
+            case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
+            case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
+            default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
             }
             if (!ok) atomicAnd(&F(F_OKJ), 0);
         }
@@ -260,15 +261,70 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         if (w == 0 && do_lu) {
             for (int i = 0; i < N; i++) U[i] = Y[i] * INV[i];
         }
-        /* ---- P5: LU.  FP64: pivot (warp 0) then row updates (all warps);
-         *      mixed: the whole FP32 factorisation on warp 0 ---- */
+        /* ---- P5: LU.  FP64: pivot (warp 0) then row updates (all warps).
+         *      Mixed: equilibrated FP32 factorisation and first solve on
+         *      warp 0; each refinement's FP64 residual rows i = w mod NP on
+         *      all warps, the FP32 correction on warp 0; the single-lane FP64
+         *      elimination for a dense or non-finite system ---- */
         if (MIXED) {
+            const MixedSolve<Net, 32> ms{J, JF};
             if (w == 0 && do_lu) {
-                float xs[N];
-                for (int i = 0; i < N; i++) xs[i] = (float)G[i];
-                gauss_elim_f32<N, 32>(JF, xs);
-                for (int i = 0; i < N; i++) G[i] = (double)xs[i];
+                double g[N], x[N];
+                int sx[N], tx[N], px[N];
+                for (int i = 0; i < N; i++) g[i] = G[i];
+                if (!F(F_DENSE) && ms.prepare(g, sx, tx, px, x)) {
+                    for (int i = 0; i < N; i++) {
+                        MI(i) = sx[i];
+                        MI(N + i) = tx[i];
+                        MI(2 * N + i) = px[i];
+                        X[i] = x[i];
+                    }
+                    F(F_MIX) = 1;
+                    F(F_EPREV) = 0x7ff;
+                } else {
+                    gauss_elim_fast<N, 32>(J, g);
+                    for (int i = 0; i < N; i++) G[i] = g[i];
+                    F(F_MIX) = 0;
+                }
             }
+            __syncthreads();
+            for (int it = 0; it < MixedSolve<Net, 32>::MAX_REFINE; it++) {
+                const bool refining = do_lu && F(F_MIX) == 1;
+                if (!__syncthreads_or(refining)) break;
+                if (refining) {
+#pragma unroll
+                    for (int i = 0; i < N; i++)
+                        if (i % NP == w) Y[i] = ms.residual_row(i, G[i], X);
+                }
+                __syncthreads();
+                if (w == 0 && refining) {
+                    double r[N], x[N];
+                    int sx[N], tx[N], px[N];
+                    for (int i = 0; i < N; i++) {
+                        r[i] = Y[i];
+                        x[i] = X[i];
+                        sx[i] = MI(i);
+                        tx[i] = MI(N + i);
+                        px[i] = MI(2 * N + i);
+                    }
+                    int eprev = F(F_EPREV);
+                    bool more;
+                    if (ms.refine(px, sx, tx, r, x, eprev, more)) {
+                        for (int i = 0; i < N; i++) X[i] = x[i];
+                        F(F_EPREV) = eprev;
+                        F(F_MIX) = more ? 1 : 2;
+                    } else {
+                        double g[N];
+                        for (int i = 0; i < N; i++) g[i] = G[i];
+                        gauss_elim_fast<N, 32>(J, g);
+                        for (int i = 0; i < N; i++) G[i] = g[i];
+                        F(F_MIX) = 0;
+                    }
+                }
+                __syncthreads();
+            }
+            if (w == 0 && do_lu && F(F_MIX) != 0)
+                for (int i = 0; i < N; i++) G[i] = X[i];
         } else {
             for (int k = 0; k < N - 1; k++) {
                 __syncthreads();

@@ -185,7 +185,7 @@ __device__ __forceinline__ int cost_bucket(int c)
     return __clz(v);   /* 31 - floor(log2 v): big costs get small buckets */
 }
 
-__global__ void order_count_kernel(const int *cost, long long n, int *counts)
+static __global__ void order_count_kernel(const int *cost, long long n, int *counts)
 {
     __shared__ int sc[32];
     if (threadIdx.x < 32) sc[threadIdx.x] = 0;
@@ -197,7 +197,7 @@ __global__ void order_count_kernel(const int *cost, long long n, int *counts)
     if (threadIdx.x < 32 && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
 }
 
-__global__ void order_scan_kernel(const int *counts, int *offsets)
+static __global__ void order_scan_kernel(const int *counts, int *offsets)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int run = 0;
@@ -207,7 +207,7 @@ __global__ void order_scan_kernel(const int *counts, int *offsets)
     }
 }
 
-__global__ void order_scatter_kernel(const int *cost, long long n, int *offsets, int *order)
+static __global__ void order_scatter_kernel(const int *cost, long long n, int *offsets, int *order)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
@@ -257,32 +257,30 @@ __device__ void gauss_elim_local(double *A, double *x)
     }
 }
 
-/* BE_chem_solve (BE_chem_solve.C:79-241) over one strip in lockstep: one
- * block, one thread per cell.  All cells share the sweep loop; a negative
- * value anywhere fails the strip at the RHS or Jacobian stage, a NaN stops
- * the sweep at the first such cell in cell order (later cells keep their
+/* BE_chem_solve (BE_chem_solve.C:79-241) over one strip in lockstep, on the
+ * per-thread state of a block with one thread per cell (act: the thread has
+ * a cell; c: its index).  All cells share the sweep loop; a negative value
+ * anywhere fails the strip at the RHS or Jacobian stage, a NaN stops the
+ * sweep at the first such cell in cell order (later cells keep their
  * pre-update values), and the strip converges only when every cell passed
- * the max-norm test.  Writes u and atol back as the reference does and the
- * last temperature of each cell to Ts. */
+ * the max-norm test.  u and at are updated as the reference writes them back
+ * (unscaled); T receives the cell's last temperature.  Returns the
+ * reference's return value, the same in every thread.  first_bad: one int
+ * of shared memory.  Every thread of the block must call it. */
 template <class Net>
-__global__ void __launch_bounds__(DENGO_MAX_NCELLS)
-be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstrip,
-                const double *scaling, TableSet ts, int max_sweeps, int *ret, double *Ts)
+__device__ int be_strip_solve(bool act, int c, int nstrip, double (&u)[Net::N], double (&at)[Net::N],
+                              const double (&rt)[Net::N], const double (&sc)[Net::N], double dt,
+                              const TableSet &ts, int max_sweeps, double &T, int *first_bad)
 {
     constexpr int N = Net::N;
-    const int c = threadIdx.x;
-    const bool act = c < nstrip;
-    __shared__ int first_bad;
-    double us[N], u0[N], sc[N], inv[N], at[N], rt[N], y[N], g[N], upre[N];
+    double us[N], u0[N], inv[N], y[N], g[N], upre[N];
     double R[Net::NT];
     double A[N * N];
     if (act) {
         for (int i = 0; i < N; i++) {
-            sc[i] = scaling[c * N + i];
             inv[i] = 1.0 / sc[i];
-            us[i] = u[c * N + i] * inv[i];
-            at[i] = atol[c * N + i] * inv[i];
-            rt[i] = rtol[c * N + i];
+            us[i] = u[i] * inv[i];
+            at[i] = at[i] * inv[i];
             u0[i] = us[i];
         }
     }
@@ -290,11 +288,10 @@ be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstr
     int fail_mode = 0; /* 0 none, 1 u = y*sc (RHS/Jacobian failure) */
     for (int isweep = 0; isweep < max_sweeps; isweep++) {
         bool ok = true;
-        double T = 0, Tge = 0;
+        double Tge = 0;
         if (act) {
             for (int i = 0; i < N; i++) y[i] = us[i] * sc[i];
             Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
-            Ts[c] = T;
             interpolate_local<Net>(ts, dg_log(T), R);
             ok = Net::rhs(y, R, T, ts.z, g);
         }
@@ -331,12 +328,14 @@ be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstr
                 }
             }
         }
-        if (c == 0) first_bad = nstrip;
+        if (c == 0) *first_bad = nstrip;
         __syncthreads();
-        if (act && nan) atomicMin(&first_bad, c);
+        if (act && nan) atomicMin(first_bad, c);
         __syncthreads();
-        if (first_bad < nstrip) {
-            if (act && c > first_bad)
+        const int fb = *first_bad;
+        __syncthreads();
+        if (fb < nstrip) {
+            if (act && c > fb)
                 for (int i = 0; i < N; i++) us[i] = upre[i];
             rv = 1;
             break;
@@ -347,11 +346,141 @@ be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstr
     }
     if (act) {
         for (int i = 0; i < N; i++) {
-            u[c * N + i] = fail_mode ? y[i] * sc[i] : us[i] * sc[i];
-            atol[c * N + i] = at[i] * sc[i];
+            u[i] = fail_mode ? y[i] * sc[i] : us[i] * sc[i];
+            at[i] = at[i] * sc[i];
         }
     }
-    if (c == 0) *ret = fail_mode ? 1 : rv;
+    return fail_mode ? 1 : rv;
+}
+
+/* BE_chem_solve as a kernel: one block, one thread per cell; u, atol
+ * (number densities, AoS) updated in place, the return value in *ret and
+ * each cell's last temperature in Ts. */
+template <class Net>
+__global__ void __launch_bounds__(DENGO_MAX_NCELLS)
+be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstrip,
+                const double *scaling, TableSet ts, int max_sweeps, int *ret, double *Ts)
+{
+    constexpr int N = Net::N;
+    const int c = threadIdx.x;
+    const bool act = c < nstrip;
+    __shared__ int first_bad;
+    double us[N], sc[N], at[N], rt[N];
+    if (act) {
+        for (int i = 0; i < N; i++) {
+            sc[i] = scaling[c * N + i];
+            us[i] = u[c * N + i];
+            at[i] = atol[c * N + i];
+            rt[i] = rtol[c * N + i];
+        }
+    }
+    double T = 0;
+    const int rv = be_strip_solve<Net>(act, c, nstrip, us, at, rt, sc, dt, ts, max_sweeps, T,
+                                       &first_bad);
+    if (act) {
+        for (int i = 0; i < N; i++) {
+            u[c * N + i] = us[i];
+            atol[c * N + i] = at[i];
+        }
+        Ts[c] = T;
+    }
+    if (c == 0) *ret = rv;
+}
+
+/* Outputs of run_strip_kernel; the trajectory arrays may be null. */
+struct RunOut {
+    double *ttot, *dt;   /* [1] */
+    int *iters;          /* [1]: iterations taken (the reference's iter + 1) */
+    double *traj;        /* [niter][nstrip][N] state after each BE_chem_solve */
+    double *traj_T;      /* [niter][nstrip] last temperature of each solve */
+    unsigned char *traj_ok; /* [niter] 1 when the solve converged */
+    double *traj_t, *traj_dt; /* [niter] ttot and dt at each solve */
+};
+
+/* The Cython driver run_<n> (rates_and_rate_tables_run.pyx.template:114-205)
+ * on one strip in lockstep, after its mass-to-number conversion: prev and
+ * scale start as the input, the electrons are made consistent (the
+ * reference's running total over the strip), dt = tf/1e5; then up to niter
+ * BE_chem_solve calls: on success prev = scale = u, ttot += dt, dt *= 1.1,
+ * dt clipped to tf - ttot, stop when ttot >= tf; on failure dt /= 2,
+ * u = scale = prev, stop when dt < 1e-30 tf. */
+template <class Net>
+__global__ void __launch_bounds__(DENGO_MAX_NCELLS)
+run_strip_kernel(double *input, const double *rtol, double *atol, int nstrip, double tf, int niter,
+                 TableSet ts, int max_sweeps, RunOut out)
+{
+    constexpr int N = Net::N;
+    const int c = threadIdx.x;
+    const bool act = c < nstrip;
+    __shared__ int first_bad;
+    double u[N], prev[N], sc[N], at[N], rt[N];
+    if (act) {
+        for (int i = 0; i < N; i++) {
+            prev[i] = input[c * N + i];
+            sc[i] = prev[i];
+            at[i] = atol[c * N + i];
+            rt[i] = rtol[c * N + i];
+        }
+    }
+    __syncthreads();
+    if (c == 0) {
+        /* ensure_electron_consistency over the strip, in cell order */
+        double total = 0.0;
+        for (int k = 0; k < nstrip; k++) {
+            double y[N];
+            for (int i = 0; i < N; i++) y[i] = input[k * N + i];
+            total = Net::electron_sum(y, total);
+            if (Net::IDE >= 0) input[k * N + Net::IDE] = total;
+        }
+    }
+    __syncthreads();
+    if (act)
+        for (int i = 0; i < N; i++) u[i] = input[c * N + i];
+    double dt = tf / 1e5, ttot = 0.0;
+    int iter = 0;
+    for (; iter < niter; iter++) {
+        double T = 0;
+        const int status = be_strip_solve<Net>(act, c, nstrip, u, at, rt, sc, dt, ts, max_sweeps,
+                                               T, &first_bad);
+        if (out.traj && act)
+            for (int i = 0; i < N; i++) out.traj[((size_t)iter * nstrip + c) * N + i] = u[i];
+        if (out.traj_T && act) out.traj_T[(size_t)iter * nstrip + c] = T;
+        if (c == 0) {
+            if (out.traj_ok) out.traj_ok[iter] = status == 0;
+            if (out.traj_t) out.traj_t[iter] = ttot;
+            if (out.traj_dt) out.traj_dt[iter] = dt;
+        }
+        if (status == 0) {
+            if (act)
+                for (int i = 0; i < N; i++) {
+                    prev[i] = u[i];
+                    sc[i] = u[i];
+                }
+            ttot += dt;
+            dt *= 1.1;
+            if (tf - ttot < dt) dt = tf - ttot;
+        } else {
+            dt /= 2.0;
+            if (act)
+                for (int i = 0; i < N; i++) {
+                    u[i] = prev[i];
+                    sc[i] = u[i];
+                }
+            if (dt < 1e-30 * tf) break;
+            continue;
+        }
+        if (ttot >= tf) break;
+    }
+    if (act)
+        for (int i = 0; i < N; i++) {
+            input[c * N + i] = u[i];
+            atol[c * N + i] = at[i];
+        }
+    if (c == 0) {
+        *out.ttot = ttot;
+        *out.dt = dt;
+        *out.iters = iter < niter ? iter + 1 : niter;
+    }
 }
 
 }  // namespace dg

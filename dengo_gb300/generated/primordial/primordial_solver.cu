@@ -38,6 +38,13 @@ struct Net {
         return false;
     }
 
+    /* structural nonzeros of I - dt J: entry (eq q, var v) can be nonzero */
+    __host__ __device__ static constexpr unsigned long long jnz_col(int v)
+    {
+        return v == 0 ? 0x20full : v == 1 ? 0x11full : v == 2 ? 0x31full : v == 3 ? 0x31full : v == 4 ? 0x11full : v == 5 ? 0x360ull : v == 6 ? 0x3e0ull : v == 7 ? 0x3c0ull : v == 8 ? 0x3ffull : v == 9 ? 0x0ull : 0ull;
+    }
+    __host__ __device__ static constexpr bool jnz(int q, int v) { return q == v || ((jnz_col(v) >> q) & 1ull) != 0; }
+
     static const char *species_name(int i)
     {
         static const char *names[N] = { "H2_1", "H2_2", "H_1", "H_2", "H_m0", "He_1", "He_2", "He_3", "de", "ge", };
@@ -895,6 +902,54 @@ using Api = dg::Api<Net>;
 
 }  // namespace dgnet_primordial
 
+/* Engine variants.  Compiled alone this file instantiates every kernel; the
+ * package build compiles variant k in a unit of its own (-DDG_KERNEL_PART=k)
+ * and the entry points with -DDG_SPLIT_KERNELS, in parallel. */
+#if defined(DG_KERNEL_PART)
+#if DG_KERNEL_PART == 0
+template int dg::launch_lane<dgnet_primordial::Net, 32, false>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 1
+template int dg::launch_lane<dgnet_primordial::Net, 32, true>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 2
+template int dg::launch_lane<dgnet_primordial::Net, 64, false>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 3
+template int dg::launch_lane<dgnet_primordial::Net, 64, true>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 4
+template int dg::launch_lane<dgnet_primordial::Net, 128, false>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 5
+template int dg::launch_lane<dgnet_primordial::Net, 128, true>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 6
+template int dg::launch_split<dgnet_primordial::Net, 2, false>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 7
+template int dg::launch_split<dgnet_primordial::Net, 2, true>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 8
+template int dg::launch_split<dgnet_primordial::Net, 4, false>(DG_LAUNCH_ARGS);
+#endif
+#if DG_KERNEL_PART == 9
+template int dg::launch_split<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
+#else
+#if defined(DG_SPLIT_KERNELS)
+extern template int dg::launch_lane<dgnet_primordial::Net, 32, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_lane<dgnet_primordial::Net, 32, true>(DG_LAUNCH_ARGS);
+extern template int dg::launch_lane<dgnet_primordial::Net, 64, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_lane<dgnet_primordial::Net, 64, true>(DG_LAUNCH_ARGS);
+extern template int dg::launch_lane<dgnet_primordial::Net, 128, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_lane<dgnet_primordial::Net, 128, true>(DG_LAUNCH_ARGS);
+extern template int dg::launch_split<dgnet_primordial::Net, 2, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_split<dgnet_primordial::Net, 2, true>(DG_LAUNCH_ARGS);
+extern template int dg::launch_split<dgnet_primordial::Net, 4, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_split<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
+
 extern "C" {
 
 primordial_data *primordial_setup_data(int *NumberOfFields, char ***FieldNames)
@@ -931,6 +986,14 @@ int primordial_solve_cells_host(primordial_data *data, const dengo_cell_batch *b
                              const dengo_solver_config *cfg)
 {
     return dgnet_primordial::Api::solve_host(data, batch, z, cfg);
+}
+
+int primordial_run_strip(primordial_data *data, double tf, int niter, double z, double *input, double *rtol,
+                      double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,
+                      unsigned char *traj_ok, double *traj_t, double *traj_dt)
+{
+    return dgnet_primordial::Api::run_strip(data, tf, niter, z, input, rtol, atol, nstrip, ttot, dt,
+                                         traj, traj_T, traj_ok, traj_t, traj_dt);
 }
 
 int calculate_rhs_primordial(double *input, double *rhs, int nstrip, int nchem, void *sdata)
@@ -1062,8 +1125,17 @@ long long primordial_data_field_offset(const char *field)
 
 const char *primordial_species_name(int i) { return dgnet_primordial::Net::species_name(i); }
 
+/* the species' weight as the reference's templates print it (the Cython
+ * driver divides its initial conditions by it) */
+double primordial_species_weight(int i)
+{
+    static const double w[] = { 2.0, 2.0, 1.00794, 1.00794, 1.00794, 4.002602, 4.002602, 4.002602, 1.0, 1.0, };
+    return (i >= 0 && i < 10) ? w[i] : 0.0;
+}
+
 const char *primordial_last_error(void) { return dg::last_error_buf(); }
 
 void dengo_default_config(dengo_solver_config *cfg) { dg_default_config_impl(cfg); }
 
 }  /* extern "C" */
+#endif  /* DG_KERNEL_PART */

@@ -37,7 +37,7 @@ def primordial_network(T_bounds=(1.0, 1e9), n_bins=1024, with_compton=False):
     return net
 
 
-SHIPPED_NETWORKS = ("primordial",)
+SHIPPED_NETWORKS = ("primordial", "oxygen")
 
 
 def build_network(name):

@@ -85,6 +85,9 @@ def _declare(lib, n):
         "%s_table_length" % n: (C.c_int, [C.c_int]),
         "%s_data_field_offset" % n: (C.c_longlong, [C.c_char_p]),
         "%s_species_name" % n: (C.c_char_p, [C.c_int]),
+        "%s_species_weight" % n: (C.c_double, [C.c_int]),
+        "%s_run_strip" % n: (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_double, P_D, P_D,
+                                       P_D, C.c_int, P_D, P_D, P_D, P_D, C.c_void_p, P_D, P_D]),
         "%s_last_error" % n: (C.c_char_p, []),
         "dengo_default_config": (None, [C.POINTER(SolverConfig)]),
     }
@@ -211,6 +214,50 @@ class Solver:
         if rc != 0:
             raise RuntimeError("solve_cells_host failed (%d): %s" % (rc, self.last_error()))
         return out
+
+    # ---- the reference's Cython driver ---------------------------------
+    def run(self, ics, tf, niter=10000, intermediate=1, z=-1.0):
+        """``run_<name>(ics, tf, niter, intermediate, z)`` of the reference's
+        Cython module (rates_and_rate_tables_run.pyx.template:81-205) on one
+        strip of at most 1024 cells, solved on the GPU by ``<name>_run_strip``.
+
+        ``ics`` maps species names to 1-d arrays; each is divided by the
+        species' weight, rtol = 1e-6 and atol = 1e-6 x input, as there.
+        Returns ``(rv, rv_t)``: final values times the weights, and (when
+        ``intermediate``) the per-iteration species, ``T``, ``successful``,
+        ``t`` and ``dt``, zeros after the last iteration taken."""
+        n = self.name
+        w = [getattr(self.lib, "%s_species_weight" % n)(i) for i in range(self.N)]
+        dims = len(ics[self.species[-1]])
+        inp = np.empty((dims, self.N))
+        for j, s in enumerate(self.species):
+            inp[:, j] = np.asarray(ics[s], np.float64) / w[j]
+        atol = inp * 1e-06
+        rtol = np.full_like(inp, 1e-06)
+        ttot, dt = C.c_double(), C.c_double()
+        traj = np.zeros((niter, dims, self.N)) if intermediate else None
+        traj_T = np.zeros((niter, dims)) if intermediate else None
+        ok = np.zeros(niter, np.uint8) if intermediate else None
+        t_int = np.zeros(niter) if intermediate else None
+        dt_int = np.zeros(niter) if intermediate else None
+        addr = lambda a: None if a is None else a.ctypes.data_as(P_D)
+        iters = getattr(self.lib, "%s_run_strip" % n)(
+            self.data, float(tf), int(niter), float(z), _dptr(inp), _dptr(rtol), _dptr(atol),
+            dims, C.byref(ttot), C.byref(dt), addr(traj), addr(traj_T),
+            None if ok is None else ok.ctypes.data, addr(t_int), addr(dt_int))
+        if iters < 0:
+            raise RuntimeError(self.last_error())
+        self.last_run = dict(iterations=iters, ttot=ttot.value, dt=dt.value, atol=atol)
+        rv = {s: inp[:, j] * w[j] for j, s in enumerate(self.species)}
+        rv_t = {}
+        if intermediate:
+            for j, s in enumerate(self.species):
+                rv_t[s] = traj[:, :, j].T.copy()[:niter]
+            rv_t["successful"] = ok.astype("bool")
+            rv_t["T"] = traj_T.T.copy()
+            rv_t["t"] = t_int
+            rv_t["dt"] = dt_int
+        return rv, rv_t
 
     # ---- strip entry points ---------------------------------------------
     def calculate_rhs(self, state):

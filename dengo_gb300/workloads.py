@@ -41,6 +41,9 @@ PRIMORDIAL_CONFIGS = {
     # neutral gas only (T <= 1e4 K): every cell converges in a few hundred
     # sweeps; used to measure the solver's throughput without the stiff tail
     "cold": dict(nH=(1.0, 1e6), T=(10.0, 1e4), unstable=0.0, seed=20244),
+    # ionised gas only (T >= 3e5 K): the stiff cells that run to the substep
+    # cap; used to profile the per-cell critical path
+    "hot": dict(nH=(1.0, 1e6), T=(3e5, 1e8), unstable=0.0, seed=20245),
 }
 
 
@@ -82,3 +85,40 @@ def primordial_cells(ncells, config="config1", seed=None, dt_factor=0.1):
     rho = state[:, :-1].sum(axis=1)
     tff = np.sqrt(3.0 * np.pi / (32.0 * G_NEWTON * rho))
     return state, dt_factor * tff
+
+
+# Oxygen ion-by-ion cells: H, He, O ions, electrons, energy (16 equations).
+OXYGEN_ORDER = ("H_1", "H_2", "He_1", "He_2", "He_3", "O_1", "O_2", "O_3", "O_4", "O_5",
+                "O_6", "O_7", "O_8", "O_9", "de", "ge")
+OXYGEN_WEIGHTS = dict(H=1.00794, He=4.002602, O=15.9994)
+
+
+def oxygen_cells(ncells, seed=20246, dt_range=(1e10, 1e12)):
+    """Return ``(state, dtf)`` for the oxygen network (config 4).
+
+    nH ~ logU(1e-4, 1e2) cm^-3, T ~ logU(1e4, 1e9) K, n_He = Y/(4(1-Y)) nH with
+    Y = 0.24, n_O = 4.9e-4 nH; the ionisation state of each element is a
+    seeded Dirichlet(1) draw over its stages; electrons from charge
+    neutrality; ge from T with gamma = 5/3; dtf ~ logU(dt_range) s."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nH = _logu(rng, 1e-4, 1e2, ncells)
+    T = _logu(rng, 1e4, 1e9, ncells)
+    n = {}
+    for atom, nnuc, stages in (("H", nH, 2), ("He", 0.24 / (4 * 0.76) * nH, 3),
+                               ("O", 4.9e-4 * nH, 9)):
+        frac = rng.dirichlet(np.ones(stages), ncells)
+        frac = np.maximum(frac, 1e-12)
+        frac /= frac.sum(axis=1, keepdims=True)
+        for i in range(stages):
+            n["%s_%d" % (atom, i + 1)] = nnuc * frac[:, i]
+    n["de"] = sum(n["%s_%d" % (a, i + 1)] * i for a, st in (("H", 2), ("He", 3), ("O", 9))
+                  for i in range(st))
+    w = {s: OXYGEN_WEIGHTS[s.split("_")[0]] for s in OXYGEN_ORDER if s not in ("de", "ge")}
+    w["de"] = 1.0
+    density = sum(w[s] * n[s] for s in OXYGEN_ORDER if s not in ("de", "ge"))
+    gsum = sum(n[s] / (GAMMA - 1.0) for s in OXYGEN_ORDER if s != "ge")
+    ge = T * KB * gsum / (density * MH)
+    state = np.empty((ncells, len(OXYGEN_ORDER)))
+    for i, s in enumerate(OXYGEN_ORDER):
+        state[:, i] = ge if s == "ge" else n[s] * w[s] * MH
+    return state, _logu(rng, *dt_range, ncells)

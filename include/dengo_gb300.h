@@ -33,8 +33,13 @@
  *   <n>_solve_cells_host    the same batch with host pointers (copies in and
  *                           out inside the call; per-cell dtf, unlike
  *                           dengo_evolve_<n> whose dtf is one scalar)
+ *   <n>_run_strip           the reference's Cython driver run_<n>
+ *                           (rates_and_rate_tables_run.pyx.template:114-205)
+ *                           on one strip in lockstep: BE_chem_solve with its
+ *                           own dt control, scale refresh, niter cap and
+ *                           dt < 1e-30 tf stop, optional trajectories
  *   <n>_ntables, <n>_table_name, <n>_table_length, <n>_data_field_offset,
- *   <n>_nspecies, <n>_species_name, <n>_last_error
+ *   <n>_nspecies, <n>_species_name, <n>_species_weight, <n>_last_error
  *                           introspection for bindings
  *
  * All computation runs on the GPU; there is no CPU fallback.  Functions that
@@ -62,7 +67,7 @@ enum dengo_cell_status {
 /* Arithmetic of the Newton step. */
 enum dengo_precision {
     DENGO_FP64 = 0,            /* the reference's FP64 arithmetic, bit-faithful */
-    DENGO_MIXED = 1            /* FP32 Jacobian + LU, FP64 residual and refinement */
+    DENGO_MIXED = 1            /* equilibrated FP32 LU + FP64 iterative refinement of each Newton step */
 };
 
 /* How cells are assigned to lanes. */
@@ -164,12 +169,18 @@ typedef int (*jac_f)(double *, double *, int, int, void *);
                                void *stream);                                  \
     int n##_solve_cells_host(n##_data *data, const dengo_cell_batch *batch,    \
                              double z, const dengo_solver_config *cfg);        \
+    int n##_run_strip(n##_data *data, double tf, int niter, double z,          \
+                      double *input, double *rtol, double *atol, int nstrip,   \
+                      double *ttot, double *dt, double *traj, double *traj_T,  \
+                      unsigned char *traj_ok, double *traj_t,                  \
+                      double *traj_dt);                                        \
     int n##_ntables(void);                                                     \
     const char *n##_table_name(int k);                                         \
     int n##_table_length(int k);                                               \
     long long n##_data_field_offset(const char *field);                        \
     int n##_nspecies(void);                                                    \
     const char *n##_species_name(int i);                                       \
+    double n##_species_weight(int i);                                          \
     const char *n##_last_error(void);
 
 /* The unprefixed reference names, exported by every network library (one

@@ -325,3 +325,16 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
     *dt_out = dt;
     return iter < niter ? iter + 1 : niter;
 }
+
+/* dgo_run_strip on a data object built from `tables` (freed on return). */
+int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, double tf,
+                         int niter, double z, double *input, double *rtol, double *atol,
+                         int dims, const dgo_config *cfg, double *ttot_out, double *dt_out,
+                         dgo_stats *st)
+{
+    void *data = net->alloc_data(tables);
+    int it = dgo_run_strip(net, data, tf, niter, z, input, rtol, atol, dims, cfg, ttot_out,
+                           dt_out, st);
+    net->free_data(data);
+    return it;
+}

@@ -90,6 +90,12 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
                   int dims, const dgo_config *cfg, double *ttot_out,
                   double *dt_out, dgo_stats *st);
 
+/* dgo_run_strip on a data object built from the tables (freed on return). */
+int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, double tf,
+                         int niter, double z, double *input, double *rtol, double *atol,
+                         int dims, const dgo_config *cfg, double *ttot_out, double *dt_out,
+                         dgo_stats *st);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,31 @@ class Oracle:
                     sweeps=sw, failures=fl)
 
 
+class Stats(C.Structure):
+    _fields_ = [("substeps_ok", C.c_longlong), ("substeps_fail", C.c_longlong),
+                ("sweeps", C.c_longlong), ("status", C.c_int)]
+
+
+def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0):
+    """The Cython driver's loop (dgo_run_strip) on one strip of number
+    densities (already divided by the weights).  Returns a dict."""
+    inp = np.ascontiguousarray(input_number, np.float64).copy()
+    rt = np.full_like(inp, 1e-06)
+    at = inp * 1e-06
+    keep, tp = orc._tables(tables_in_order)
+    ttot, dt, st = C.c_double(), C.c_double(), Stats()
+    cfg = orc.config()
+    fn = orc.lib.dgo_run_strip_tables
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.POINTER(P_D), C.c_double, C.c_int, C.c_double, P_D, P_D, P_D,
+                   C.c_int, C.POINTER(Config), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                   C.POINTER(Stats)]
+    it = fn(orc.net_addr, tp, float(tf), int(niter), float(z), _dp(inp), _dp(rt), _dp(at),
+            inp.shape[0], C.byref(cfg), C.byref(ttot), C.byref(dt), C.byref(st))
+    return dict(state=inp, atol=at, ttot=ttot.value, dt=dt.value, iterations=it,
+                substeps_ok=st.substeps_ok, substeps_fail=st.substeps_fail, sweeps=st.sweeps)
+
+
 class Reference:
     """The reference's own generated solver, built by oracle/ref_build.py
     (only where the reference checkout exists)."""
@@ -102,7 +127,7 @@ class Reference:
         path = os.path.join(REF, "libref_%s.so" % name)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
-        os.environ.setdefault("DGO_REF_TABLE_DIR", os.path.join(REF, name))
+        os.environ["DGO_REF_TABLE_DIR"] = os.path.join(REF, name)
         self.lib = C.CDLL(path)
         self.lib.ref_evolve_cells.argtypes = [P_D, P_D, C.c_double, P_D, P_D, P_D, C.c_longlong,
                                               P_D, C.c_int]

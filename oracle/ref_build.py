@@ -117,6 +117,74 @@ def _reference_primordial():
     return net
 
 
+def _reference_oxygen():
+    """The reference's own ion-by-ion setup (dengo/ion_by_ion.py:33-56) for
+    H, O and He.  ChiantiPy is absent: a stand-in module lets
+    ``chianti_rate`` register its reactions (it only checks that ChiantiPy
+    imported), and every rate and cooling table is then replaced by the
+    seeded synthetic curve this package tabulates for the same ion
+    (dengo_gb300/ion_by_ion.py), so both sides consume identical tables.  The
+    reference's Python-2 implicit import of ``reaction_classes``
+    (ion_by_ion.py:24) is satisfied by aliasing the module."""
+    sys.path.insert(0, REF_ROOT)
+    sys.path.insert(0, os.path.dirname(HERE))
+    _install_shims()
+    import sympy
+    import dengo.reaction_classes as rc
+    import dengo.chemical_network as cn
+    sys.modules["reaction_classes"] = rc
+    rc.ch = types.ModuleType("chianti_stand_in")
+    rc.chu = rc.ch
+    _patch_cooling_actions(rc, sympy)
+    from dengo.ion_by_ion import setup_ionization
+    from dengo_gb300 import ion_by_ion as mine
+    net = cn.ChemicalNetwork()
+    net.add_species("de")
+    for atom in ("H", "O", "He"):
+        s, c, r = setup_ionization(atom)
+        num = {"H": 1, "He": 2, "O": 8}[atom]
+        for i in range(num + 1):
+            name = rc.species_registry["%s_%d" % (atom, i + 1)].name
+            if "%s_i" % name in rc.reaction_registry:
+                rc.reaction_registry["%s_i" % name].coeff_fn = mine.ionization_rate(atom, i)
+            if "%s_r" % name in rc.reaction_registry:
+                rc.reaction_registry["%s_r" % name].coeff_fn = mine.recombination_rate(atom, i)
+            act = rc.cooling_registry["%s_c" % name]
+            act.tables["%s_c" % name] = mine.cooling_rate(atom, i)
+        net.add_collection(s, c, r)
+    net.init_temperature((1e0, 1e10), n_bins=8192)
+    return net
+
+
+def _patch_cooling_actions(rc, sympy):
+    def equation(self):
+        if self._eq is not None:
+            return self._eq
+        symbols = {n: s.symbol for n, s in rc.species_registry.items()}
+        ta = {n: sympy.Symbol("%s_%s[i]" % (self.name, n)) for n in self.tables}
+        tp = {n: sympy.Symbol(n) for n in self.temporaries}
+        self.table_symbols.update(ta)
+        self.temp_symbols.update(tp)
+        symbols.update(ta)
+        symbols.update(tp)
+        self._eq = eval(self._equation, symbols)
+        for n, e in self.temporaries.items():
+            scope = {k: s.symbol for k, s in rc.species_registry.items()}
+            scope.update(ta)
+            self._eq = self._eq.subs(n, sympy.sympify(e, locals=scope))
+        return self._eq
+
+    def species(self):
+        self.equation
+        bad = set(list(self.temp_symbols.values()) + list(self.table_symbols.values()))
+        return {rc.species_registry[str(s).replace("[i]", "")]
+                for s in self.equation.atoms(sympy.Symbol) if s not in bad}
+
+    rc.CoolingAction.equation = property(equation)
+    rc.CoolingAction.species = property(species)
+    rc.CoolingAction.__lt__ = lambda a, b: a.name < b.name
+
+
 HARNESS = r"""
 /* ORACLE -- test infrastructure: C entry points over the reference's
  * rendered solver, written by oracle/ref_build.py. */
@@ -179,11 +247,17 @@ void ref_evolve_cells(const double *dtf, double *dt, double z, double *input, do
 
 
 def build(name="primordial"):
-    if name != "primordial":
-        raise ValueError("only the primordial network renders with the reference here")
+    """Render and compile one network in a fresh interpreter (the reference's
+    registries are module globals, so networks are built one per process)."""
+    if name not in ("primordial", "oxygen"):
+        raise ValueError("networks rendered with the reference here: primordial, oxygen")
     if not os.path.isdir(os.path.join(REF_ROOT, "dengo")):
         raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
-    net = _reference_primordial()
+    if "dengo" in sys.modules:
+        lib = os.path.join(OUT, "libref_%s.so" % name)
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
+        return lib
+    net = _reference_primordial() if name == "primordial" else _reference_oxygen()
     odir = os.path.join(OUT, name)
     os.makedirs(odir, exist_ok=True)
     net.write_solver(name, output_dir=odir, ode_solver_source=None)

@@ -155,5 +155,40 @@ def main():
     print("wrote golden vectors to", HERE)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and len(sys.argv) == 1:
     main()
+
+
+def make_oxygen():
+    """Golden vectors of the oxygen ion-by-ion network (16 equations): the
+    reference's own setup_ionization and templates, with the synthetic
+    CHIANTI stand-in tables (oracle/ref_build.py)."""
+    import ref_build
+    from oracle import Reference
+    from dengo_gb300.workloads import oxygen_cells
+    ref_build.build("oxygen")
+    ref = Reference("oxygen")
+    out = {}
+    st, dtf = oxygen_cells(48, seed=515)
+    r = ref.evolve_cells(st, dtf, nthreads=8)
+    out["evolve_in"], out["evolve_dtf"] = st, dtf
+    for k in ("state", "atol", "dt", "ttot"):
+        out["evolve_%s" % k] = r[k]
+    # the solver's table order, and a SHA-256 of each table the reference wrote
+    import hashlib
+    from dengo_gb300.codegen.spec import network_spec
+    from dengo_gb300.ion_by_ion import oxygen_network
+    spec = network_spec(oxygen_network(), "oxygen")
+    tdir = os.path.join(ROOT, "oracle", "_ref", "oxygen", "oxygen_tables.h5.d")
+    files = {f[:-4]: os.path.join(tdir, f) for f in os.listdir(tdir)}
+    out["table_order"] = np.array([t.name for t in spec.tables])
+    sums = []
+    for t in spec.tables:
+        sums.append(hashlib.sha256(np.fromfile(files[t.name]).tobytes()).hexdigest())
+    out["table_sha256"] = np.array(sums)
+    np.savez_compressed(os.path.join(HERE, "oxygen_golden.npz"), **out)
+    print("wrote oxygen golden vectors")
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "oxygen":
+    make_oxygen()
