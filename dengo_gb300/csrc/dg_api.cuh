@@ -486,6 +486,53 @@ struct Api {
         return launch_engine<Net>(g, io, kc, cfg, st, g->queue);
     }
 
+    /* ---------------- allocation-free variant ----------------
+     * Same solve as solve_device, but its scratch -- the work-queue counter,
+     * the cost-hint bucket counters and the cell-order buffer -- lives in a
+     * caller-provided device region (the generated file passes the address
+     * of its static __device__ array).  Nothing here allocates.  Layout of
+     * the region: [0, 8) queue counter, [256, 512) 64 bucket counters,
+     * [512, ...) order buffer (4 bytes per cell). */
+    static constexpr size_t NOALLOC_HEADER = 512;
+
+    static int solve_device_noalloc(Data *d, const dengo_cell_batch *b, double z,
+                                    const dengo_solver_config *cfg_in, void *stream,
+                                    unsigned char *scratch, size_t scratch_bytes)
+    {
+        if (!d || !b || !scratch) {
+            set_error("%s_solve_cells_device_noalloc: null argument", Net::NAME);
+            return -1;
+        }
+        const long long max_cells = (long long)((scratch_bytes - NOALLOC_HEADER) / sizeof(int));
+        if (b->ncells > max_cells) {
+            set_error("%s_solve_cells_device_noalloc: %lld cells exceed the allocation-free "
+                      "maximum of %lld cells per call", Net::NAME, b->ncells, max_cells);
+            return -1;
+        }
+        dengo_solver_config cfg;
+        if (cfg_in) cfg = *cfg_in;
+        else dengo_default_config(&cfg);
+        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED) {
+            set_error("%s_solve_cells_device_noalloc: unknown precision %d", Net::NAME,
+                      cfg.precision);
+            return -1;
+        }
+        Gpu *g = gpu(d);
+        cudaStream_t st = (cudaStream_t)stream;
+        if (load_z(d, z, st) != 0) return -1;
+        unsigned long long *queue = (unsigned long long *)scratch;
+        int *counts = (int *)(scratch + 256);
+        int *order = (int *)(scratch + NOALLOC_HEADER);
+        CellIO io = cell_io(b);
+        if (b->cost_hint && b->ncells > 0) {
+            if (launch_order(b->cost_hint, b->ncells, counts, order, st) != 0) return -1;
+            io.order = order;
+        }
+        KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
+        g->ts.z = z;
+        return launch_engine<Net>(g, io, kc, cfg, st, queue);
+    }
+
     /* <n>_solve_cells_host: the batch's pointers are host pointers.  The
      * arrays are copied to the device, solved, and copied back before the
      * call returns. */

@@ -1522,6 +1522,48 @@ int oxygen_solve_cells_device(oxygen_data *data, const dengo_cell_batch *batch, 
     return dgnet_oxygen::Api::solve_device(data, batch, z, cfg, stream);
 }
 
+/* ---- allocation-free solve ------------------------------------------------
+ * For callers that cannot allocate device memory while they run -- a host
+ * code that reserves the device's memory for its own pool at start-up, or
+ * one that must not let a call synchronise the device the way cudaMalloc
+ * and cudaFree do.  The solver's scratch (work-queue counter, cost-hint
+ * bucket counters, cell-order buffer) lives in this file-scope array, which
+ * every GPU that loads the library holds until the process exits.  The
+ * array's host-side name is only a stand-in, so its device address is looked
+ * up once per device with cudaGetSymbolAddress, the first time the entry
+ * point runs on that device: make that first call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race on it; each call
+ * clears the counters it uses before its kernels read them. */
+#define OXYGEN_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define OXYGEN_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) unsigned char oxygen_noalloc_scratch[OXYGEN_NOALLOC_SCRATCH_BYTES];
+static unsigned char *oxygen_noalloc_addr[OXYGEN_NOALLOC_MAX_DEVICES];
+
+int oxygen_solve_cells_device_noalloc(oxygen_data *data, const dengo_cell_batch *batch, double z,
+                                       const dengo_solver_config *cfg, void *stream)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= OXYGEN_NOALLOC_MAX_DEVICES) {
+        dg::set_error("oxygen_solve_cells_device_noalloc: no usable current device (%s)",
+                      cudaGetErrorString(e));
+        return -1;
+    }
+    if (!oxygen_noalloc_addr[dev]) {
+        unsigned char *p = nullptr;
+        e = cudaGetSymbolAddress((void **)&p, oxygen_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            dg::set_error("oxygen_solve_cells_device_noalloc: cudaGetSymbolAddress failed: %s",
+                          cudaGetErrorString(e));
+            return -1;
+        }
+        oxygen_noalloc_addr[dev] = p;
+    }
+    return dgnet_oxygen::Api::solve_device_noalloc(data, batch, z, cfg, stream,
+                                                    oxygen_noalloc_addr[dev],
+                                                    OXYGEN_NOALLOC_SCRATCH_BYTES);
+}
+
 int oxygen_solve_cells_host(oxygen_data *data, const dengo_cell_batch *batch, double z,
                              const dengo_solver_config *cfg)
 {

@@ -152,6 +152,7 @@ struct oxygen_data_ {
 };
 
 DENGO_DECLARE_NETWORK(oxygen)
+DENGO_DECLARE_NETWORK_NOALLOC(oxygen)
 
 #ifdef __cplusplus
 }

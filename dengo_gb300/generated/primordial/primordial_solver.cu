@@ -982,6 +982,48 @@ int primordial_solve_cells_device(primordial_data *data, const dengo_cell_batch 
     return dgnet_primordial::Api::solve_device(data, batch, z, cfg, stream);
 }
 
+/* ---- allocation-free solve ------------------------------------------------
+ * For callers that cannot allocate device memory while they run -- a host
+ * code that reserves the device's memory for its own pool at start-up, or
+ * one that must not let a call synchronise the device the way cudaMalloc
+ * and cudaFree do.  The solver's scratch (work-queue counter, cost-hint
+ * bucket counters, cell-order buffer) lives in this file-scope array, which
+ * every GPU that loads the library holds until the process exits.  The
+ * array's host-side name is only a stand-in, so its device address is looked
+ * up once per device with cudaGetSymbolAddress, the first time the entry
+ * point runs on that device: make that first call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race on it; each call
+ * clears the counters it uses before its kernels read them. */
+#define PRIMORDIAL_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define PRIMORDIAL_NOALLOC_MAX_DEVICES 64
+static __device__ __align__(256) unsigned char primordial_noalloc_scratch[PRIMORDIAL_NOALLOC_SCRATCH_BYTES];
+static unsigned char *primordial_noalloc_addr[PRIMORDIAL_NOALLOC_MAX_DEVICES];
+
+int primordial_solve_cells_device_noalloc(primordial_data *data, const dengo_cell_batch *batch, double z,
+                                       const dengo_solver_config *cfg, void *stream)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= PRIMORDIAL_NOALLOC_MAX_DEVICES) {
+        dg::set_error("primordial_solve_cells_device_noalloc: no usable current device (%s)",
+                      cudaGetErrorString(e));
+        return -1;
+    }
+    if (!primordial_noalloc_addr[dev]) {
+        unsigned char *p = nullptr;
+        e = cudaGetSymbolAddress((void **)&p, primordial_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            dg::set_error("primordial_solve_cells_device_noalloc: cudaGetSymbolAddress failed: %s",
+                          cudaGetErrorString(e));
+            return -1;
+        }
+        primordial_noalloc_addr[dev] = p;
+    }
+    return dgnet_primordial::Api::solve_device_noalloc(data, batch, z, cfg, stream,
+                                                    primordial_noalloc_addr[dev],
+                                                    PRIMORDIAL_NOALLOC_SCRATCH_BYTES);
+}
+
 int primordial_solve_cells_host(primordial_data *data, const dengo_cell_batch *batch, double z,
                              const dengo_solver_config *cfg)
 {

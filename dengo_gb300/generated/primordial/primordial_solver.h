@@ -176,6 +176,7 @@ struct primordial_data_ {
 };
 
 DENGO_DECLARE_NETWORK(primordial)
+DENGO_DECLARE_NETWORK_NOALLOC(primordial)
 
 #ifdef __cplusplus
 }

@@ -183,6 +183,27 @@ typedef int (*jac_f)(double *, double *, int, int, void *);
     double n##_species_weight(int i);                                          \
     const char *n##_last_error(void);
 
+/* <n>_solve_cells_device_noalloc -- no counterpart in the reference.
+ * The same solve as <n>_solve_cells_device, for callers that cannot allocate
+ * device memory while they run (a host code that hands all device memory to
+ * its own pool at start-up, or one that must not let a call synchronise the
+ * device as cudaMalloc/cudaFree do).  It allocates nothing: its scratch (the
+ * work-queue counter, the cost-hint bucket counters and the cell-order
+ * buffer) is a 4 MiB static device array inside the library, held by every
+ * GPU that loads the library until the process exits, which caps a call at
+ * 1 048 448 cells (larger batches are rejected with an error, -1).  The
+ * first call on a device looks up that array's device address; make it
+ * before any stream capture.  Calls share the array, so calls that overlap
+ * on the GPU race; the counters are cleared at the start of every call.
+ * The caller still passes the data context from <n>_setup_data* and every
+ * input and output array. */
+#define DENGO_DECLARE_NETWORK_NOALLOC(n)                                       \
+    int n##_solve_cells_device_noalloc(n##_data *data,                         \
+                                       const dengo_cell_batch *batch,          \
+                                       double z,                               \
+                                       const dengo_solver_config *cfg,         \
+                                       void *stream);
+
 /* The unprefixed reference names, exported by every network library (one
  * network per library, as in the reference). */
 void ensure_electron_consistency(double *input, int nstrip, int nchem);
@@ -193,6 +214,7 @@ int BE_chem_solve(rhs_f f, jac_f J, double *u, double dt, double *rtol,
                   void *sdata, double *u0, double *s, double *gu, double *Ju);
 
 DENGO_DECLARE_NETWORK(primordial)
+DENGO_DECLARE_NETWORK_NOALLOC(primordial)
 
 #ifdef __cplusplus
 }
