@@ -11,13 +11,14 @@
  * instruction still serves 32 cells.
  *
  * Work split of one sweep (barriers between phases):
- *   warp 0        substep bookkeeping, T(ge), log T, bin; residual; pivot
- *                 search and row swap; back substitution; Newton update and
- *                 convergence test; cell refill (work queue)
+ *   warp 0        substep bookkeeping, T(ge), log T, bin; pivot search and
+ *                 row swap; back substitution; the convergence decision;
+ *                 cell refill (work queue)
  *   all warps     table interpolation (tables k = w mod NP), RHS rows and
  *                 Jacobian entries of part w (generated partition balanced by
- *                 operation count), multipliers and row updates of the LU
- *                 for rows i = w mod NP
+ *                 operation count); for rows i = w mod NP: the residual, the
+ *                 LU multipliers and row updates, the Newton update and the
+ *                 row's max-norm / NaN test (mixed: the refinement residual)
  * Every value is computed with exactly the operations of the single-lane
  * engine (dg_engine.cuh), so results are bit-identical to it and hence to the
  * reference.  Per-cell state lives in shared memory as [slot][32] doubles.
@@ -51,7 +52,7 @@ struct SplitLayout {
     static constexpr int PREV = RT + N;
     static constexpr int SCAL = PREV + N;  /* T, Tge, Tdef, -dt, piv, 1/piv */
     static constexpr int SLOTS = SCAL + 6;
-    static constexpr int NFLAGS = 10;
+    static constexpr int NFLAGS = 10 + N;  /* 10 cell flags, then one per row (F_ROW + i) */
     /* per-cell ints after the doubles: NFLAGS flags, then (mixed) the row
      * and column scale exponents and the FP32 pivots, N each */
     static constexpr int NINTS = NFLAGS + (MIXED ? 3 * N : 0);
@@ -60,7 +61,7 @@ struct SplitLayout {
 
 /* per-cell int flags; F_MIX: 0 FP64 elimination, 1 refining, 2 refined */
 enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6,
-             F_MIX = 7, F_EPREV = 8 };
+             F_MIX = 7, F_EPREV = 8, F_ROW = 10 };
 
 /* The mixed variant is held to the register budget of three 4-warp CTAs per
  * SM, the occupancy its shared memory allows for the 10-species network. */
@@ -229,15 +230,18 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             }
         }
         __syncthreads();
-        /* ---- P3 (warp 0): residual g = u - u0 - dt f (scaled), y for the Jacobian ---- */
-        if (w == 0 && act && F(F_OKR)) {
-            for (int i = 0; i < N; i++) {
+        /* ---- P3 (all warps, rows i = w mod NP): residual g = u - u0 - dt f
+         *      (scaled), y for the Jacobian ---- */
+        if (act && F(F_OKR)) {
+            const double dtv = -S[3];
+            for (int i = w; i < N; i += NP) {
                 const double u = Y[i] * INV[i];
                 double g = G[i] * INV[i];
-                g = u - U0[i] - dt * g;
+                g = u - U0[i] - dtv * g;
                 G[i] = g;
                 U[i] = u;
                 Y[i] = u * SC[i];
+                if (MIXED) MI(N + i) = MixedSolve<Net, 32>::NONE;
             }
         }
         __syncthreads();
@@ -258,23 +262,83 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         }
         __syncthreads();
         const bool do_lu = do_j && F(F_OKJ);
-        if (w == 0 && do_lu) {
-            for (int i = 0; i < N; i++) U[i] = Y[i] * INV[i];
-        }
+        /* u = y / scale after the Jacobian (rows i = w mod NP; the mixed
+         * refinement below reuses Y for the residual of the same rows) */
+        if (do_lu)
+            for (int i = w; i < N; i += NP) U[i] = Y[i] * INV[i];
         /* ---- P5: LU.  FP64: pivot (warp 0) then row updates (all warps).
          *      Mixed: equilibrated FP32 factorisation and first solve on
          *      warp 0; each refinement's FP64 residual rows i = w mod NP on
          *      all warps, the FP32 correction on warp 0; the single-lane FP64
          *      elimination for a dense or non-finite system ---- */
         if (MIXED) {
-            const MixedSolve<Net, 32> ms{J, JF};
+            using MS = MixedSolve<Net, 32>;
+            const MS ms{J, JF};
+            const bool eq = do_lu && !F(F_DENSE);
+            /* M1 (rows i = w mod NP): row scale exponent s_i, finiteness of
+             * the row and of g_i, and the row's share of each column's
+             * largest scaled exponent (MI(N + j), reset to NONE in P3) */
+            if (eq) {
+#pragma unroll
+                for (int i = 0; i < N; i++) {
+                    if (i % NP != w) continue;
+                    int m = 0;
+                    bool fin = dg_expo(G[i]) != 0x7ff;
+#pragma unroll
+                    for (int j = 0; j < N; j++) {
+                        const int e = dg_expo(J[j * N + i]);
+                        fin = fin && e != 0x7ff;
+                        m = e > m ? e : m;
+                    }
+                    const int si = m ? 1022 - m : 0;
+                    MI(i) = si;
+                    F(F_ROW + i) = fin;
+#pragma unroll
+                    for (int j = 0; j < N; j++) {
+                        if (!Net::jnz(i, j)) continue;
+                        const int e = dg_expo(J[j * N + i]);
+                        if (e != 0) atomicMax(&MI(N + j), e + si);
+                    }
+                }
+            }
+            __syncthreads();
+            /* M2 (rows i = w mod NP): R A C rounded to FP32 */
+            if (eq) {
+#pragma unroll
+                for (int i = 0; i < N; i++) {
+                    if (i % NP != w) continue;
+                    const int si = MI(i);
+#pragma unroll
+                    for (int j = 0; j < N; j++) {
+                        const int cm = MI(N + j);
+                        const int tj = cm == MS::NONE ? 0 : 1022 - cm;
+                        JF[j * N + i] = Net::jnz(i, j) ? dg_f32_scaled(J[j * N + i], si + tj) : 0.0f;
+                    }
+                }
+            }
+            __syncthreads();
+            /* M3 (warp 0): FP32 factorisation and first solve; the FP64
+             * elimination for a dense or non-finite system */
             if (w == 0 && do_lu) {
                 double g[N], x[N];
                 int sx[N], tx[N], px[N];
-                for (int i = 0; i < N; i++) g[i] = G[i];
-                if (!F(F_DENSE) && ms.prepare(g, sx, tx, px, x)) {
+                bool ok = eq;
+                for (int i = 0; i < N; i++) {
+                    g[i] = G[i];
+                    ok = ok && F(F_ROW + i);
+                }
+                if (ok) {
                     for (int i = 0; i < N; i++) {
-                        MI(i) = sx[i];
+                        sx[i] = MI(i);
+                        const int cm = MI(N + i);
+                        tx[i] = cm == MS::NONE ? 0 : 1022 - cm;
+                    }
+                    ms.factor(px);
+                    int ed;
+                    ok = ms.apply(px, sx, tx, g, x, ed);
+                }
+                if (ok) {
+                    for (int i = 0; i < N; i++) {
                         MI(N + i) = tx[i];
                         MI(2 * N + i) = px[i];
                         X[i] = x[i];
@@ -389,18 +453,26 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             }
         }
         __syncthreads();
-        /* ---- P6 (warp 0): Newton update, convergence, substep control ---- */
+        /* ---- P6a (all warps, rows i = w mod NP): Newton update and each
+         *      row's max-norm / NaN test ---- */
+        if (act && F(F_OKR) && F(F_OKJ)) {
+            for (int i = w; i < N; i += NP) {
+                const double u = U[i] - 1.0 * G[i];
+                U[i] = u;
+                F(F_ROW + i) = dg_abs_gt_val(G[i], AT[i] + RT[i] * fabs(u)) ? 1 : (dg_isnan(u) ? 2 : 0);
+            }
+        }
+        __syncthreads();
+        /* ---- P6b (warp 0): the first row that fails decides, as in the
+         *      reference's row loop; substep control ---- */
         if (w == 0 && act) {
             bool ok = F(F_OKR) && F(F_OKJ), unsolved = false, nan = false;
             if (ok) {
-                for (int i = 0; i < N; i++) U[i] = U[i] - 1.0 * G[i];
                 for (int i = 0; i < N; i++) {
-                    if (dg_abs_gt_val(G[i], AT[i] + RT[i] * fabs(U[i]))) {
-                        unsolved = true;
-                        break;
-                    }
-                    if (dg_isnan(U[i])) {
-                        nan = true;
+                    const int r = F(F_ROW + i);
+                    if (r) {
+                        unsolved = r == 1;
+                        nan = r == 2;
                         break;
                     }
                 }
