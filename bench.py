@@ -106,6 +106,12 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+# DRAM bytes per cell of one solver launch, from the ncu captures of the
+# split engine on 14 592 cells (read + write; the state and tolerances, the
+# tables stay in L2).
+DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592}
+
+
 def temperatures(state):
     """Gas temperature of each cell (mass densities + ge), gamma = 5/3."""
     from dengo_gb300.workloads import KB, MH, PRIMORDIAL_ORDER, PRIMORDIAL_WEIGHTS
@@ -345,7 +351,10 @@ def run_ours(args):
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": None,
+                     "traffic": DRAM_BYTES_PER_CELL[args.precision] * n,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "14 592-cell launch (profiles/evolve_split_%s_cold14592.md)"
+                                       ", scaled by cells" % args.precision,
                      "peak_source": "measured FP64 FMA throughput (dg_peak.cu), this run",
                      "flop_per_sweep": F_SWEEP},
     }

@@ -51,7 +51,8 @@ struct SplitLayout {
     static constexpr int RT = AT + N;
     static constexpr int PREV = RT + N;
     static constexpr int SCAL = PREV + N;  /* T, Tge, Tdef, -dt, piv, 1/piv */
-    static constexpr int SLOTS = SCAL + 6;
+    static constexpr int RPV = SCAL + 6;    /* FP64 path: 1/pivot of each step */
+    static constexpr int SLOTS = RPV + (MIXED ? 0 : N);
     static constexpr int NFLAGS = 10 + N;  /* 10 cell flags, then one per row (F_ROW + i) */
     /* per-cell ints after the doubles: NFLAGS flags, then (mixed) the row
      * and column scale exponents and the FP32 pivots, N each */
@@ -62,6 +63,17 @@ struct SplitLayout {
 /* per-cell int flags; F_MIX: 0 FP64 elimination, 1 refining, 2 refined */
 enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6,
              F_MIX = 7, F_EPREV = 8, F_ROW = 10 };
+
+/* The FP64 elimination for a cell the mixed solve hands back (dense or
+ * non-finite system); kept out of line because it is rarely taken and large. */
+template <int N>
+__device__ __noinline__ void fp64_fallback(Slots<32> J, Slots<32> G)
+{
+    double g[N];
+    for (int i = 0; i < N; i++) g[i] = G[i];
+    gauss_elim_fast<N, 32>(J, g);
+    for (int i = 0; i < N; i++) G[i] = g[i];
+}
 
 /* The mixed variant is held to the register budget of three 4-warp CTAs per
  * SM, the occupancy its shared memory allows for the 10-species network. */
@@ -77,7 +89,8 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
     const Slots<32> J{cellbase + L::J * 32}, R{cellbase + L::R * 32}, Y{cellbase + L::Y * 32},
         G{cellbase + L::G * 32}, U{cellbase + L::U * 32}, U0{cellbase + L::U0 * 32},
         SC{cellbase + L::SC * 32}, INV{cellbase + L::INV * 32}, AT{cellbase + L::AT * 32},
-        RT{cellbase + L::RT * 32}, PREV{cellbase + L::PREV * 32}, S{cellbase + L::SCAL * 32};
+        RT{cellbase + L::RT * 32}, PREV{cellbase + L::PREV * 32}, S{cellbase + L::SCAL * 32},
+        RPV{cellbase + L::RPV * 32};
     const SlotsF<32> JF{(float *)(dg_smem + L::JF * 32) + l};
     int *iflags = (int *)(dg_smem + L::SLOTS * 32);
     auto F = [&](int f) -> int & { return iflags[f * 32 + l]; };
@@ -346,8 +359,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                     F(F_MIX) = 1;
                     F(F_EPREV) = 0x7ff;
                 } else {
-                    gauss_elim_fast<N, 32>(J, g);
-                    for (int i = 0; i < N; i++) G[i] = g[i];
+                    fp64_fallback<N>(J, G);
                     F(F_MIX) = 0;
                 }
             }
@@ -378,10 +390,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                         F(F_EPREV) = eprev;
                         F(F_MIX) = more ? 1 : 2;
                     } else {
-                        double g[N];
-                        for (int i = 0; i < N; i++) g[i] = G[i];
-                        gauss_elim_fast<N, 32>(J, g);
-                        for (int i = 0; i < N; i++) G[i] = g[i];
+                        fp64_fallback<N>(J, G);
                         F(F_MIX) = 0;
                     }
                 }
@@ -413,8 +422,10 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                         G[p] = t;
                     }
                     const double piv = J[k * N + k];
+                    const double rp = 1.0 / piv;
                     S[4] = piv;
-                    S[5] = 1.0 / piv;
+                    S[5] = rp;
+                    RPV[k] = rp;   /* reused by the back substitution */
                 }
                 __syncthreads();
                 if (do_lu) {
@@ -439,7 +450,9 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             }
             __syncthreads();
             if (w == 0 && do_lu) {
-                /* back substitution; the pivots are the final diagonal */
+                /* back substitution; the pivots are the final diagonal and
+                 * their reciprocals were formed during the elimination */
+                RPV[N - 1] = 1.0 / J[(N - 1) * N + (N - 1)];
                 for (int i = N - 1; i >= 0; i--) {
                     double xi = G[i];
                     for (int j = i + 1; j < N; j++) {
@@ -447,8 +460,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                         const double xj = G[j];
                         if (dg_nonzero(aij) || !dg_finite(xj)) xi = xi - aij * xj;
                     }
-                    const double piv = J[i * N + i];
-                    G[i] = dg_div(xi, piv, 1.0 / piv);
+                    G[i] = dg_div(xi, J[i * N + i], RPV[i]);
                 }
             }
         }

@@ -14,8 +14,10 @@ Ferland's HDF5 cooling tables.  Neither is available here, so the tables are
 seeded smooth synthetic curves of the physical shape (``synthetic_rates``):
 ionisation ~ T^1/2 exp(-chi/kT), recombination ~ T^-0.7, cooling ~ T^1/2
 exp(-chi/kT), with ionisation potentials and amplitudes drawn per ion from a
-seed derived from the ion's name.  The same tables feed the GPU solver and the
-oracle.  Photo-ionisation/heating (HM12 tables) are not set up.
+seed derived from the ion's name.  The UV-background tables (HM12) are
+replaced the same way (``photo_data``), and the reference's own redshift
+interpolation and extrapolation turn them into rate tables (``photo_rate``).
+The same tables feed the GPU solver and the oracle.
 """
 
 import hashlib
@@ -73,27 +75,100 @@ def cooling_rate(atom, stage):
     return rate
 
 
-@registry_setup
-def setup_ionization(atom_name, photo_background=None, cooling=True):
-    """Register the ions of ``atom_name`` with their ionisation,
-    recombination and cooling terms; returns the new names."""
-    if photo_background is not None:
-        raise NotImplementedError("photo-ionisation tables (HM12) are not available here")
+def photo_data(element, ion_name, kind):
+    """Seeded synthetic stand-in for the ion-by-ion UV-background tables the
+    reference reads (input/photoionization/<el>_ion_by_ion_photoionization_
+    <bg>.h5, input/photoheating/...; datasets ``z`` and ``<ion>``): 60
+    redshifts in [0.01, 15], a log-normal bump in 1 + z per ion."""
+    rng = _ion_rng("%s:%s:%s" % (kind, element, ion_name))
+    z = np.logspace(-2.0, np.log10(15.0), 60)
+    lo, hi = (-13.5, -11.0) if kind == "photoionization" else (-25.5, -23.0)
+    amp = 10 ** rng.uniform(lo, hi)
+    zp = rng.uniform(1.5, 3.5)
+    vals = amp * np.exp(-0.5 * ((np.log1p(z) - np.log1p(zp)) / 0.6) ** 2) + amp * 1e-3
+    return z, vals
+
+
+def photo_rate(element, ion_name, kind):
+    """Redshift table of a photoionisation rate or photoheating term: the
+    reference's interpolation and log-space extrapolation
+    (reaction_classes.py:214-260, 457-503, end_method 0), same numpy
+    operations, on the tables of ``photo_data``."""
+    def rate(network):
+        dataz, dataS = photo_data(element, ion_name, kind)
+        vals = np.interp(network.z, dataz, dataS)
+        vals = np.log10(vals)
+        logz = np.log10(network.z)
+        logdataz = np.log10(dataz)
+        logdataS = np.log10(dataS)
+        extrapdown = logdataS[0] + \
+            (logz - logdataz[0]) * (logdataS[0] - logdataS[1]) \
+            / (logdataz[0] - logdataz[1])
+        vals[logz < logdataz[0]] = extrapdown[logz < logdataz[0]]
+        extrapup = logdataS[-1] + \
+            (logz - logdataz[-1]) * (logdataS[-1] - logdataS[-2]) \
+            / (logdataz[-1] - logdataz[-2])
+        vals[logz > logdataz[-1]] = extrapup[logz > logdataz[-1]]
+        vals = 10.0**vals
+        return vals
+    return rate
+
+
+def _register_ions(atom_name, photo_background=None, cooling=True):
+    """Register the ions of ``atom_name`` and their terms; returns the names
+    of everything registered: [species, cooling actions, reactions]."""
     num = periodic_table_by_name[atom_name][0]
     de = species_registry["de"]
     ions = {i: AtomicSpecies(atom_name, i) for i in range(num + 1)}
+    names = [set(), set(), set()]
     for i in range(num + 1):
         s = ions[i]
+        names[0].add(s.name)
         sm1, sp1 = ions.get(i - 1), ions.get(i + 1)
         if sp1 is not None:
-            Reaction("%s_i" % s.name, ionization_rate(atom_name, i),
-                     [(1, s), (1, de)], [(1, sp1), (2, de)])
+            names[2].add(Reaction("%s_i" % s.name, ionization_rate(atom_name, i),
+                                  [(1, s), (1, de)], [(1, sp1), (2, de)]).name)
         if sm1 is not None:
-            Reaction("%s_r" % s.name, recombination_rate(atom_name, i),
-                     [(1, s), (1, de)], [(1, sm1)])
+            names[2].add(Reaction("%s_r" % s.name, recombination_rate(atom_name, i),
+                                  [(1, s), (1, de)], [(1, sm1)]).name)
         if cooling:
             act = CoolingAction("%s_c" % s.name, "-%s_c * %s * de" % (s.name, s.name))
             act.tables["%s_c" % s.name] = cooling_rate(atom_name, i)
+            names[1].add(act.name)
+        if sp1 is not None and photo_background is not None:
+            ion = s.name.lower()
+            el = ion.split("_")[0]
+            names[2].add(Reaction("%s_pi" % s.name, photo_rate(el, ion, "photoionization"),
+                                  [(1, s)], [(1, sp1), (1, de)]).name)
+            if cooling:
+                act = CoolingAction("%s_ph" % s.name, "%s_ph * %s" % (s.name, s.name))
+                act.tables["%s_ph" % s.name] = photo_rate(el, ion, "photoheating")
+                names[1].add(act.name)
+    return names
+
+
+@registry_setup
+def setup_ionization(atom_name, photo_background=None, cooling=True):
+    """Register the ions of ``atom_name`` with their ionisation,
+    recombination and cooling terms; returns the new names (the reference's
+    registry_setup contract).  With a ``photo_background`` every ion but the
+    bare nucleus also gets ``<ion>_pi`` (photoionisation, ion -> next ion +
+    e) and, with cooling, ``<ion>_ph`` (photoheating ``<ion>_ph * <ion>``),
+    tabulated in redshift (reaction_classes.py:200-271, 443-514)."""
+    _register_ions(atom_name, photo_background, cooling)
+
+
+def oxygen_uvb_network(T_bounds=(1e0, 1e10), n_bins=8192, z_bounds=(0.0, 15.0), n_z_bins=100):
+    """The oxygen network under a (synthetic) UV background: photoionisation
+    and photoheating of every ion, tabulated on 100 redshifts over [0, 15]."""
+    from .chemical_network import ChemicalNetwork
+    net = ChemicalNetwork()
+    net.add_species("de")
+    for atom in ("H", "O", "He"):
+        net.add_collection(*_register_ions(atom, photo_background="HM12"))
+    net.init_temperature(T_bounds, n_bins=n_bins)
+    net.init_redshift(z_bounds, n_z_bins=n_z_bins)
+    return net
 
 
 def oxygen_network(T_bounds=(1e0, 1e10), n_bins=8192):
@@ -103,7 +178,6 @@ def oxygen_network(T_bounds=(1e0, 1e10), n_bins=8192):
     net = ChemicalNetwork()
     net.add_species("de")
     for atom in ("H", "O", "He"):
-        s, c, r = setup_ionization(atom)
-        net.add_collection(s, c, r)
+        net.add_collection(*_register_ions(atom))
     net.init_temperature(T_bounds, n_bins=n_bins)
     return net

@@ -5,6 +5,8 @@
   of ``primordial_cooling`` except ``compton``), tables of 1024 log-spaced
   bins over 1-1e9 K.
 * ``oxygen``: H, He and O ion-by-ion (16 equations); see :mod:`ion_by_ion`.
+* ``oxygen_uvb``: the same ions under a UV background: photoionisation and
+  photoheating tabulated in redshift (100 bins over z in [0, 15]).
 """
 
 from . import reaction_classes as rc
@@ -37,7 +39,7 @@ def primordial_network(T_bounds=(1.0, 1e9), n_bins=1024, with_compton=False):
     return net
 
 
-SHIPPED_NETWORKS = ("primordial", "oxygen")
+SHIPPED_NETWORKS = ("primordial", "oxygen", "oxygen_uvb")
 
 
 def build_network(name):
@@ -47,4 +49,7 @@ def build_network(name):
     if name == "oxygen":
         from .ion_by_ion import oxygen_network
         return oxygen_network()
+    if name == "oxygen_uvb":
+        from .ion_by_ion import oxygen_uvb_network
+        return oxygen_uvb_network()
     raise KeyError("unknown network %r" % name)

@@ -338,3 +338,7 @@ int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, do
     net->free_data(data);
     return it;
 }
+
+/* log x correctly rounded to double (through long double; checked against
+ * a 200-bit log in tests/test_oracle_golden.py) */
+double dgo_crlog(double x) { return (double)logl(x); }

@@ -96,6 +96,9 @@ int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, do
                          int dims, const dgo_config *cfg, double *ttot_out, double *dt_out,
                          dgo_stats *st);
 
+/* log x correctly rounded (long double log rounded to double) */
+double dgo_crlog(double x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,6 +18,13 @@
 
 #include "../be_oracle.h"
 
+/* log T of calculate_temperature: the reference's libm log, or (built with
+ * -DDGO_LOG=dgo_crlog) a correctly rounded one, for telling libm rounding
+ * apart from other differences */
+#ifndef DGO_LOG
+#define DGO_LOG log
+#endif
+
 #define MAX_NCELLS 1024
 #define NCHEM 16
 #define NTAB 36
@@ -132,7 +139,7 @@ void dgo_oxygen_calculate_temperature(dgo_oxygen_data *data, double *input,
         } else if (data->Ts[i] > data->bounds[1]) {
             data->Ts[i] = data->bounds[1];
         }
-        data->logTs[i] = log(data->Ts[i]);
+        data->logTs[i] = DGO_LOG(data->Ts[i]);
         data->invTs[i] = 1.0 / data->Ts[i];
         data->dTs_ge[i] = density*mh/(kb*(H_1/(gamma - 1.0) + H_2/(gamma - 1.0) + He_1/(gamma - 1.0) + He_2/(gamma - 1.0) + He_3/(gamma - 1.0) + O_1/(gamma - 1.0) + O_2/(gamma - 1.0) + O_3/(gamma - 1.0) + O_4/(gamma - 1.0) + O_5/(gamma - 1.0) + O_6/(gamma - 1.0) + O_7/(gamma - 1.0) + O_8/(gamma - 1.0) + O_9/(gamma - 1.0) + de/(gamma - 1.0)));
     }

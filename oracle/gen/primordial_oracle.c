@@ -18,6 +18,13 @@
 
 #include "../be_oracle.h"
 
+/* log T of calculate_temperature: the reference's libm log, or (built with
+ * -DDGO_LOG=dgo_crlog) a correctly rounded one, for telling libm rounding
+ * apart from other differences */
+#ifndef DGO_LOG
+#define DGO_LOG log
+#endif
+
 #define MAX_NCELLS 1024
 #define NCHEM 10
 #define NTAB 44
@@ -114,7 +121,7 @@ void dgo_primordial_calculate_temperature(dgo_primordial_data *data, double *inp
         } else if (data->Ts[i] > data->bounds[1]) {
             data->Ts[i] = data->bounds[1];
         }
-        data->logTs[i] = log(data->Ts[i]);
+        data->logTs[i] = DGO_LOG(data->Ts[i]);
         data->invTs[i] = 1.0 / data->Ts[i];
         data->dTs_ge[i] = density*mh/(kb*(H2_1/(gamma - 1.0) + H2_2/(gamma - 1.0) + H_1/(gamma - 1.0) + H_2/(gamma - 1.0) + H_m0/(gamma - 1.0) + He_1/(gamma - 1.0) + He_2/(gamma - 1.0) + He_3/(gamma - 1.0) + de/(gamma - 1.0)));
     }

@@ -26,14 +26,16 @@ class Config(C.Structure):
                 ("dt_ratio_floor", C.c_double), ("floor_value", C.c_double)]
 
 
-def build_oracle(name="primordial", force=False):
-    """Compile the C restatement for network ``name`` (gcc)."""
+def build_oracle(name="primordial", force=False, crlog=False):
+    """Compile the C restatement for network ``name`` (gcc).  ``crlog``: the
+    variant whose log T is correctly rounded instead of libm's."""
     os.makedirs(BUILD, exist_ok=True)
-    out = os.path.join(BUILD, "libdgo_%s.so" % name)
+    out = os.path.join(BUILD, "libdgo_%s%s.so" % (name, "_crlog" if crlog else ""))
     srcs = [os.path.join(HERE, "be_oracle.c"), os.path.join(HERE, "gen", "%s_oracle.c" % name)]
     if force or not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out)
                                                for s in srcs):
-        subprocess.check_call(["gcc"] + CFLAGS + srcs + ["-o", out, "-lm"])
+        extra = ["-DDGO_LOG=dgo_crlog"] if crlog else []
+        subprocess.check_call(["gcc"] + CFLAGS + extra + srcs + ["-o", out, "-lm"])
     return out
 
 
@@ -44,9 +46,9 @@ def _dp(a):
 class Oracle:
     """The C restatement of the reference solver for one network."""
 
-    def __init__(self, name="primordial"):
+    def __init__(self, name="primordial", crlog=False):
         self.name = name
-        self.lib = C.CDLL(build_oracle(name))
+        self.lib = C.CDLL(build_oracle(name, crlog=crlog))
         self.net_addr = C.addressof(C.c_char.in_dll(self.lib, "dgo_%s_network" % name))
         self.lib.dgo_default_config.restype = Config
         self.lib.dgo_evolve_cells.argtypes = [

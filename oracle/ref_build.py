@@ -47,7 +47,31 @@ ALIASES = dict(HI="H_1", HII="H_2", HM="H_m0", HeI="He_1", HeII="He_2",
 def _install_shims():
     h5 = types.ModuleType("h5py")
 
+    class _Reader:
+        """The UV-background input files (input/photoionization/<el>_ion_by_
+        ion_photoionization_<bg>.h5, input/photoheating/...), served from the
+        seeded stand-in tables of dengo_gb300/ion_by_ion.py."""
+
+        def __init__(self, path):
+            base = os.path.basename(path)
+            self.element = base.split("_")[0]
+            self.kind = "photoionization" if "photoionization" in base else "photoheating"
+
+        def __getitem__(self, key):
+            from dengo_gb300.ion_by_ion import photo_data
+            z, vals = photo_data(self.element, key if key != "z" else self.element + "_1",
+                                 self.kind)
+            return z if key == "z" else vals
+
+        def close(self):
+            pass
+
     class _File:
+        def __new__(cls, path, mode="r"):
+            if path.startswith("input/photo"):
+                return _Reader(path)
+            return super().__new__(cls)
+
         def __init__(self, path, mode="r"):
             self.path = path
             os.makedirs(path + ".d", exist_ok=True)
@@ -117,7 +141,7 @@ def _reference_primordial():
     return net
 
 
-def _reference_oxygen():
+def _reference_oxygen(photo_background=None):
     """The reference's own ion-by-ion setup (dengo/ion_by_ion.py:33-56) for
     H, O and He.  ChiantiPy is absent: a stand-in module lets
     ``chianti_rate`` register its reactions (it only checks that ChiantiPy
@@ -141,7 +165,7 @@ def _reference_oxygen():
     net = cn.ChemicalNetwork()
     net.add_species("de")
     for atom in ("H", "O", "He"):
-        s, c, r = setup_ionization(atom)
+        s, c, r = setup_ionization(atom, photo_background=photo_background)
         num = {"H": 1, "He": 2, "O": 8}[atom]
         for i in range(num + 1):
             name = rc.species_registry["%s_%d" % (atom, i + 1)].name
@@ -153,6 +177,8 @@ def _reference_oxygen():
             act.tables["%s_c" % name] = mine.cooling_rate(atom, i)
         net.add_collection(s, c, r)
     net.init_temperature((1e0, 1e10), n_bins=8192)
+    if photo_background is not None:
+        net.init_redshift((0.0, 15.0), n_z_bins=100)
     return net
 
 
@@ -249,15 +275,17 @@ void ref_evolve_cells(const double *dtf, double *dt, double z, double *input, do
 def build(name="primordial"):
     """Render and compile one network in a fresh interpreter (the reference's
     registries are module globals, so networks are built one per process)."""
-    if name not in ("primordial", "oxygen"):
-        raise ValueError("networks rendered with the reference here: primordial, oxygen")
+    if name not in ("primordial", "oxygen", "oxygen_uvb"):
+        raise ValueError("networks rendered with the reference here: primordial, oxygen, "
+                         "oxygen_uvb")
     if not os.path.isdir(os.path.join(REF_ROOT, "dengo")):
         raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
     if "dengo" in sys.modules:
         lib = os.path.join(OUT, "libref_%s.so" % name)
         subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
         return lib
-    net = _reference_primordial() if name == "primordial" else _reference_oxygen()
+    net = (_reference_primordial() if name == "primordial" else
+           _reference_oxygen("HM12" if name == "oxygen_uvb" else None))
     odir = os.path.join(OUT, name)
     os.makedirs(odir, exist_ok=True)
     net.write_solver(name, output_dir=odir, ode_solver_source=None)

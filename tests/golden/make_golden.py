@@ -159,36 +159,42 @@ if __name__ == "__main__" and len(sys.argv) == 1:
     main()
 
 
-def make_oxygen():
-    """Golden vectors of the oxygen ion-by-ion network (16 equations): the
+def make_ion(name="oxygen", zs=(None,)):
+    """Golden vectors of an ion-by-ion network (16 equations): the
     reference's own setup_ionization and templates, with the synthetic
-    CHIANTI stand-in tables (oracle/ref_build.py)."""
+    CHIANTI and UV-background stand-in tables (oracle/ref_build.py).  For a
+    network with redshift tables, one set of outputs per redshift."""
+    import hashlib
     import ref_build
     from oracle import Reference
+    from dengo_gb300.codegen.spec import network_spec
+    from dengo_gb300.networks import build_network
     from dengo_gb300.workloads import oxygen_cells
-    ref_build.build("oxygen")
-    ref = Reference("oxygen")
+    ref_build.build(name)
+    ref = Reference(name)
     out = {}
     st, dtf = oxygen_cells(48, seed=515)
-    r = ref.evolve_cells(st, dtf, nthreads=8)
     out["evolve_in"], out["evolve_dtf"] = st, dtf
-    for k in ("state", "atol", "dt", "ttot"):
-        out["evolve_%s" % k] = r[k]
+    for z in zs:
+        r = ref.evolve_cells(st, dtf, nthreads=8, z=-1.0 if z is None else z)
+        tag = "" if z is None else "_z%g" % z
+        for k in ("state", "atol", "dt", "ttot"):
+            out["evolve%s_%s" % (tag, k)] = r[k]
+    if zs != (None,):
+        out["redshifts"] = np.array(zs, dtype=float)
     # the solver's table order, and a SHA-256 of each table the reference wrote
-    import hashlib
-    from dengo_gb300.codegen.spec import network_spec
-    from dengo_gb300.ion_by_ion import oxygen_network
-    spec = network_spec(oxygen_network(), "oxygen")
-    tdir = os.path.join(ROOT, "oracle", "_ref", "oxygen", "oxygen_tables.h5.d")
+    spec = network_spec(build_network(name), name)
+    tdir = os.path.join(ROOT, "oracle", "_ref", name, "%s_tables.h5.d" % name)
     files = {f[:-4]: os.path.join(tdir, f) for f in os.listdir(tdir)}
     out["table_order"] = np.array([t.name for t in spec.tables])
-    sums = []
-    for t in spec.tables:
-        sums.append(hashlib.sha256(np.fromfile(files[t.name]).tobytes()).hexdigest())
-    out["table_sha256"] = np.array(sums)
-    np.savez_compressed(os.path.join(HERE, "oxygen_golden.npz"), **out)
-    print("wrote oxygen golden vectors")
+    out["table_sha256"] = np.array([hashlib.sha256(np.fromfile(files[t.name]).tobytes()).hexdigest()
+                                    for t in spec.tables])
+    np.savez_compressed(os.path.join(HERE, "%s_golden.npz" % name), **out)
+    print("wrote %s golden vectors" % name)
 
 
-if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "oxygen":
-    make_oxygen()
+if __name__ == "__main__" and len(sys.argv) > 1:
+    if sys.argv[1] == "oxygen":
+        make_ion("oxygen")
+    elif sys.argv[1] == "oxygen_uvb":
+        make_ion("oxygen_uvb", zs=(0.0, 2.5, 9.0, 20.0))

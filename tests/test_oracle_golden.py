@@ -46,3 +46,17 @@ def test_edge_cases_behave_like_reference(golden, tables_in_order, oracle):
     assert r["status"][1] == 2                                     # negative density
     assert r["status"][2] == 2                                     # zero density -> NaN
     assert np.array_equal(r["state"][0], g["evolve_edge_in"][0])  # untouched state
+
+
+def test_oracle_correctly_rounded_log():
+    """dgo_crlog (the oracle variant's log T) is log correctly rounded."""
+    import ctypes as C
+    mpmath = pytest.importorskip("mpmath")
+    from oracle import build_oracle
+    lib = C.CDLL(build_oracle("primordial", crlog=True))
+    lib.dgo_crlog.restype = C.c_double
+    lib.dgo_crlog.argtypes = [C.c_double]
+    mpmath.mp.prec = 200
+    xs = np.exp(np.random.default_rng(5).uniform(0.0, np.log(2e9), 5000))
+    for x in xs:
+        assert lib.dgo_crlog(float(x)) == float(mpmath.log(mpmath.mpf(float(x)))), x
