@@ -57,6 +57,10 @@ def parse():
     p.add_argument("--order", type=int, default=1, help="start the costliest cells first")
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--warps-per-cell", type=int, default=4, choices=[1, 2, 4])
+    p.add_argument("--sweep-budget", type=int, default=2000,
+                   help="> 0: redistribute cells still running after this many Newton "
+                        "sweeps into a second, densely packed launch (same results)")
+    p.add_argument("--tail-grid", type=int, default=0)
     p.add_argument("--max-substeps", type=int, default=50000,
                    help="the reference's cap; lower only to profile a short launch")
     p.add_argument("--no-e2e", action="store_true")
@@ -230,6 +234,7 @@ def run_ours(args):
     cfg.schedule, cfg.block = args.schedule, args.block
     cfg.precision = 1 if args.precision == "mixed" else 0
     cfg.warps_per_cell = args.warps_per_cell
+    cfg.sweep_budget, cfg.tail_grid = args.sweep_budget, args.tail_grid
     cfg.max_substeps = args.max_substeps
 
     def device_batch(st_host):
@@ -345,9 +350,10 @@ def run_ours(args):
                    "cells_per_gpu": n, "precision": args.precision, "schedule": args.schedule,
                    "order": "costliest first" if args.order else "input order",
                    "warps_per_cell": args.warps_per_cell,
+                   "sweep_budget": args.sweep_budget,
                    "l2": "flushed (256 MB write) before every step",
                    "warmup": "%d steps over a %d-cell copy" % (args.warmup, wn)},
-        "wall_s": wall, "step_ms": step_ms, "gpu_launches": args.steps,
+        "wall_s": wall, "step_ms": step_ms, "gpu_launches": args.steps * ((4 if args.sweep_budget > 0 else 1) + (3 if args.order else 0)),
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,

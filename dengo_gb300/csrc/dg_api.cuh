@@ -69,6 +69,14 @@ struct Gpu {
     int *order = nullptr;         /* cell order built from a cost hint */
     long long order_cap = 0;
     int *order_counts = nullptr;  /* [64]: bucket counts and offsets */
+    /* two-launch solve (sweep budget): suspension records, the resume list
+     * and its length, a status array when the caller passes none */
+    double *rec = nullptr;
+    long long rec_cap = 0;        /* cells */
+    int *resume_list = nullptr;
+    int *status_buf = nullptr;
+    long long list_cap = 0;       /* cells */
+    unsigned int *resume_count = nullptr;
 };
 
 /* Writes order[0..n) (longest first) from the per-cell cost hint on stream
@@ -451,6 +459,10 @@ struct Api {
             cudaFree(g->d_buf);
             cudaFree(g->order);
             cudaFree(g->order_counts);
+            cudaFree(g->rec);
+            cudaFree(g->resume_list);
+            cudaFree(g->status_buf);
+            cudaFree(g->resume_count);
             if (g->stream) cudaStreamDestroy(g->stream);
             delete g;
         }
@@ -483,7 +495,64 @@ struct Api {
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         g->ts.z = z;
-        return launch_engine<Net>(g, io, kc, cfg, st, g->queue);
+        if (cfg.sweep_budget <= 0 || b->ncells <= 0)
+            return launch_engine<Net>(g, io, kc, cfg, st, g->queue);
+        return solve_two_launch(g, io, kc, cfg, st);
+    }
+
+    /* Stiff-cell redistribution.  Launch 1 solves every cell but sets aside
+     * (writes a suspension record for) each cell that reaches the sweep
+     * budget at a substep boundary; a list of the set-aside cells is built
+     * on the device; launch 2 resumes them from their records on one CTA per
+     * SM per 32 set-aside cells (the surplus CTAs exit at once), the cells
+     * spread over those CTAs: a few stiff cells then share warps -- free on
+     * the FP64 pipe -- instead of competing CTAs sharing each SM's FP64
+     * units.  Every cell's operations are those of one launch, so the
+     * results are bit-identical to it. */
+    static int solve_two_launch(Gpu *g, CellIO io, KernelCfg kc, dengo_solver_config cfg,
+                                cudaStream_t st)
+    {
+        const long long n = io.ncells;
+        if (n > g->rec_cap) {
+            if (g->rec) cudaFree(g->rec);
+            g->rec = nullptr;
+            g->rec_cap = 0;
+            DG_CUDA(cudaMalloc(&g->rec, sizeof(double) * rec_len<N>() * n));
+            g->rec_cap = n;
+        }
+        if (n > g->list_cap) {
+            if (g->resume_list) cudaFree(g->resume_list);
+            if (g->status_buf) cudaFree(g->status_buf);
+            g->resume_list = g->status_buf = nullptr;
+            g->list_cap = 0;
+            DG_CUDA(cudaMalloc(&g->resume_list, sizeof(int) * n));
+            DG_CUDA(cudaMalloc(&g->status_buf, sizeof(int) * n));
+            g->list_cap = n;
+        }
+        if (!g->resume_count) DG_CUDA(cudaMalloc(&g->resume_count, sizeof(unsigned int)));
+        CellIO io1 = io;
+        if (!io1.status) io1.status = g->status_buf;
+        KernelCfg k1 = kc;
+        k1.sweep_budget = cfg.sweep_budget;
+        k1.rec = g->rec;
+        if (int e = launch_engine<Net>(g, io1, k1, cfg, st, g->queue)) return e;
+        DG_CUDA(cudaMemsetAsync(g->resume_count, 0, sizeof(unsigned int), st));
+        const int lg = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+        resume_list_fill_kernel<<<lg, 256, 0, st>>>(g->resume_list, n);
+        resume_list_kernel<<<lg, 256, 0, st>>>(io1.status, n, g->resume_list, g->resume_count);
+        DG_CUDA(cudaGetLastError());
+        CellIO io2 = io;
+        io2.order = g->resume_list;
+        KernelCfg k2 = kc;
+        k2.resume = 1;
+        k2.rec = g->rec;
+        k2.resume_count = g->resume_count;
+        k2.nsm = g->nsm;
+        dengo_solver_config c2 = cfg;
+        if (c2.schedule == DENGO_SCHED_PER_THREAD) c2.schedule = DENGO_SCHED_QUEUE;
+        c2.grid = cfg.tail_grid;   /* 0: the persistent default; CTAs whose
+                                      first 32 entries are past the list exit */
+        return launch_engine<Net>(g, io2, k2, c2, st, g->queue);
     }
 
     /* ---------------- allocation-free variant ----------------
@@ -969,6 +1038,8 @@ extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg)
     cfg->block = 0;
     cfg->grid = 0;
     cfg->warps_per_cell = 1;
+    cfg->sweep_budget = 0;
+    cfg->tail_grid = 0;
 }
 
 #endif

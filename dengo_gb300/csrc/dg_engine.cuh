@@ -34,7 +34,8 @@
 
 namespace dg {
 
-enum : int { ST_OK = 0, ST_MAX_SUBSTEPS = 1, ST_DT_UNDERFLOW = 2 };
+/* ST_SUSPENDED: set aside by the sweep budget; finished by a resume launch */
+enum : int { ST_OK = 0, ST_MAX_SUBSTEPS = 1, ST_DT_UNDERFLOW = 2, ST_SUSPENDED = 3 };
 
 /* Rate/cooling tables on the device, bin-major: for bin b and table k the
  * pair (r_k[b], r_k[b+1] - r_k[b]).  The difference is the reference's own
@@ -70,7 +71,26 @@ struct KernelCfg {
     int max_substeps;
     double dt_ratio_floor;
     double floor_value;
+    /* stiff-cell redistribution: a cell that has taken sweep_budget sweeps
+     * (> 0) writes its suspension record at its next substep boundary and
+     * ends with ST_SUSPENDED; with resume set, cells start from their record
+     * instead of the input.  rec: rec_len<N>() doubles per cell. */
+    int sweep_budget;
+    int resume;
+    double *rec;
+    /* resume launch: the number of suspended cells (device) and the SM
+     * count; only as many CTAs as give every SM one CTA per 32 (or BLOCK)
+     * of those cells keep running, so a few stiff cells share warps rather
+     * than competing CTAs */
+    const unsigned int *resume_count;
+    int nsm;
 };
+
+/* Suspension record of a cell at a substep boundary: state y, prev, scale,
+ * atol (all unscaled number densities), dt, ttot, accepted substeps, sweeps,
+ * failed substeps -- everything the driver carries between substeps. */
+template <int N>
+__host__ __device__ constexpr int rec_len() { return 4 * N + 5; }
 
 template <class Net, int BLOCK, bool MIXED = false>
 struct Lane {
@@ -322,7 +342,26 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
     const Slots<BLOCK> RT{base + L::OFF_RT * BLOCK};
 
     const long long stride = (long long)gridDim.x * BLOCK;
-    long long qi = queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * BLOCK + tid;
+    if (cfg.resume && cfg.resume_count) {
+        /* one lane per set-aside cell: a cell left waiting for a lane would
+         * start its remaining ~10^5 sweeps only when another finished */
+        const long long per_round = (long long)cfg.nsm * BLOCK;
+        const long long rounds = ((long long)*cfg.resume_count + per_round - 1) / per_round;
+        if (blockIdx.x >= cfg.nsm * (rounds > 0 ? rounds : 1)) return;
+    }
+    /* the work queue hands each warp 32 consecutive cells to start with (cells
+     * adjacent in the order, alike in cost, share a warp) -- except when
+     * resuming, where cells are spread over the CTAs; lanes then refill one
+     * cell at a time */
+    long long qi;
+    {
+        unsigned long long base = 0;
+        const bool chunk = queue && !cfg.resume;
+        if (chunk && (tid & 31) == 0) base = atomicAdd(queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        qi = chunk ? (long long)base + (tid & 31)
+                   : (queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * BLOCK + tid);
+    }
     long long cell = 0;
     bool dense = false;   /* a scale is not a positive finite number */
 
@@ -343,6 +382,30 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
         isweep = 0;
     };
     auto cell_begin = [&]() -> bool {
+        if (cfg.resume) {
+            /* continue a suspended cell from its record */
+            const double *rc = cfg.rec + cell * rec_len<N>();
+            dense = false;
+#pragma unroll
+            for (int s = 0; s < N; s++) {
+                y[s] = rc[s];
+                PREV[s] = rc[N + s];
+                SC[s] = rc[2 * N + s];
+                AT[s] = rc[3 * N + s];
+                RT[s] = io.rtol ? io.rtol[cell * io.cs + s * io.ss] : io.rtol_scalar;
+                INV[s] = 1.0 / SC[s];
+                dense = dense || !(SC[s] > 0.0 && dg_finite(SC[s]));
+            }
+            dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+            dt = rc[4 * N];
+            ttot = rc[4 * N + 1];
+            siter = (int)rc[4 * N + 2];
+            nsweeps = (int)rc[4 * N + 3];
+            nfail = (int)rc[4 * N + 4];
+            if (!(ttot < dtf)) return false;
+            substep_begin();
+            return true;
+        }
         double at[N];
 #pragma unroll
         for (int s = 0; s < N; s++) {
@@ -393,9 +456,26 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
         if (io.sweeps) io.sweeps[cell] = nsweeps;
         if (io.failures) io.failures[cell] = nfail;
     };
+    auto suspend = [&]() {
+        double *rc = cfg.rec + cell * rec_len<N>();
+#pragma unroll
+        for (int s = 0; s < N; s++) {
+            rc[s] = y[s];
+            rc[N + s] = PREV[s];
+            rc[2 * N + s] = SC[s];
+            rc[3 * N + s] = AT[s];
+        }
+        rc[4 * N] = dt;
+        rc[4 * N + 1] = ttot;
+        rc[4 * N + 2] = siter;
+        rc[4 * N + 3] = nsweeps;
+        rc[4 * N + 4] = nfail;
+        io.status[cell] = ST_SUSPENDED;
+    };
     auto fetch = [&]() {
         while (qi < io.ncells) {
             cell = io.order ? (long long)io.order[qi] : qi;
+            if (cell < 0) break; /* end of a resume list */
             if (cell_begin()) {
                 active = true;
                 return;
@@ -507,11 +587,12 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
             for (int i = 0; i < N; i++) y[i] = PREV[i];
             if (dt / dtf < cfg.dt_ratio_floor) done = ST_DT_UNDERFLOW;
         }
-        if (done < 0) {
+        if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
             substep_begin();
             continue;
         }
-        cell_end(done);
+        if (done < 0) suspend();
+        else cell_end(done);
         qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
         fetch();
     }

@@ -105,7 +105,25 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
     int siter = 0, isweep = 0, nsweeps = 0, nfail = 0;
     bool active = false, dense = false;
     const long long stride = (long long)gridDim.x * 32;
-    if (w == 0) qi = queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * 32 + l;
+    if (cfg.resume && cfg.resume_count) {
+        /* one lane per set-aside cell: a cell left waiting for a lane would
+         * start its remaining ~10^5 sweeps only when another finished */
+        const long long per_round = (long long)cfg.nsm * 32;
+        const long long rounds = ((long long)*cfg.resume_count + per_round - 1) / per_round;
+        if (blockIdx.x >= cfg.nsm * (rounds > 0 ? rounds : 1)) return;
+    }
+    if (w == 0) {
+        /* the work queue hands each CTA 32 consecutive cells to start with, so
+         * cells adjacent in the order (alike in cost) share a CTA -- except
+         * when resuming, where cells are spread over the CTAs; lanes then
+         * refill one cell at a time */
+        unsigned long long base = 0;
+        const bool chunk = queue && !cfg.resume;
+        if (chunk && l == 0) base = atomicAdd(queue, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        qi = chunk ? (long long)base + l
+                   : (queue ? (long long)atomicAdd(queue, 1ull) : (long long)blockIdx.x * 32 + l);
+    }
 
     auto substep_begin = [&]() {
         for (int i = 0; i < N; i++) {
@@ -117,6 +135,29 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         isweep = 0;
     };
     auto cell_begin = [&]() -> bool {
+        if (cfg.resume) {
+            /* continue a suspended cell from its record */
+            const double *rc = cfg.rec + cell * rec_len<N>();
+            dense = false;
+            for (int s = 0; s < N; s++) {
+                Y[s] = rc[s];
+                PREV[s] = rc[N + s];
+                SC[s] = rc[2 * N + s];
+                AT[s] = rc[3 * N + s];
+                RT[s] = io.rtol ? io.rtol[cell * io.cs + s * io.ss] : io.rtol_scalar;
+                INV[s] = 1.0 / SC[s];
+                dense = dense || !(SC[s] > 0.0 && dg_finite(SC[s]));
+            }
+            dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+            dt = rc[4 * N];
+            ttot = rc[4 * N + 1];
+            siter = (int)rc[4 * N + 2];
+            nsweeps = (int)rc[4 * N + 3];
+            nfail = (int)rc[4 * N + 4];
+            if (!(ttot < dtf)) return false;
+            substep_begin();
+            return true;
+        }
         double y[N], at[N];
         for (int s = 0; s < N; s++) {
             const long long off = cell * io.cs + s * io.ss;
@@ -162,9 +203,25 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         if (io.sweeps) io.sweeps[cell] = nsweeps;
         if (io.failures) io.failures[cell] = nfail;
     };
+    auto suspend = [&]() {
+        double *rc = cfg.rec + cell * rec_len<N>();
+        for (int s = 0; s < N; s++) {
+            rc[s] = Y[s];
+            rc[N + s] = PREV[s];
+            rc[2 * N + s] = SC[s];
+            rc[3 * N + s] = AT[s];
+        }
+        rc[4 * N] = dt;
+        rc[4 * N + 1] = ttot;
+        rc[4 * N + 2] = siter;
+        rc[4 * N + 3] = nsweeps;
+        rc[4 * N + 4] = nfail;
+        io.status[cell] = ST_SUSPENDED;
+    };
     auto fetch = [&]() {
         while (qi < io.ncells) {
             cell = io.order ? (long long)io.order[qi] : qi;
+            if (cell < 0) break; /* end of a resume list */
             if (cell_begin()) {
                 active = true;
                 return;
@@ -526,10 +583,11 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                     if (dt / dtf < cfg.dt_ratio_floor) done = ST_DT_UNDERFLOW;
                 }
                 for (int i = 0; i < N; i++) Y[i] = y[i];
-                if (done < 0) {
+                if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
                     substep_begin();
                 } else {
-                    cell_end(done);
+                    if (done < 0) suspend();
+                    else cell_end(done);
                     qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
                     fetch();
                 }

@@ -214,6 +214,23 @@ static __global__ void order_scatter_kernel(const int *cost, long long n, int *o
         order[atomicAdd(&offsets[cost_bucket(cost[i])], 1)] = (int)i;
 }
 
+/* The resume list of a two-launch solve: list[0..count) = the suspended
+ * cells (any order), then -1 (the end marker the engines stop at). */
+static __global__ void resume_list_fill_kernel(int *list, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        list[i] = -1;
+}
+
+static __global__ void resume_list_kernel(const int *status, long long n, int *list,
+                                          unsigned int *count)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        if (status[i] == ST_SUSPENDED) list[atomicAdd(count, 1u)] = (int)i;
+}
+
 /* Scaled Jacobian store into a per-thread array (BE_chem_solve.C:301-318). */
 template <int N>
 struct ScaledLocalPut {

@@ -28,7 +28,8 @@ class SolverConfig(C.Structure):
     _fields_ = [("max_newton_sweeps", C.c_int), ("max_substeps", C.c_int),
                 ("dt_ratio_floor", C.c_double), ("floor_value", C.c_double),
                 ("precision", C.c_int), ("schedule", C.c_int),
-                ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int)]
+                ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int),
+                ("sweep_budget", C.c_int), ("tail_grid", C.c_int)]
 
 
 class CellBatch(C.Structure):
@@ -154,6 +155,7 @@ class Solver:
         cfg.dt_ratio_floor, cfg.floor_value = 1e-15, 1e-25
         cfg.precision, cfg.schedule, cfg.block, cfg.grid = DENGO_FP64, SCHED_AUTO, 0, 0
         cfg.warps_per_cell = 1
+        cfg.sweep_budget, cfg.tail_grid = 0, 0
         return cfg
 
     # ---- reference-shaped host entry points ----------------------------

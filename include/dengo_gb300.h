@@ -93,6 +93,15 @@ typedef struct dengo_solver_config {
     int grid;                  /* blocks, 0 = tuned default             */
     int warps_per_cell;        /* warps sharing each cell's sweep: 1, 2 or
                                   4 (32 cells per group of warps); 0 = tuned */
+    int sweep_budget;          /* > 0: redistribute stiff cells -- a cell
+                                  that has taken this many Newton sweeps is
+                                  set aside at its next substep boundary and
+                                  finished in a second launch that packs
+                                  the set-aside cells densely; results are
+                                  unchanged.  0 = one launch */
+    int tail_grid;             /* blocks of that second launch, 0 = as
+                                  many as fit (the allocation-free entry
+                                  point always makes one launch) */
 } dengo_solver_config;
 
 void dengo_default_config(dengo_solver_config *cfg);

@@ -275,3 +275,40 @@ def test_temperature_from_mass_density(solver, golden):
     state, _ = primordial_cells(8, "config1", seed=2)
     T = solver.temperature_from_mass_density(state)
     assert np.all(T >= 1.0) and np.all(np.isfinite(T))
+
+
+@pytest.mark.parametrize("wpc,precision", [(4, 0), (1, 0), (4, 1)])
+def test_sweep_budget_redistribution_is_bit_identical(solver, golden, wpc, precision):
+    """Two-launch solve (stiff cells set aside at a sweep budget and resumed
+    packed in a second launch) gives the one-launch results bit for bit:
+    state, atol, dt, ttot, status and counters, with and without a cost-hint
+    order, including the edge cases."""
+    import torch
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(300, "config3", seed=78)
+    state = np.concatenate([state, golden["evolve_edge_in"]])
+    dtf = np.concatenate([dtf, golden["evolve_edge_dtf"]])
+    dt0 = np.concatenate([np.full(300, -1.0), golden["evolve_edge_dt0"]])
+    n = len(dtf)
+    hint = torch.tensor(np.random.default_rng(1).integers(0, 10**5, n).astype(np.int32),
+                        device="cuda")
+    outs = []
+    for budget, use_hint in ((0, False), (7, False), (150, True), (4000, False)):
+        st = torch.tensor(state.T.copy(), device="cuda")
+        at = st * 1e-6
+        cnt = [torch.zeros(n, dtype=torch.int32, device="cuda") for _ in range(4)]
+        dt = torch.tensor(dt0, device="cuda")
+        ttot = torch.zeros(n, dtype=torch.float64, device="cuda")
+        cfg = Solver.default_config()
+        cfg.precision, cfg.warps_per_cell, cfg.sweep_budget = precision, wpc, budget
+        solver.solve_device(st, n, 1, n, at, dtf=torch.tensor(dtf, device="cuda"), dt=dt, ttot=ttot,
+                            status=cnt[0], substeps=cnt[1], sweeps=cnt[2], failures=cnt[3],
+                            config=cfg, stream=torch.cuda.current_stream(),
+                            cost_hint=hint if use_hint else None)
+        torch.cuda.synchronize()
+        outs.append([x.cpu().numpy() for x in [st, at, dt, ttot] + cnt])
+    assert set(np.unique(outs[0][4])) <= {0, 1, 2}
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
