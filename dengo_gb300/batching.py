@@ -18,8 +18,10 @@ the fastest; the measured table is kept in a JSON cache keyed by network,
 precision, GPU and sample, so a process tunes once per workload.
 
 ``StepGraph`` captures one hydro step -- atol = 1e-6 x state, then the
-solve with the previous step's sweep counts as cost hint -- into a CUDA
-graph over fixed device buffers, and replays it for every later step.
+solve with the previous step's sweep counts as cost hint (with a sweep
+budget: both launches of the stiff-cell redistribution and the list built
+between them) -- into a CUDA graph over fixed device buffers, and replays it
+for every later step.
 """
 
 import hashlib
@@ -214,12 +216,14 @@ class StepGraph:
             self.graph.replay()
 
 
-def compare(network="primordial", config="config3", cells=16384, steps=3, precision=0, seed=None):
+def compare(network="primordial", config="config3", cells=16384, steps=3, precision=0, seed=None,
+            sweep_budget=2000):
     """Config-3 comparison: the plain one-cell-per-thread launch (block 64,
     no refill, no ordering, eager launches) against the persistent work queue
-    with the autotuned variant, longest-first order and graph-captured steps,
-    on the same seeded cells and the same number of hydro steps.  Returns a
-    dict with both arms' device times and converged cells/s."""
+    with the autotuned variant, stiff-cell redistribution after
+    ``sweep_budget`` sweeps and graph-captured steps, on the same seeded
+    cells and the same number of hydro steps.  Returns a dict with both arms'
+    device times and converged cells/s."""
     import torch
     from .workloads import primordial_cells
     solver = Solver(network)
@@ -250,6 +254,8 @@ def compare(network="primordial", config="config3", cells=16384, steps=3, precis
     out["autotuned"] = best
     out["autotune_table"] = table
     cfg = make_config(best, precision)
+    cfg.sweep_budget = sweep_budget
+    out["sweep_budget"] = sweep_budget
     g = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg, order=best["order"])
     g.capture()
     run(g, "persistent_graph_autotuned")
@@ -267,5 +273,7 @@ if __name__ == "__main__":
     p.add_argument("--cells", type=int, default=16384)
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--precision", type=int, default=0)
+    p.add_argument("--sweep-budget", type=int, default=2000)
     a = p.parse_args()
-    print(json.dumps(compare(a.network, a.config, a.cells, a.steps, a.precision)))
+    print(json.dumps(compare(a.network, a.config, a.cells, a.steps, a.precision,
+                             sweep_budget=a.sweep_budget)))

@@ -117,7 +117,8 @@ class ServingLoop:
     hbm_budget      bytes of request state the loop may hold on the device
     max_group_cells cells per launch group
     config          dengo_solver_config for every launch (default: the
-                    split engine, 4 warps per cell, FP64)"""
+                    split engine, 4 warps per cell, FP64, stiff cells
+                    redistributed after 2000 sweeps)"""
 
     def __init__(self, networks=("primordial", "oxygen"), slots=4, hbm_budget=40 << 30,
                  max_group_cells=1 << 20, config=None, device=0):
@@ -127,6 +128,7 @@ class ServingLoop:
         if config is None:
             config = Solver.default_config()
             config.warps_per_cell = 4
+            config.sweep_budget = 2000
         self.slots = [_Slot(torch, self.device, networks, config) for _ in range(slots)]
         self.networks = tuple(networks)
         self.budget = int(hbm_budget)
@@ -334,7 +336,7 @@ def serve_benchmark(rate=50.0, duration=10.0, slots=4, budget_gb=40.0, edge_rang
     """The serving workload under Poisson arrivals, then the same requests
     submitted at once (batch throughput); returns both summaries."""
     cfg = Solver.default_config()
-    cfg.warps_per_cell, cfg.precision = 4, precision
+    cfg.warps_per_cell, cfg.precision, cfg.sweep_budget = 4, precision, 2000
     reqs = poisson_requests(rate, duration, edge_range, dt_range=dt_range, seed=seed,
                             max_edge=max_edge)
     loop = ServingLoop(slots=slots, hbm_budget=int(budget_gb * (1 << 30)), config=cfg)

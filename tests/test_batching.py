@@ -53,3 +53,27 @@ def test_autotune_picks_a_measured_candidate(solver, tmp_path, monkeypatch):
     assert len({r["sweeps"] for r in table}) == 1
     again, _ = autotune(solver, state, dtf, sample=512, max_substeps=300, repeats=1, cands=cands)
     assert again == best and (tmp_path / "tune.json").exists()
+
+
+@pytest.mark.gpu
+def test_graph_replay_with_sweep_budget_equals_eager_steps(solver):
+    """The two-launch solve (stiff-cell redistribution) captured in a graph
+    gives the eager steps' bits."""
+    import torch
+    from dengo_gb300.batching import StepGraph
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(2000, "config3", seed=18)
+    cfg = Solver.default_config()
+    cfg.warps_per_cell, cfg.sweep_budget, cfg.max_substeps = 4, 30, 2000
+    dev = torch.device("cuda")
+    d_dtf = torch.tensor(dtf, device=dev)
+    eager = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg)
+    graph = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg).capture()
+    for _ in range(2):
+        eager.eager()
+        graph.replay()
+    torch.cuda.synchronize()
+    a, b = eager.state.cpu().numpy(), graph.state.cpu().numpy()
+    assert np.array_equal(a.view(np.int64), b.view(np.int64))
+    assert torch.equal(eager.status, graph.status) and torch.equal(eager.sweeps, graph.sweeps)
