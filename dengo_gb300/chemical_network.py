@@ -254,9 +254,12 @@ class ChemicalNetwork:
 
         Writes ``<name>_solver.cu`` (device functions + kernels + the C
         entry points), ``<name>_solver.h`` (drop-in C header),
-        ``<name>_solver_run.py`` (ctypes driver mirroring the reference's
-        ``run_<name>``), ``<name>_tables.dgt`` (rate/cooling tables) and,
-        when ``init_values`` is given, ``<name>_initial_conditions.dgt``.
+        ``<name>_solver_main.cu`` (stand-alone driver), ``<name>_solver_run.py``
+        (``run_<name>`` / ``main_run_<name>`` of the reference's Cython module,
+        over ctypes), ``<name>_solver_main.py``, ``<name>_tables.dgt``
+        (rate/cooling tables) and, when ``init_values`` is given,
+        ``<name>_initial_conditions.dgt`` -- the reference's file set with the
+        Cython and HDF5 pieces replaced.
         ``solver_template`` selects a template family by name, as in the
         reference (chemical_network.py:285-293); the reference's name maps
         to this package's CUDA family.  ``ode_solver_source`` is accepted for

@@ -22,7 +22,10 @@ TEMPLATE_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__fi
 
 FAMILIES = {
     "rates_and_rate_tables": ((".cu", "rates_and_rate_tables.cu.j2"),
-                              (".h", "rates_and_rate_tables.h.j2")),
+                              (".h", "rates_and_rate_tables.h.j2"),
+                              ("_main.cu", "rates_and_rate_tables_main.cu.j2"),
+                              ("_run.py", "rates_and_rate_tables_run.py.j2"),
+                              ("_main.py", "rates_and_rate_tables_main.py.j2")),
 }
 FAMILIES["cuda_be"] = FAMILIES["rates_and_rate_tables"]
 

@@ -71,6 +71,7 @@ class NetworkSpec:
     # operation count (longest-first greedy).
     rhs_part: dict = field(default_factory=dict)      # {NP: [part per row]}
     jac_part: dict = field(default_factory=dict)      # {NP: [var][eq] part}
+    stop_time: str = "3.1557e13"   # literal: the network's stop_time (the main driver's dtf)
 
     @property
     def N(self):
@@ -178,6 +179,7 @@ def network_spec(net, name):
         z_bounds=(_lit(net.z_bounds[0]), _lit(net.z_bounds[1])),
         nz=(len(z) if z is not None else 0),
         input_is_number=bool(getattr(net, "input_is_number", False)),
+        stop_time=repr(float(net.stop_time)),
         mass_density_ref=ccode_ref(md), mass_density_dev=ccode_device(md),
         T_ref=ccode_ref(T), T_dev=ccode_device(T),
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),

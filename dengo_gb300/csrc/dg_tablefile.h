@@ -1,5 +1,5 @@
 /*
- * Reader for the .dgt table bundle written by dengo_gb300/tablefile.py
+ * Reader and writer of the .dgt table bundle (dengo_gb300/tablefile.py)
  * (magic "DGTBL001", uint32 count, then per dataset: uint32 name length,
  * name, uint64 element count, float64 values; little-endian).  It replaces
  * the HDF5 reads of the reference (rates_and_rate_tables.C.template:278-304).
@@ -13,6 +13,7 @@
 
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace dg {
@@ -42,6 +43,29 @@ inline bool read_table_file(const char *path, std::map<std::string, std::vector<
     }
     fclose(f);
     if (!ok) err = std::string("malformed table bundle ") + path;
+    return ok;
+}
+
+/* Writes the named arrays as a .dgt bundle (the layout above). */
+inline bool write_table_file(const char *path,
+                             const std::vector<std::pair<std::string, std::vector<double>>> &sets,
+                             std::string &err)
+{
+    FILE *f = fopen(path, "wb");
+    if (!f) {
+        err = std::string("cannot create ") + path;
+        return false;
+    }
+    const uint32_t count = (uint32_t)sets.size();
+    bool ok = fwrite("DGTBL001", 1, 8, f) == 8 && fwrite(&count, 4, 1, f) == 1;
+    for (size_t i = 0; ok && i < sets.size(); i++) {
+        const uint32_t ln = (uint32_t)sets[i].first.size();
+        const uint64_t n = sets[i].second.size();
+        ok = fwrite(&ln, 4, 1, f) == 1 && fwrite(sets[i].first.data(), 1, ln, f) == ln &&
+             fwrite(&n, 8, 1, f) == 1 && fwrite(sets[i].second.data(), 8, n, f) == n;
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) err = std::string("cannot write ") + path;
     return ok;
 }
 

@@ -1699,6 +1699,68 @@ long long oxygen_data_field_offset(const char *field)
 
 const char *oxygen_species_name(int i) { return dgnet_oxygen::Net::species_name(i); }
 
+/* oxygen_main (rates_and_rate_tables.C.template:56-145): reads
+ * oxygen_initial_conditions.dgt (one array per species, the solver's
+ * input units), evolves every cell for the network's stop_time with
+ * rtol = 1e-9, atol = 1e-9 x input, and writes oxygen_solution.dgt: the
+ * species, T (temperature_from_mass_density of the result), time (ttot) and
+ * timestep (dt).  The files are in the current directory, or in argv[1]. */
+int oxygen_main(int argc, char **argv)
+{
+    const std::string dir = (argc > 1 && argv && argv[1]) ? std::string(argv[1]) + "/" : std::string();
+    std::map<std::string, std::vector<double>> ic;
+    std::string err;
+    if (!dg::read_table_file((dir + "oxygen_initial_conditions.dgt").c_str(), ic, err)) {
+        dg::set_error("oxygen_main: %s", err.c_str());
+        return 1;
+    }
+    constexpr int N = dgnet_oxygen::Net::N;
+    const auto ge = ic.find(dgnet_oxygen::Net::species_name(dgnet_oxygen::Net::IGE));
+    if (ge == ic.end()) {
+        dg::set_error("oxygen_main: no %s in the initial conditions",
+                      dgnet_oxygen::Net::species_name(dgnet_oxygen::Net::IGE));
+        return 1;
+    }
+    const size_t dims = ge->second.size();
+    std::vector<double> input(dims * N), atol(dims * N), rtol(dims * N, 1e-09);
+    for (int i = 0; i < N; i++) {
+        const auto it = ic.find(dgnet_oxygen::Net::species_name(i));
+        if (it == ic.end() || it->second.size() != dims) {
+            dg::set_error("oxygen_main: initial condition for %s missing or of the wrong length",
+                          dgnet_oxygen::Net::species_name(i));
+            return 1;
+        }
+        for (size_t j = 0; j < dims; j++) {
+            input[j * N + i] = it->second[j];
+            atol[j * N + i] = it->second[j] * 1e-09;
+        }
+    }
+    oxygen_data *data = oxygen_setup_data(NULL, NULL);
+    if (!data) return 1;
+    const double dtf = 31557000000000.0;
+    double dt = -1.0;
+    const double z = -1.0;
+    const double ttot = dengo_evolve_oxygen(dtf, &dt, z, input.data(), rtol.data(), atol.data(),
+                                           (long long)dims, data);
+    std::vector<double> T(dims);
+    oxygen_temperature_from_mass_density(input.data(), (int)dims, N, T.data());
+    oxygen_free_data(data);
+    std::vector<std::pair<std::string, std::vector<double>>> out;
+    for (int i = 0; i < N; i++) {
+        std::vector<double> v(dims);
+        for (size_t j = 0; j < dims; j++) v[j] = input[j * N + i];
+        out.emplace_back(dgnet_oxygen::Net::species_name(i), std::move(v));
+    }
+    out.emplace_back("T", std::move(T));
+    out.emplace_back("time", std::vector<double>(1, ttot));
+    out.emplace_back("timestep", std::vector<double>(1, dt));
+    if (!dg::write_table_file((dir + "oxygen_solution.dgt").c_str(), out, err)) {
+        dg::set_error("oxygen_main: %s", err.c_str());
+        return 1;
+    }
+    return ttot < 0 ? 1 : 0;
+}
+
 /* the species' weight as the reference's templates print it (the Cython
  * driver divides its initial conditions by it) */
 double oxygen_species_weight(int i)

@@ -1,0 +1,19 @@
+/* THIS FILE HAS BEEN AUTO-GENERATED by dengo_gb300.  DO NOT EDIT.
+ *
+ * Stand-alone driver of network "oxygen" (the reference's
+ * rates_and_rate_tables_main.C.template): oxygen_initial_conditions.dgt
+ * -> oxygen_solution.dgt, in the current directory or in argv[1].
+ *
+ *   nvcc -o oxygen_main oxygen_solver_main.cu -I <package>/include -I . \
+ *        -L . -loxygen_solver -Xlinker -rpath -Xlinker .
+ */
+#include <stdio.h>
+
+#include "oxygen_solver.h"
+
+int main(int argc, char **argv)
+{
+    const int rc = oxygen_main(argc, argv);
+    if (rc != 0) fprintf(stderr, "oxygen_main: %s\n", oxygen_last_error());
+    return rc;
+}

@@ -1,0 +1,7 @@
+"""THIS FILE HAS BEEN AUTO-GENERATED by dengo_gb300.  DO NOT EDIT.
+
+Runs oxygen_uvb_main through the library (the reference's
+rates_and_rate_tables_main.py.template)."""
+import oxygen_uvb_solver_run
+
+oxygen_uvb_solver_run.main_run_oxygen_uvb()

@@ -87,6 +87,7 @@ def _declare(lib, n):
         "%s_data_field_offset" % n: (C.c_longlong, [C.c_char_p]),
         "%s_species_name" % n: (C.c_char_p, [C.c_int]),
         "%s_species_weight" % n: (C.c_double, [C.c_int]),
+        "%s_main" % n: (C.c_int, [C.c_int, C.c_void_p]),
         "%s_run_strip" % n: (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_double, P_D, P_D,
                                        P_D, C.c_int, P_D, P_D, P_D, P_D, C.c_void_p, P_D, P_D]),
         "%s_last_error" % n: (C.c_char_p, []),

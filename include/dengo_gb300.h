@@ -38,6 +38,10 @@
  *                           on one strip in lockstep: BE_chem_solve with its
  *                           own dt control, scale refresh, niter cap and
  *                           dt < 1e-30 tf stop, optional trajectories
+ *   <n>_main                the reference's stand-alone driver
+ *                           (rates_and_rate_tables.C.template:56-145) with
+ *                           <n>_initial_conditions.dgt / <n>_solution.dgt in
+ *                           place of its HDF5 files
  *   <n>_ntables, <n>_table_name, <n>_table_length, <n>_data_field_offset,
  *   <n>_nspecies, <n>_species_name, <n>_species_weight, <n>_last_error
  *                           introspection for bindings
@@ -183,6 +187,7 @@ typedef int (*jac_f)(double *, double *, int, int, void *);
                       double *ttot, double *dt, double *traj, double *traj_T,  \
                       unsigned char *traj_ok, double *traj_t,                  \
                       double *traj_dt);                                        \
+    int n##_main(int argc, char **argv);                                       \
     int n##_ntables(void);                                                     \
     const char *n##_table_name(int k);                                         \
     int n##_table_length(int k);                                               \

@@ -106,4 +106,38 @@ def test_write_solver_writes_all_outputs(net, tmp_path):
     paths = net.write_solver("demo", output_dir=str(tmp_path), init_values=init)
     names = sorted(os.path.basename(p) for p in paths)
     assert names == ["demo_initial_conditions.dgt", "demo_solver.cu", "demo_solver.h",
+                     "demo_solver_main.cu", "demo_solver_main.py", "demo_solver_run.py",
                      "demo_tables.dgt"]
+    run = open(os.path.join(str(tmp_path), "demo_solver_run.py")).read()
+    assert "def run_demo(" in run and "def main_run_demo(" in run
+    assert "demo_main(argc, argv)" in open(os.path.join(str(tmp_path), "demo_solver_main.cu")).read()
+
+
+WRITER_CHECK = "\n".join([
+    '#include "dg_tablefile.h"',
+    "int main(int, char **argv) {",
+    "    std::vector<std::pair<std::string, std::vector<double>>> s;",
+    '    s.emplace_back("H_1", std::vector<double>{1.5, -2.25e-300, 3.0});',
+    '    s.emplace_back("time", std::vector<double>(1, 4.5e13));',
+    "    std::string err;",
+    "    std::map<std::string, std::vector<double>> back;",
+    "    if (!dg::write_table_file(argv[1], s, err)) return 1;",
+    "    if (!dg::read_table_file(argv[1], back, err)) return 2;",
+    '    return back["H_1"][1] == -2.25e-300 && back["time"][0] == 4.5e13 ? 0 : 3;',
+    "}", ""])
+
+
+def test_table_file_c_writer_round_trip(tmp_path):
+    """The C++ .dgt writer (csrc/dg_tablefile.h, used by <n>_main for the
+    solution file) produces what the Python reader reads."""
+    import subprocess
+    from dengo_gb300.tablefile import read_table_file
+    src = tmp_path / "w.cpp"
+    src.write_text(WRITER_CHECK)
+    exe = tmp_path / "w"
+    subprocess.check_call(["g++", "-std=c++17", "-I", os.path.join(ROOT, "dengo_gb300", "csrc"),
+                           str(src), "-o", str(exe)])
+    out = tmp_path / "sol.dgt"
+    assert subprocess.call([str(exe), str(out)]) == 0
+    d = read_table_file(str(out))
+    assert list(d) == ["H_1", "time"] and d["H_1"][1] == -2.25e-300 and d["time"][0] == 4.5e13

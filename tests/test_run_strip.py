@@ -50,3 +50,44 @@ def test_gpu_run_strip_matches_oracle(solver, oracle, tables_in_order, tf, niter
     assert not rv_t["successful"][it:].any() and not rv_t["H_1"][:, it:].any()
     assert np.all(rv_t["T"][:, :it] > 0)
     assert np.all(np.diff(rv_t["t"][:it]) >= 0) and rv_t["dt"][0] == tf / 1e5
+
+
+@pytest.mark.gpu
+def test_generated_run_module(solver):
+    """<n>_solver_run.py (generated beside the library) exposes run_<n> with
+    the Cython module's signature."""
+    import importlib.util
+    import os
+    from dengo_gb300.build import network_dir
+    path = os.path.join(network_dir("primordial"), "primordial_solver_run.py")
+    spec = importlib.util.spec_from_file_location("primordial_solver_run", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    ics = _ics(8, 44)
+    rv, rv_t = mod.run_primordial(ics, 1e8, niter=500, intermediate=1)
+    rv2, _ = solver.run(ics, 1e8, niter=500, intermediate=0)
+    for s in PRIMORDIAL_ORDER:
+        assert np.array_equal(rv[s].view(np.int64), rv2[s].view(np.int64)), s
+    assert rv_t["H_1"].shape == (8, 500)
+
+
+@pytest.mark.gpu
+def test_main_driver_matches_evolve(solver, tmp_path):
+    """primordial_main: initial-conditions file -> solution file, as the
+    reference's stand-alone driver (stop_time, rtol = 1e-9, atol = 1e-9 x
+    input); equal to dengo_evolve_primordial with the same arguments."""
+    import ctypes as C
+    from dengo_gb300.tablefile import read_table_file, write_table_file
+    state, _ = primordial_cells(12, "cold", seed=61)
+    write_table_file(str(tmp_path / "primordial_initial_conditions.dgt"),
+                     {s: state[:, j] for j, s in enumerate(solver.species)})
+    argv = (C.c_char_p * 2)(b"primordial_main", str(tmp_path).encode())
+    rc = solver.lib.primordial_main(2, C.cast(argv, C.c_void_p))
+    assert rc == 0, solver.last_error()
+    sol = read_table_file(str(tmp_path / "primordial_solution.dgt"))
+    ref, _, ttot, dt = solver.evolve(state, 3.1557e13, rtol=np.full_like(state, 1e-9),
+                                     atol=state * 1e-9)
+    for j, s in enumerate(solver.species):
+        assert np.array_equal(sol[s].view(np.int64), ref[:, j].view(np.int64)), s
+    assert sol["time"][0] == ttot and sol["timestep"][0] == dt
+    assert np.array_equal(sol["T"], solver.temperature_from_mass_density(ref))
