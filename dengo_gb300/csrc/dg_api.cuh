@@ -507,8 +507,9 @@ struct Api {
      * SM per 32 set-aside cells (the surplus CTAs exit at once), the cells
      * spread over those CTAs: a few stiff cells then share warps -- free on
      * the FP64 pipe -- instead of competing CTAs sharing each SM's FP64
-     * units.  Every cell's operations are those of one launch, so the
-     * results are bit-identical to it. */
+     * units; launch 3 does the same for the cells launch 2 set aside at 16
+     * times the budget.  Every cell's operations are those of one launch,
+     * so the results are bit-identical to it. */
     static int solve_two_launch(Gpu *g, CellIO io, KernelCfg kc, dengo_solver_config cfg,
                                 cudaStream_t st)
     {
@@ -536,23 +537,33 @@ struct Api {
         k1.sweep_budget = cfg.sweep_budget;
         k1.rec = g->rec;
         if (int e = launch_engine<Net>(g, io1, k1, cfg, st, g->queue)) return e;
-        DG_CUDA(cudaMemsetAsync(g->resume_count, 0, sizeof(unsigned int), st));
+        /* Resume launches: the set-aside cells run with a budget 16 times
+         * larger, and the few that still run past it are set aside once more
+         * and finished by a last launch, where they are few enough to spread
+         * one CTA per SM. */
+        const int budgets[2] = {cfg.sweep_budget * 16 > cfg.sweep_budget ? cfg.sweep_budget * 16 : 0, 0};
         const int lg = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-        resume_list_fill_kernel<<<lg, 256, 0, st>>>(g->resume_list, n);
-        resume_list_kernel<<<lg, 256, 0, st>>>(io1.status, n, g->resume_list, g->resume_count);
-        DG_CUDA(cudaGetLastError());
-        CellIO io2 = io;
-        io2.order = g->resume_list;
-        KernelCfg k2 = kc;
-        k2.resume = 1;
-        k2.rec = g->rec;
-        k2.resume_count = g->resume_count;
-        k2.nsm = g->nsm;
-        dengo_solver_config c2 = cfg;
-        if (c2.schedule == DENGO_SCHED_PER_THREAD) c2.schedule = DENGO_SCHED_QUEUE;
-        c2.grid = cfg.tail_grid;   /* 0: the persistent default; CTAs whose
-                                      first 32 entries are past the list exit */
-        return launch_engine<Net>(g, io2, k2, c2, st, g->queue);
+        for (int r = 0; r < 2; r++) {
+            DG_CUDA(cudaMemsetAsync(g->resume_count, 0, sizeof(unsigned int), st));
+            resume_list_fill_kernel<<<lg, 256, 0, st>>>(g->resume_list, n);
+            resume_list_kernel<<<lg, 256, 0, st>>>(io1.status, n, g->resume_list, g->resume_count);
+            DG_CUDA(cudaGetLastError());
+            CellIO io2 = io;
+            io2.order = g->resume_list;
+            if (r == 0) io2.status = io1.status;   /* the last launch writes the caller's */
+            KernelCfg k2 = kc;
+            k2.resume = 1;
+            k2.rec = g->rec;
+            k2.resume_count = g->resume_count;
+            k2.nsm = g->nsm;
+            k2.sweep_budget = budgets[r];
+            dengo_solver_config c2 = cfg;
+            if (c2.schedule == DENGO_SCHED_PER_THREAD) c2.schedule = DENGO_SCHED_QUEUE;
+            c2.grid = cfg.tail_grid;   /* 0: the persistent default; CTAs past the
+                                          rounds the list needs exit */
+            if (int e = launch_engine<Net>(g, io2, k2, c2, st, g->queue)) return e;
+        }
+        return 0;
     }
 
     /* ---------------- allocation-free variant ----------------

@@ -100,12 +100,14 @@ typedef struct dengo_solver_config {
     int sweep_budget;          /* > 0: redistribute stiff cells -- a cell
                                   that has taken this many Newton sweeps is
                                   set aside at its next substep boundary and
-                                  finished in a second launch that packs
-                                  the set-aside cells densely; results are
+                                  resumed by a later launch that spreads the
+                                  set-aside cells over the SMs (again at 16x
+                                  the budget, then finished); results are
                                   unchanged.  0 = one launch */
-    int tail_grid;             /* blocks of that second launch, 0 = as
-                                  many as fit (the allocation-free entry
-                                  point always makes one launch) */
+    int tail_grid;             /* blocks of the resume launches, 0 = as
+                                  many as the set-aside cells need (the
+                                  allocation-free entry point always makes
+                                  one launch) */
 } dengo_solver_config;
 
 void dengo_default_config(dengo_solver_config *cfg);
