@@ -69,7 +69,7 @@ struct Gpu {
     int *order = nullptr;         /* cell order built from a cost hint */
     long long order_cap = 0;
     int *order_counts = nullptr;  /* [64]: bucket counts and offsets */
-    /* two-launch solve (sweep budget): suspension records, the resume list
+    /* redistributed solve (sweep budget): suspension records, the resume list
      * and its length, a status array when the caller passes none */
     double *rec = nullptr;
     long long rec_cap = 0;        /* cells */
@@ -497,7 +497,7 @@ struct Api {
         g->ts.z = z;
         if (cfg.sweep_budget <= 0 || b->ncells <= 0)
             return launch_engine<Net>(g, io, kc, cfg, st, g->queue);
-        return solve_two_launch(g, io, kc, cfg, st);
+        return solve_redistributed(g, io, kc, cfg, st);
     }
 
     /* Stiff-cell redistribution.  Launch 1 solves every cell but sets aside
@@ -510,8 +510,8 @@ struct Api {
      * units; launch 3 does the same for the cells launch 2 set aside at 16
      * times the budget.  Every cell's operations are those of one launch,
      * so the results are bit-identical to it. */
-    static int solve_two_launch(Gpu *g, CellIO io, KernelCfg kc, dengo_solver_config cfg,
-                                cudaStream_t st)
+    static int solve_redistributed(Gpu *g, CellIO io, KernelCfg kc, dengo_solver_config cfg,
+                                   cudaStream_t st)
     {
         const long long n = io.ncells;
         if (n > g->rec_cap) {
@@ -541,7 +541,7 @@ struct Api {
          * larger, and the few that still run past it are set aside once more
          * and finished by a last launch, where they are few enough to spread
          * one CTA per SM. */
-        const int budgets[2] = {cfg.sweep_budget * 16 > cfg.sweep_budget ? cfg.sweep_budget * 16 : 0, 0};
+        const int budgets[2] = {cfg.sweep_budget < (1 << 26) ? cfg.sweep_budget * 16 : 0, 0};
         const int lg = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
         for (int r = 0; r < 2; r++) {
             DG_CUDA(cudaMemsetAsync(g->resume_count, 0, sizeof(unsigned int), st));

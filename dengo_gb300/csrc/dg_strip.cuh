@@ -214,7 +214,7 @@ static __global__ void order_scatter_kernel(const int *cost, long long n, int *o
         order[atomicAdd(&offsets[cost_bucket(cost[i])], 1)] = (int)i;
 }
 
-/* The resume list of a two-launch solve: list[0..count) = the suspended
+/* The resume list of a redistributed solve (sweep budget): list[0..count) = the suspended
  * cells (any order), then -1 (the end marker the engines stop at). */
 static __global__ void resume_list_fill_kernel(int *list, long long n)
 {

@@ -57,7 +57,7 @@ def test_autotune_picks_a_measured_candidate(solver, tmp_path, monkeypatch):
 
 @pytest.mark.gpu
 def test_graph_replay_with_sweep_budget_equals_eager_steps(solver):
-    """The two-launch solve (stiff-cell redistribution) captured in a graph
+    """The redistributed solve (stiff-cell redistribution, three launches) captured in a graph
     gives the eager steps' bits."""
     import torch
     from dengo_gb300.batching import StepGraph

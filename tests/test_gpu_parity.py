@@ -279,8 +279,9 @@ def test_temperature_from_mass_density(solver, golden):
 
 @pytest.mark.parametrize("wpc,precision", [(4, 0), (1, 0), (4, 1)])
 def test_sweep_budget_redistribution_is_bit_identical(solver, golden, wpc, precision):
-    """Two-launch solve (stiff cells set aside at a sweep budget and resumed
-    packed in a second launch) gives the one-launch results bit for bit:
+    """Stiff-cell redistribution (cells set aside at a sweep budget, resumed
+    in a second launch, set aside again at 16 times the budget and finished
+    in a third) gives the one-launch results bit for bit:
     state, atol, dt, ttot, status and counters, with and without a cost-hint
     order, including the edge cases."""
     import torch
