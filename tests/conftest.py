@@ -45,3 +45,28 @@ def solver():
         build_network("primordial")
     from dengo_gb300.runtime import Solver
     return Solver("primordial")
+
+
+def write_report(name, data):
+    """Write ``data`` as JSON to ``$DENGO_REPORT_DIR/<name>.json`` when that
+    variable is set (measurement runs); tests do nothing otherwise."""
+    import json
+    out = os.environ.get("DENGO_REPORT_DIR")
+    if not out:
+        return
+    os.makedirs(out, exist_ok=True)
+    with open(os.path.join(out, name + ".json"), "w") as f:
+        json.dump(data, f, indent=1)
+
+
+def species_error_report(names, err, conv_cells, tol):
+    """Per species: max and median floored relative error over the converged
+    cells and the fraction of them within ``tol``."""
+    import numpy as np
+    rep = {"cells": int(conv_cells), "tol": tol, "species": {}}
+    for k, nm in enumerate(names):
+        e = err[:, k]
+        rep["species"][nm] = {"max": float(e.max(initial=0.0)),
+                              "median": float(np.median(e)) if len(e) else 0.0,
+                              "frac_within_tol": float(np.mean(e <= tol)) if len(e) else 1.0}
+    return rep

@@ -208,8 +208,33 @@ def test_mixed_precision_within_1e6_of_oracle(solver, oracle, config, seed, n, m
     assert np.all(out["status"][conv] == 0)
     err = floored_rel_err(out["state"][conv], ref["state"][conv], 1e-6 * np.abs(state[conv]))
     per_cell = err.max(axis=1)
+    from conftest import species_error_report, write_report
+    write_report("mixed_species_primordial_%s_w%d" % (config, wpc),
+                 species_error_report(solver.species, err, conv.sum(), MIXED_TOL))
     assert np.mean(per_cell <= MIXED_TOL) >= min_frac, np.sort(per_cell)[-5:]
     assert np.mean(out["sweeps"][conv] == ref["sweeps"][conv]) >= min_frac
+
+
+@pytest.mark.parametrize("wpc", [1, 4])
+def test_twenty_newton_sweeps_match_oracle(solver, oracle, wpc):
+    """``max_newton_sweeps = 20`` (the config-1 setting; the reference's
+    BE_chem_solve hard-codes 10, BE_chem_solve.C:87): the GPU and the oracle
+    with the same limit agree cell by cell, and the limit changes the result
+    (the failure counts differ from the 10-sweep run on these cells)."""
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(96, "config3", seed=2020)
+    cfg = Solver.default_config()
+    cfg.max_newton_sweeps, cfg.warps_per_cell = 20, wpc
+    out = solver.solve_host(state, dtf, rtol=1e-6, config=cfg, counters=True)
+    ref = oracle.evolve_cells(solver._tables, state, dtf, nthreads=0, max_sweeps=20)
+    ten = oracle.evolve_cells(solver._tables, state, dtf, nthreads=0, max_sweeps=10)
+    assert np.any(ref["failures"] != ten["failures"])
+    same = check_cells(out["state"], ref["state"], out["status"], ref["status"], "20 sweeps")
+    ok = ref["status"] == 0
+    for k in ("substeps", "sweeps", "failures"):
+        assert np.array_equal(out[k][ok], ref[k][ok]), k
+    assert same >= int(0.9 * ok.sum())
 
 
 def test_batch_invariance(solver):

@@ -146,4 +146,6 @@ def test_gpu_mixed_within_1e6():
     conv = ref["status"] == 0
     err = np.abs(out["state"][conv] - ref["state"][conv]) / np.maximum(
         np.abs(ref["state"][conv]), 1e-6 * np.abs(st[conv]))
+    from conftest import species_error_report, write_report
+    write_report("mixed_species_oxygen", species_error_report(s.species, err, conv.sum(), 1e-6))
     assert np.mean(err.max(axis=1) <= 1e-6) >= 0.8, np.sort(err.max(axis=1))[-10:]
