@@ -4,6 +4,10 @@
   (reactions k01-k19, k21-k23 of ``primordial_rates``; every cooling action
   of ``primordial_cooling`` except ``compton``), tables of 1024 log-spaced
   bins over 1-1e9 K.
+* ``primordial_compton``: the same with Compton cooling off the CMB
+  (``primordial_cooling.py``'s ``compton`` action: ``-comp (1+z)^4
+  (T - 2.73 (1+z)) de``), whose term reads the call's redshift and the
+  cell's temperature directly; 45 tables.
 * ``oxygen``: H, He and O ion-by-ion (16 equations); see :mod:`ion_by_ion`.
 * ``oxygen_uvb``: the same ions under a UV background: photoionisation and
   photoheating tabulated in redshift (100 bins over z in [0, 15]).
@@ -39,13 +43,15 @@ def primordial_network(T_bounds=(1.0, 1e9), n_bins=1024, with_compton=False):
     return net
 
 
-SHIPPED_NETWORKS = ("primordial", "oxygen", "oxygen_uvb")
+SHIPPED_NETWORKS = ("primordial", "primordial_compton", "oxygen", "oxygen_uvb")
 
 
 def build_network(name):
     """The network a shipped solver is generated from, by solver name."""
     if name == "primordial":
         return primordial_network()
+    if name == "primordial_compton":
+        return primordial_network(with_compton=True)
     if name == "oxygen":
         from .ion_by_ion import oxygen_network
         return oxygen_network()

@@ -16,9 +16,11 @@ Recipe (runs only where the reference checkout exists):
      it (chemical_network.py:314);
    * temporaries are parsed with the species and table symbols in scope, so
      ``galdl`` of ``gloverabel08`` refers to the species symbols
-     (reaction_classes.py:346-350).
+     (reaction_classes.py:346-350) and ``comp`` of ``compton`` to its table
+     rather than to ``sympy.comp`` (primordial_cooling.py:280-292).
 2. Build the primordial network (all reactions; all cooling actions except
-   ``compton``; 1024 bins over 1-1e9 K) and call the reference's
+   ``compton``, or all of them for ``primordial_compton``; 1024 bins over
+   1-1e9 K), or an ion-by-ion network, and call the reference's
    ``write_solver(..., ode_solver_source=None)`` into ``oracle/_ref/<name>/``:
    the rendered ``<name>_solver.C/.h`` and the tables.
 3. Compile the rendered solver together with the reference's
@@ -93,7 +95,7 @@ def _install_shims():
                         "docutils.utils.roman": dur})
 
 
-def _reference_primordial():
+def _reference_primordial(with_compton=False):
     sys.path.insert(0, REF_ROOT)
     _install_shims()
     import sympy
@@ -133,7 +135,7 @@ def _reference_primordial():
     import dengo.primordial_cooling  # noqa: F401
     net = cn.ChemicalNetwork()
     for c in sorted(rc.cooling_registry):
-        if c != "compton":
+        if c != "compton" or with_compton:
             net.add_cooling(c)
     for r in sorted(rc.reaction_registry):
         net.add_reaction(r)
@@ -275,17 +277,19 @@ void ref_evolve_cells(const double *dtf, double *dt, double z, double *input, do
 def build(name="primordial"):
     """Render and compile one network in a fresh interpreter (the reference's
     registries are module globals, so networks are built one per process)."""
-    if name not in ("primordial", "oxygen", "oxygen_uvb"):
-        raise ValueError("networks rendered with the reference here: primordial, oxygen, "
-                         "oxygen_uvb")
+    if name not in ("primordial", "primordial_compton", "oxygen", "oxygen_uvb"):
+        raise ValueError("networks rendered with the reference here: primordial, "
+                         "primordial_compton, oxygen, oxygen_uvb")
     if not os.path.isdir(os.path.join(REF_ROOT, "dengo")):
         raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
     if "dengo" in sys.modules:
         lib = os.path.join(OUT, "libref_%s.so" % name)
         subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
         return lib
-    net = (_reference_primordial() if name == "primordial" else
-           _reference_oxygen("HM12" if name == "oxygen_uvb" else None))
+    if name.startswith("primordial"):
+        net = _reference_primordial(with_compton=(name == "primordial_compton"))
+    else:
+        net = _reference_oxygen("HM12" if name == "oxygen_uvb" else None)
     odir = os.path.join(OUT, name)
     os.makedirs(odir, exist_ok=True)
     net.write_solver(name, output_dir=odir, ode_solver_source=None)

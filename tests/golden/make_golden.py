@@ -61,6 +61,18 @@ def edge_cells():
     return cells, dtfs, dts
 
 
+def compton_cells():
+    """Config-1 cells, and config-1 cells made diffuse (x 1e-4 in every
+    density) and hotter (ge x 10), where Compton cooling off the CMB is a
+    large share of the cooling at the higher redshifts."""
+    a, da = primordial_cells(32, "config1", seed=1971)
+    b, db = primordial_cells(32, "config1", seed=1972)
+    b = b.copy()
+    b[:, :9] *= 1e-4
+    b[:, 9] *= 10.0
+    return np.concatenate([a, b]), np.concatenate([da, db * 100.0])
+
+
 def main():
     import ref_build
     from oracle import Reference
@@ -159,11 +171,12 @@ if __name__ == "__main__" and len(sys.argv) == 1:
     main()
 
 
-def make_ion(name="oxygen", zs=(None,)):
+def make_ion(name="oxygen", zs=(None,), cells=None):
     """Golden vectors of an ion-by-ion network (16 equations): the
     reference's own setup_ionization and templates, with the synthetic
     CHIANTI and UV-background stand-in tables (oracle/ref_build.py).  For a
-    network with redshift tables, one set of outputs per redshift."""
+    network whose terms depend on the redshift, one set of outputs per
+    redshift.  ``cells``: (state, dtf), by default 48 seeded oxygen cells."""
     import hashlib
     import ref_build
     from oracle import Reference
@@ -173,7 +186,7 @@ def make_ion(name="oxygen", zs=(None,)):
     ref_build.build(name)
     ref = Reference(name)
     out = {}
-    st, dtf = oxygen_cells(48, seed=515)
+    st, dtf = cells if cells is not None else oxygen_cells(48, seed=515)
     out["evolve_in"], out["evolve_dtf"] = st, dtf
     for z in zs:
         r = ref.evolve_cells(st, dtf, nthreads=8, z=-1.0 if z is None else z)
@@ -198,3 +211,6 @@ if __name__ == "__main__" and len(sys.argv) > 1:
         make_ion("oxygen")
     elif sys.argv[1] == "oxygen_uvb":
         make_ion("oxygen_uvb", zs=(0.0, 2.5, 9.0, 20.0))
+    elif sys.argv[1] == "primordial_compton":
+        make_ion("primordial_compton", zs=(-1.0, 0.0, 3.0, 9.0, 19.0),
+                 cells=compton_cells())
