@@ -25,8 +25,8 @@ import hashlib
 import numpy as np
 
 from .periodic_table import periodic_table_by_name
-from .reaction_classes import (AtomicSpecies, CoolingAction, Reaction, registry_setup,
-                               species_registry)
+from .reaction_classes import (AtomicSpecies, chianti_rate, ion_cooling_rate,
+                               ion_photoheating_rate, ion_photoionization_rate, registry_setup)
 
 _EV_K = 1.1605e4  # K per eV
 
@@ -115,35 +115,21 @@ def photo_rate(element, ion_name, kind):
 
 
 def _register_ions(atom_name, photo_background=None, cooling=True):
-    """Register the ions of ``atom_name`` and their terms; returns the names
-    of everything registered: [species, cooling actions, reactions]."""
+    """Register the ions of ``atom_name`` and their terms, in the reference's
+    order (dengo/ion_by_ion.py:33-56); returns the names of everything
+    registered: [species, cooling actions, reactions]."""
     num = periodic_table_by_name[atom_name][0]
-    de = species_registry["de"]
     ions = {i: AtomicSpecies(atom_name, i) for i in range(num + 1)}
-    names = [set(), set(), set()]
+    names = [{s.name for s in ions.values()}, set(), set()]
     for i in range(num + 1):
         s = ions[i]
-        names[0].add(s.name)
-        sm1, sp1 = ions.get(i - 1), ions.get(i + 1)
-        if sp1 is not None:
-            names[2].add(Reaction("%s_i" % s.name, ionization_rate(atom_name, i),
-                                  [(1, s), (1, de)], [(1, sp1), (2, de)]).name)
-        if sm1 is not None:
-            names[2].add(Reaction("%s_r" % s.name, recombination_rate(atom_name, i),
-                                  [(1, s), (1, de)], [(1, sm1)]).name)
+        names[2].update(chianti_rate(atom_name, ions.get(i - 1), s, ions.get(i + 1)))
         if cooling:
-            act = CoolingAction("%s_c" % s.name, "-%s_c * %s * de" % (s.name, s.name))
-            act.tables["%s_c" % s.name] = cooling_rate(atom_name, i)
-            names[1].add(act.name)
-        if sp1 is not None and photo_background is not None:
-            ion = s.name.lower()
-            el = ion.split("_")[0]
-            names[2].add(Reaction("%s_pi" % s.name, photo_rate(el, ion, "photoionization"),
-                                  [(1, s)], [(1, sp1), (1, de)]).name)
+            names[1].update(ion_cooling_rate(s, atom_name))
+        if i != num and photo_background is not None:
+            names[2].update(ion_photoionization_rate(s, photo_background=photo_background))
             if cooling:
-                act = CoolingAction("%s_ph" % s.name, "%s_ph * %s" % (s.name, s.name))
-                act.tables["%s_ph" % s.name] = photo_rate(el, ion, "photoheating")
-                names[1].add(act.name)
+                names[1].update(ion_photoheating_rate(s, photo_background=photo_background))
     return names
 
 

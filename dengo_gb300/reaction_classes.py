@@ -320,3 +320,73 @@ class CoolingAction:
 
 
 cooling_action = CoolingAction.create_cooling_action
+
+
+# -- ion-by-ion registration helpers (reaction_classes.py:167-198, 200-271,
+# 379-441, 443-514 of the reference).  Each registers the same reactions and
+# cooling actions, under the same names and conditions, as the reference's
+# function of that name and returns the new names.  The reference tabulates
+# them from CHIANTI, Gnat & Ferland's cooling tables and the HM12 UV
+# background; those data are not available, so the tables come from the
+# seeded synthetic curves of :mod:`dengo_gb300.ion_by_ion`.
+
+def _ion_stage(species):
+    """(element, stage) of an AtomicSpecies named ``<El>_<stage + 1>``."""
+    ion_name = species.name.lower()
+    if "_" not in ion_name:
+        raise RuntimeError("Name must be in 'Ion Species' format: %s" % species.name)
+    element, state = ion_name.split("_")[:2]
+    return element, int(state) - 1
+
+
+def chianti_rate(atom_name, sm1, s, sp1):
+    """Collisional ionisation ``<s>_i`` (s + e -> sp1 + 2e, when ``sp1``
+    exists) and recombination ``<s>_r`` (s + e -> sm1, when ``sm1``
+    exists)."""
+    from .ion_by_ion import ionization_rate, recombination_rate
+    _, stage = _ion_stage(s)
+    de = species_registry["de"]
+    new_rates = []
+    if sp1 is not None:
+        Reaction("%s_i" % s.name, ionization_rate(atom_name, stage),
+                 [(1, s), (1, de)], [(1, sp1), (2, de)])
+        new_rates.append("%s_i" % s.name)
+    if sm1 is not None:
+        Reaction("%s_r" % s.name, recombination_rate(atom_name, stage),
+                 [(1, s), (1, de)], [(1, sm1)])
+        new_rates.append("%s_r" % s.name)
+    return new_rates
+
+
+def ion_cooling_rate(species, atom_name):
+    """Cooling action ``<s>_c``: ``-<s>_c * <s> * de`` with one table."""
+    from .ion_by_ion import cooling_rate
+    _, stage = _ion_stage(species)
+    act = CoolingAction("%s_c" % species.name, "-%s_c * %s * de" % (species.name, species.name))
+    act.tables["%s_c" % species.name] = cooling_rate(atom_name, stage)
+    return ["%s_c" % species.name]
+
+
+def ion_photoionization_rate(species, photo_background="HM12"):
+    """Photoionisation ``<s>_pi`` (s -> next ion + e), tabulated in
+    redshift, when the next ion is registered."""
+    from .ion_by_ion import photo_rate
+    element, stage = _ion_stage(species)
+    nxt = "%s_%s" % (element.capitalize(), stage + 2)
+    if nxt not in species_registry:
+        return []
+    Reaction("%s_pi" % species.name, photo_rate(element, species.name.lower(), "photoionization"),
+             [(1, species)], [(1, species_registry[nxt]), (1, species_registry["de"])])
+    return ["%s_pi" % species.name]
+
+
+def ion_photoheating_rate(species, photo_background="HM12"):
+    """Photoheating cooling action ``<s>_ph``: ``<s>_ph * <s>``, tabulated in
+    redshift."""
+    from .ion_by_ion import photo_rate
+    element, _ = _ion_stage(species)
+    if species.name not in species_registry:
+        return []
+    act = CoolingAction("%s_ph" % species.name, "%s_ph * %s" % (species.name, species.name))
+    act.tables["%s_ph" % species.name] = photo_rate(element, species.name.lower(), "photoheating")
+    return ["%s_ph" % species.name]

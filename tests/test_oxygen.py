@@ -149,3 +149,23 @@ def test_gpu_mixed_within_1e6():
     from conftest import species_error_report, write_report
     write_report("mixed_species_oxygen", species_error_report(s.species, err, conv.sum(), 1e-6))
     assert np.mean(err.max(axis=1) <= 1e-6) >= 0.8, np.sort(err.max(axis=1))[-10:]
+
+
+def test_ion_helpers_register_the_references_names():
+    """The reference's ion-by-ion helpers (reaction_classes.py:167-198,
+    200-271, 379-441, 443-514) exist under the same names and register the
+    same terms: the shipped ion networks are built through them."""
+    from dengo_gb300 import reaction_classes as rc
+    from dengo_gb300.ion_by_ion import oxygen_uvb_network
+    oxygen_uvb_network()
+    o1, o2, o9 = (rc.species_registry[n] for n in ("O_1", "O_2", "O_9"))
+    assert rc.chianti_rate("O", None, o1, o2) == ["O_1_i"]
+    assert rc.chianti_rate("O", rc.species_registry["O_8"], o9, None) == ["O_9_r"]
+    assert rc.ion_cooling_rate(o2, "O") == ["O_2_c"]
+    assert rc.ion_photoionization_rate(o1) == ["O_1_pi"]
+    assert rc.ion_photoionization_rate(o9) == []
+    assert rc.ion_photoheating_rate(o1) == ["O_1_ph"]
+    r = rc.reaction_registry["O_1_pi"]
+    assert [s.name for _, s in r.left_side] == ["O_1"]
+    assert sorted(s.name for _, s in r.right_side) == ["O_2", "de"]
+    assert rc.cooling_registry["O_1_ph"]._equation == "O_1_ph * O_1"
