@@ -18,8 +18,8 @@ import sympy
 from .chemistry_constants import tevk, tiny, mh  # noqa: F401  (re-exported)
 from .codegen.printers import ccode_ref
 from .reaction_classes import (ChemicalSpecies, Species, cooling_registry,  # noqa: F401
-                               count_m, index_i, reaction_registry,
-                               species_registry)
+                               count_m, ensure_cooling, ensure_reaction, index_i,
+                               reaction_registry, species_registry)
 
 ge = Species("ge", 1.0, "Gas Energy")
 de = ChemicalSpecies("de", 1.0, pretty_name="Electrons")
@@ -59,7 +59,7 @@ class ChemicalNetwork:
         self.required_species.add(species_registry.get(species, species))
 
     def add_reaction(self, reaction, auto_add=True):
-        reaction = reaction_registry.get(reaction, reaction)
+        reaction = ensure_reaction(reaction)
         if reaction.name in self.reactions:
             raise RuntimeError("reaction %s already in network" % reaction.name)
         for _, s in reaction.left_side + reaction.right_side:
@@ -72,7 +72,7 @@ class ChemicalNetwork:
         reaction.coeff_sym.energy = self.energy_term
 
     def add_cooling(self, cooling_term, auto_add=True):
-        cooling_term = cooling_registry.get(cooling_term, cooling_term)
+        cooling_term = ensure_cooling(cooling_term)
         if cooling_term.name in self.cooling_actions:
             raise RuntimeError("cooling %s already in network" % cooling_term.name)
         if auto_add:

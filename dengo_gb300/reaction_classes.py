@@ -35,6 +35,7 @@ import numpy as np
 import sympy
 
 from .periodic_table import periodic_table_by_name
+from .exceptions import UnknownCoolingAction, UnknownReaction, UnknownSpecies
 
 species_registry = {}
 reaction_registry = {}
@@ -61,15 +62,27 @@ def registry_setup(func):
 
 
 def ensure_reaction(r):
-    return r if isinstance(r, Reaction) else reaction_registry[r]
+    if isinstance(r, Reaction):
+        return r
+    if r not in reaction_registry:
+        raise UnknownReaction(r)
+    return reaction_registry[r]
 
 
 def ensure_cooling(c):
-    return c if isinstance(c, CoolingAction) else cooling_registry[c]
+    if isinstance(c, CoolingAction):
+        return c
+    if c not in cooling_registry:
+        raise UnknownCoolingAction(c)
+    return cooling_registry[c]
 
 
 def ensure_species(s):
-    return s if isinstance(s, Species) else species_registry[s]
+    if isinstance(s, Species):
+        return s
+    if s not in species_registry:
+        raise UnknownSpecies(s)
+    return species_registry[s]
 
 
 count_m = sympy.Symbol("m", integer=True)
@@ -77,7 +90,7 @@ index_i = sympy.Idx("i", count_m)
 
 
 @functools.total_ordering
-class _KeyOrdered:
+class ComparableMixin:
     """Total order and hash through ``_cmpkey`` (reference: dengo/mixin.py:5-34)."""
 
     def _cmpkey(self):
@@ -110,7 +123,7 @@ class ReactionCoefficient(sympy.Symbol):
     energy = None
 
 
-class Species(_KeyOrdered):
+class Species(ComparableMixin):
     """A state variable of the network (reference: reaction_classes.py:273-285)."""
 
     def __init__(self, name, weight, pretty_name=None):
@@ -167,7 +180,7 @@ class MolecularSpecies(ChemicalSpecies):
                          "%s with %s free electrons" % (name, free_electrons))
 
 
-class Reaction(_KeyOrdered):
+class Reaction(ComparableMixin):
     """A mass-action reaction ``sum(n_l * L) -> sum(n_r * R)`` with rate table.
 
     ``coeff_fn(network)`` returns the rate on ``network.T`` (or ``network.z``

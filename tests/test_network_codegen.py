@@ -141,3 +141,20 @@ def test_table_file_c_writer_round_trip(tmp_path):
     assert subprocess.call([str(exe), str(out)]) == 0
     d = read_table_file(str(out))
     assert list(d) == ["H_1", "time"] and d["H_1"][1] == -2.25e-300 and d["time"][0] == 4.5e13
+
+
+def test_unknown_names_raise_the_references_exceptions():
+    """Lookups of unregistered names raise dengo's exception types
+    (dengo/exceptions.py), which are also KeyErrors."""
+    from dengo_gb300.chemical_network import ChemicalNetwork
+    from dengo_gb300.exceptions import DengoException, UnknownReaction, UnknownSpecies
+    from dengo_gb300.mixin import ComparableMixin
+    from dengo_gb300.reaction_classes import Species, ensure_species
+    net = ChemicalNetwork()
+    with pytest.raises(UnknownReaction) as e:
+        net.add_reaction("no_such_reaction")
+    assert isinstance(e.value, KeyError) and isinstance(e.value, DengoException)
+    assert "no_such_reaction" in str(e.value)
+    with pytest.raises(UnknownSpecies):
+        ensure_species("no_such_species")
+    assert issubclass(Species, ComparableMixin)
