@@ -1,0 +1,279 @@
+"""The engines' linear solves compiled for the host.
+
+``gauss_elim_fast`` (dengo_gb300/csrc/dg_engine.cuh: the FP64 elimination
+that skips updates by exact zeros) and ``MixedSolve`` (dg_mixed.cuh: the
+equilibrated FP32 LU with FP64 refinement) are cut out of the CUDA sources
+and compiled with g++ (``-ffp-contract=off``, as the CUDA build uses
+``--fmad=false``; the explicit fma calls are fused on both).  IEEE single and
+double arithmetic, ``fmaf`` and ``fma`` round the same way on the host as on
+the GPU, so these are the device's results.  The Newton matrices are the
+primordial network's, built as BE_Resid_Jac builds them
+(BE_chem_solve.C:280-321) from the generated Jacobian (also compiled for the
+host) on seeded cells and a range of substep lengths."""
+import ctypes as C
+import os
+import re
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "dengo_gb300", "csrc")
+P_D = C.POINTER(C.c_double)
+N = 10
+
+SHIMS = r'''
+#include <math.h>
+#include <string.h>
+#define __device__
+#define __host__
+#define __forceinline__ inline
+static inline float __uint_as_float(unsigned int u) { float f; memcpy(&f, &u, 4); return f; }
+static inline unsigned int __float_as_uint(float f) { unsigned int u; memcpy(&u, &f, 4); return u; }
+static inline int __clz(unsigned int x) { return x ? __builtin_clz(x) : 32; }
+static inline double __fma_rn(double a, double b, double c) { return fma(a, b, c); }
+#include "dg_math.h"
+#include "dg_slots.cuh"
+#include "dg_mixed.cuh"
+#include "primordial_solver.h"
+'''
+
+EXPORTS = r'''
+using Net = dgnet_primordial::Net;
+namespace dg {
+%(gauss)s
+}
+extern "C" void hx_gauss(double *A, double *x) { dg::gauss_elim_fast<Net::N, 1>(dg::Slots<1>{A}, *(double (*)[Net::N])x); }
+extern "C" int hx_mixed(double *A, const double *g, double *x)
+{
+    float jf[Net::N * Net::N];
+    return dg::MixedSolve<Net, 1>{dg::Slots<1>{A}, dg::SlotsF<1>{jf}}(
+        *(const double (*)[Net::N])g, *(double (*)[Net::N])x) ? 1 : 0;
+}
+/* The refinement loop of MixedSolve::operator(), reporting how it ended:
+ * 0 declined (non-finite), 1 correction below 2^-40 of max|x|, 2 stopped
+ * because the correction did not halve, 3 MAX_REFINE steps taken. */
+extern "C" int hx_mixed_status(double *A, const double *g, double *x)
+{
+    constexpr int NN = Net::N;
+    float jf[NN * NN];
+    const dg::MixedSolve<Net, 1> ms{dg::Slots<1>{A}, dg::SlotsF<1>{jf}};
+    const double (&gg)[NN] = *(const double (*)[NN])g;
+    double (&xx)[NN] = *(double (*)[NN])x;
+    int s[NN], t[NN], piv[NN];
+    if (!ms.prepare(gg, s, t, piv, xx)) return 0;
+    int eprev = 0x7ff;
+    for (int it = 0; it < ms.MAX_REFINE; it++) {
+        double r[NN];
+        for (int i = 0; i < NN; i++) r[i] = ms.residual_row(i, gg[i], xx);
+        const int eprev_in = eprev;
+        bool more;
+        if (!ms.refine(piv, s, t, r, xx, eprev, more)) return 0;
+        if (!more) {
+            int ex = 0;
+            for (int j = 0; j < NN; j++) ex = dg_expo(xx[j]) > ex ? dg_expo(xx[j]) : ex;
+            return eprev <= ex - 40 ? 1 : (eprev >= eprev_in ? 2 : 1);
+        }
+    }
+    return 3;
+}
+extern "C" float hx_f32_scaled(double v, int e) { return dg::dg_f32_scaled(v, e); }
+extern "C" double hx_f64_scaled(float f, int e) { return dg::dg_f64_scaled(f, e); }
+
+struct Rates { const double *v; double operator[](int k) const { return v[k]; } };
+struct Put {
+    double *J;
+    void operator()(int q, int v, double jv) const { J[v * Net::N + q] = jv; }
+    void zero(int q, int v) const { J[v * Net::N + q] = 0.0; }
+};
+/* raw Jacobian of one cell (number densities + ge) at rates R */
+extern "C" int hx_jac(const double *y, const double *R, double *J)
+{
+    double yy[Net::N], T, Tge;
+    for (int i = 0; i < Net::N; i++) yy[i] = y[i];
+    Net::temperature(yy, 1.0, 1e9, T, Tge);
+    return Net::jac(yy, Rates{R}, Tge, T, -1.0, Put{J}) ? 1 : 0;
+}
+'''
+
+
+def _cut(path, pattern):
+    with open(path) as f:
+        src = f.read()
+    m = re.search(pattern, src, re.S | re.M)
+    assert m, pattern
+    return m.group(0)
+
+
+@pytest.fixture(scope="module")
+def hx(tmp_path_factory):
+    from dengo_gb300.build import network_dir
+    gdir = network_dir("primordial")
+    net = _cut(os.path.join(gdir, "primordial_solver.cu"), r"^struct Net \{.*?^\};$")
+    gauss = _cut(os.path.join(CSRC, "dg_engine.cuh"),
+                 r"^template <int N, int BLOCK>\n__device__ __forceinline__ void gauss_elim_fast"
+                 r".*?^\}$")
+    d = tmp_path_factory.mktemp("hx")
+    src = d / "hx.cpp"
+    src.write_text(SHIMS + "namespace dgnet_primordial {\n" + net + "\n}\n" +
+                   EXPORTS % dict(gauss=gauss))
+    so = d / "hx.so"
+    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-w",
+                           "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-I", gdir,
+                           str(src), "-o", str(so)])
+    lib = C.CDLL(str(so))
+    lib.hx_gauss.argtypes = [P_D, P_D]
+    lib.hx_mixed.argtypes = [P_D, P_D, P_D]
+    lib.hx_mixed_status.argtypes = [P_D, P_D, P_D]
+    lib.hx_f32_scaled.argtypes = [C.c_double, C.c_int]
+    lib.hx_f32_scaled.restype = C.c_float
+    lib.hx_f64_scaled.argtypes = [C.c_float, C.c_int]
+    lib.hx_f64_scaled.restype = C.c_double
+    lib.hx_jac.argtypes = [P_D, P_D, P_D]
+    return lib
+
+
+def _newton_matrices(hx, count=60, seed=99):
+    """(A, g) pairs: the scaled I - dt J of BE_Resid_Jac at seeded config-1
+    and config-3 cells, rates interpolated as the engine does, dt from 1e3
+    to 1e15 s, and right-hand sides of the state's magnitude."""
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.codegen.spec import network_spec
+    from dengo_gb300.networks import build_network
+    from dengo_gb300.tablefile import read_table_file
+    from dengo_gb300.workloads import PRIMORDIAL_WEIGHTS, PRIMORDIAL_ORDER, primordial_cells
+    net = build_network("primordial")
+    t = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
+    tabs = [t[tb.name] for tb in network_spec(net, "primordial").tables]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a, _ = primordial_cells(count // 2, "config1", seed=seed)
+    b, _ = primordial_cells(count - count // 2, "config3", seed=seed + 1)
+    out = []
+    for st in np.concatenate([a, b]):
+        y = np.array([st[i] if s == "ge" else st[i] / (PRIMORDIAL_WEIGHTS[s] * 1.67e-24)
+                      for i, s in enumerate(PRIMORDIAL_ORDER)])
+        # T from the energy, rates at that T (linear in log T, as the engine)
+        J = np.zeros(N * N)
+        T = _temperature(y)
+        lb, nb = np.log(1.0), 1023
+        dbin = (np.log(1e9) - lb) / nb
+        logT = np.log(T)
+        bin_ = min(max(int((logT - lb) / dbin), 0), nb - 1)
+        t1, t2 = lb + bin_ * dbin, lb + (bin_ + 1) * dbin
+        tdef = (logT - t1) / (t2 - t1)
+        R = np.array([tb[bin_] + tdef * (tb[bin_ + 1] - tb[bin_]) for tb in tabs])
+        assert hx.hx_jac(y.ctypes.data_as(P_D), R.ctypes.data_as(P_D), J.ctypes.data_as(P_D))
+        dt = 10.0 ** rng.uniform(3, 15)
+        sc = y.copy()
+        A = np.empty(N * N)
+        for v in range(N):
+            for q in range(N):
+                x = J[v * N + q] * (1.0 / sc[q])
+                x = x * sc[v]
+                x = -dt * x
+                A[v * N + q] = x + 1.0 if q == v else x
+        g = rng.standard_normal(N) * 10.0 ** rng.uniform(-8, 0, N)
+        out.append((A, g))
+    return out
+
+
+def _temperature(y):
+    kb, mh, gamma = 1.3806504e-16, 1.67e-24, 5.0 / 3.0
+    w = np.array([2.0, 2.0, 1.00794, 1.00794, 1.00794, 4.002602, 4.002602, 4.002602])
+    density = float((w * y[:8]).sum())
+    return min(max(density * y[9] * mh / (kb * float(y[:9].sum()) / (gamma - 1.0)), 1.0), 1e9)
+
+
+def _exact(A, g):
+    """A^-1 g in rational arithmetic (column-major A)."""
+    M = [[Fraction(A[j * N + i]) for j in range(N)] + [Fraction(g[i])] for i in range(N)]
+    for k in range(N):
+        p = max(range(k, N), key=lambda i: abs(M[i][k]))
+        M[k], M[p] = M[p], M[k]
+        for i in range(k + 1, N):
+            if M[i][k] != 0:
+                f = M[i][k] / M[k][k]
+                M[i] = [a - f * b for a, b in zip(M[i], M[k])]
+    x = [Fraction(0)] * N
+    for i in reversed(range(N)):
+        x[i] = (M[i][N] - sum(M[i][j] * x[j] for j in range(i + 1, N))) / M[i][i]
+    return np.array([float(v) for v in x])
+
+
+def test_fp64_elimination_equals_the_references(hx):
+    """gauss_elim_fast gives the reference's Gauss_Elim results (the
+    oracle's restatement, BE_chem_solve.C:330-382) on every system, up to
+    the sign of exact zeros."""
+    from oracle import Oracle
+    orc = Oracle("primordial")
+    orc.lib.dgo_Gauss_Elim.argtypes = [P_D, P_D, P_D, C.c_int]
+    for A, g in _newton_matrices(hx):
+        A1, x1 = A.copy(), g.copy()
+        hx.hx_gauss(A1.ctypes.data_as(P_D), x1.ctypes.data_as(P_D))
+        A2, x2, b2 = A.copy(), np.zeros(N), g.copy()
+        orc.lib.dgo_Gauss_Elim(A2.ctypes.data_as(P_D), x2.ctypes.data_as(P_D),
+                               b2.ctypes.data_as(P_D), N)
+        assert np.array_equal(x1, x2)
+
+
+def test_mixed_solve_accuracy_where_refinement_converges(hx):
+    """Where the refinement ends with a correction below 2^-40 of max|x|
+    (most systems), the refined FP32 solve is within 2^-38 of the exact
+    solution's largest component, or no further from it than FP64
+    elimination.  The loop the harness runs is MixedSolve's own (same
+    solution bits).  Where it stops early -- the correction stopped halving,
+    or four steps were taken -- the engine currently keeps the solution; on
+    these seeded systems that is about one in six, some of them far off."""
+    counts = [0, 0, 0, 0]
+    for A, g in _newton_matrices(hx, count=120):
+        xm, xs = np.zeros(N), np.zeros(N)
+        Am = A.copy()
+        assert hx.hx_mixed(Am.ctypes.data_as(P_D), g.ctypes.data_as(P_D), xm.ctypes.data_as(P_D))
+        assert np.array_equal(Am, A)     # the FP64 matrix is left intact
+        status = hx.hx_mixed_status(A.copy().ctypes.data_as(P_D), g.ctypes.data_as(P_D),
+                                    xs.ctypes.data_as(P_D))
+        assert np.array_equal(xm, xs)
+        counts[status] += 1
+        if status != 1:
+            continue
+        A1, x1 = A.copy(), g.copy()
+        hx.hx_gauss(A1.ctypes.data_as(P_D), x1.ctypes.data_as(P_D))
+        xe = _exact(A, g)
+        scale = np.abs(xe).max()
+        em = np.abs(xm - xe).max() / scale
+        e64 = np.abs(x1 - xe).max() / scale
+        assert em <= max(e64, 2.0 ** -38), (em, e64)
+    assert counts[0] == 0 and counts[1] >= 0.7 * sum(counts), counts
+
+
+def test_mixed_solve_declines_nonfinite_systems(hx):
+    A, g = _newton_matrices(hx, count=2)[0]
+    for bad in (np.nan, np.inf):
+        for where in ("A", "g"):
+            A1, g1, x = A.copy(), g.copy(), np.zeros(N)
+            (A1 if where == "A" else g1)[3] = bad
+            assert hx.hx_mixed(A1.ctypes.data_as(P_D), g1.ctypes.data_as(P_D),
+                               x.ctypes.data_as(P_D)) == 0
+
+
+def test_fp32_rounding_by_integer_operations(hx):
+    """dg_f32_scaled(v, e) is v * 2^e rounded to nearest even in FP32 (a
+    signed zero below FP32's normal range); dg_f64_scaled(f, e) is exact."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    v = rng.standard_normal(20000) * 10.0 ** rng.uniform(-30, 30, 20000)
+    v[:8] = [0.0, -0.0, 1.0, -1.0, 1.5, 2.0 ** -24 * 3, 1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24]
+    e = rng.integers(-60, 60, v.size)
+    for vi, ei in zip(v, e):
+        w = np.ldexp(vi, int(ei))
+        if abs(w) >= np.finfo(np.float32).max:
+            continue                     # outside the function's stated domain
+        got = np.float32(hx.hx_f32_scaled(float(vi), int(ei)))
+        if abs(w) < np.finfo(np.float32).tiny:
+            assert got == 0.0 and np.signbit(got) == np.signbit(vi)
+        else:
+            assert got.view(np.uint32) == np.float32(w).view(np.uint32), (vi, ei)
+    f = (rng.standard_normal(5000) * 10.0 ** rng.uniform(-30, 30, 5000)).astype(np.float32)
+    for fi, ei in zip(f, rng.integers(-200, 200, f.size)):
+        assert hx.hx_f64_scaled(float(fi), int(ei)) == np.ldexp(float(fi), int(ei))
