@@ -27,9 +27,18 @@
  * inf/NaN, or the FP32 solve yields a non-finite value, mixed_solve returns
  * false and the caller runs the FP64 elimination instead (which then
  * reproduces the reference's NaN propagation).
+ *
+ * Built with DG_MIXED_STRICT=1, a refinement that ends without meeting the
+ * 2^-40 criterion (its correction stopped halving, or MAX_REFINE steps were
+ * taken) also hands the system to the FP64 elimination; by default such a
+ * solution is kept and Newton's own convergence test judges the sweep.
  */
 #ifndef DG_MIXED_CUH
 #define DG_MIXED_CUH
+
+#ifndef DG_MIXED_STRICT
+#define DG_MIXED_STRICT 0
+#endif
 
 #include "dg_math.h"
 #include "dg_slots.cuh"
@@ -265,7 +274,21 @@ struct MixedSolve {
         return fin;
     }
 
-    /* x = A^-1 g; false: A or g holds inf/NaN or the FP32 solve broke down,
+    /* Whether a refinement that stopped with last-correction exponent ed met
+     * the 2^-40 criterion (a zero correction meets it). */
+    __device__ __forceinline__ static bool refined(const double (&x)[N], int ed)
+    {
+        int ex = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const int e = dg_expo(x[j]);
+            ex = e > ex ? e : ex;
+        }
+        return ed == 0 || ed <= ex - 40;
+    }
+
+    /* x = A^-1 g; false: A or g holds inf/NaN or the FP32 solve broke down
+     * (with DG_MIXED_STRICT also: the refinement stopped short of 2^-40),
      * x undefined, A and g untouched. */
     __device__ __forceinline__ bool operator()(const double (&g)[N], double (&x)[N]) const
     {
@@ -279,9 +302,9 @@ struct MixedSolve {
             for (int i = 0; i < N; i++) r[i] = residual_row(i, g[i], x);
             bool more;
             if (!refine(piv, s, t, r, x, eprev, more)) return false;
-            if (!more) break;
+            if (!more) return !DG_MIXED_STRICT || refined(x, eprev);
         }
-        return true;
+        return !DG_MIXED_STRICT;
     }
 };
 

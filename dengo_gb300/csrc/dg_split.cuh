@@ -446,6 +446,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                         for (int i = 0; i < N; i++) X[i] = x[i];
                         F(F_EPREV) = eprev;
                         F(F_MIX) = more ? 1 : 2;
+                        if (DG_MIXED_STRICT && !more && !MS::refined(x, eprev)) F(F_MIX) = 3;
                     } else {
                         fp64_fallback<N>(J, G);
                         F(F_MIX) = 0;
@@ -453,6 +454,13 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                 }
                 __syncthreads();
             }
+#if DG_MIXED_STRICT
+            /* refinement stopped short of 2^-40 (3) or ran out of steps (1) */
+            if (w == 0 && do_lu && (F(F_MIX) == 1 || F(F_MIX) == 3)) {
+                fp64_fallback<N>(J, G);
+                F(F_MIX) = 0;
+            }
+#endif
             if (w == 0 && do_lu && F(F_MIX) != 0)
                 for (int i = 0; i < N; i++) G[i] = X[i];
         } else {

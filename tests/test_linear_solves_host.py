@@ -109,6 +109,15 @@ def _cut(path, pattern):
 
 @pytest.fixture(scope="module")
 def hx(tmp_path_factory):
+    return _build_hx(tmp_path_factory, strict=False)
+
+
+@pytest.fixture(scope="module")
+def hx_strict(tmp_path_factory):
+    return _build_hx(tmp_path_factory, strict=True)
+
+
+def _build_hx(tmp_path_factory, strict):
     from dengo_gb300.build import network_dir
     gdir = network_dir("primordial")
     net = _cut(os.path.join(gdir, "primordial_solver.cu"), r"^struct Net \{.*?^\};$")
@@ -121,6 +130,7 @@ def hx(tmp_path_factory):
                    EXPORTS % dict(gauss=gauss))
     so = d / "hx.so"
     subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-w",
+                           "-DDG_MIXED_STRICT=%d" % int(strict),
                            "-I", CSRC, "-I", os.path.join(ROOT, "include"), "-I", gdir,
                            str(src), "-o", str(so)])
     lib = C.CDLL(str(so))
@@ -246,6 +256,30 @@ def test_mixed_solve_accuracy_where_refinement_converges(hx):
         e64 = np.abs(x1 - xe).max() / scale
         assert em <= max(e64, 2.0 ** -38), (em, e64)
     assert counts[0] == 0 and counts[1] >= 0.7 * sum(counts), counts
+
+
+def test_strict_build_hands_unfinished_refinements_to_fp64(hx, hx_strict):
+    """Built with DG_MIXED_STRICT=1 the solve declines (so the engine runs
+    the FP64 elimination) exactly the systems whose refinement stopped short
+    of 2^-40, and returns the same bits as the default build on the rest."""
+    seen = set()
+    for A, g in _newton_matrices(hx, count=120):
+        x0, x1 = np.zeros(N), np.zeros(N)
+        status = hx.hx_mixed_status(A.copy().ctypes.data_as(P_D), g.ctypes.data_as(P_D),
+                                    x0.ctypes.data_as(P_D))
+        ok = hx_strict.hx_mixed(A.copy().ctypes.data_as(P_D), g.ctypes.data_as(P_D),
+                                x1.ctypes.data_as(P_D))
+        assert ok == (1 if status == 1 else 0), status
+        if ok:
+            assert np.array_equal(x0, x1)
+        seen.add(status)
+    assert seen == {1, 2, 3}
+    # a zero right-hand side: zero corrections meet the criterion
+    A, _ = _newton_matrices(hx, count=2)[0]
+    x = np.ones(N)
+    assert hx_strict.hx_mixed(A.ctypes.data_as(P_D), np.zeros(N).ctypes.data_as(P_D),
+                              x.ctypes.data_as(P_D)) == 1
+    assert not x.any()
 
 
 def test_mixed_solve_declines_nonfinite_systems(hx):
