@@ -22,6 +22,35 @@ extern "C" double h_pow2(double x) { return dg_ipow<2>(x); }
 extern "C" double h_pow3(double x) { return dg_ipow<3>(x); }
 extern "C" double h_pow4(double x) { return dg_ipow<4>(x); }
 extern "C" double h_glibc_log(double x) { return log(x); }
+/* dg_div(a, b, 1/b) against a / b on random bit patterns: a and b with
+ * uniformly random sign, exponent field and mantissa (every class of value),
+ * and on pairs whose exponents straddle the guarded range's edges.  Returns
+ * the number of results whose bits differ (NaNs compare equal). */
+extern "C" long long h_div_mismatch(long long n, unsigned long long seed) {
+    long long bad = 0;
+    for (long long i = 0; i < n; i++) {
+        seed ^= seed << 13; seed ^= seed >> 7; seed ^= seed << 17;
+        unsigned long long ba = seed;
+        seed ^= seed << 13; seed ^= seed >> 7; seed ^= seed << 17;
+        unsigned long long bb = seed;
+        if (i & 1) {   /* exponents near the guard's bounds (150, 1900, +-800) */
+            static const int ea[] = {149, 150, 151, 1899, 1900, 1901, 1023, 1100, 300};
+            static const int eb[] = {150, 1900, 1023, 949, 950, 951, 1851, 1852, 151};
+            const int ka = (int)((seed >> 3) % 9), kb = (int)((seed >> 9) % 9);
+            ba = (ba & 0x800fffffffffffffull) | ((unsigned long long)ea[ka] << 52);
+            bb = (bb & 0x800fffffffffffffull) | ((unsigned long long)eb[kb] << 52);
+        }
+        double a, b;
+        memcpy(&a, &ba, 8);
+        memcpy(&b, &bb, 8);
+        const double q = dg_div(a, b, 1.0 / b), r = a / b;
+        uint64_t bq, br;
+        memcpy(&bq, &q, 8);
+        memcpy(&br, &r, 8);
+        bad += !(bq == br || (q != q && r != r));
+    }
+    return bad;
+}
 extern "C" double h_glibc_pow(double x, double y) { return pow(x, y); }
 extern "C" long long h_log_mismatch(long long n, unsigned long long seed) {
     long long bad = 0;
@@ -53,6 +82,8 @@ def lib(tmp_path_factory):
     L.h_glibc_pow.argtypes = [C.c_double, C.c_double]
     L.h_log_mismatch.restype = C.c_longlong
     L.h_log_mismatch.argtypes = [C.c_longlong, C.c_ulonglong]
+    L.h_div_mismatch.restype = C.c_longlong
+    L.h_div_mismatch.argtypes = [C.c_longlong, C.c_ulonglong]
     return L
 
 
@@ -76,6 +107,15 @@ def test_log_special_values(lib):
 def test_log_agrees_with_glibc_except_its_misroundings(lib):
     bad = lib.h_log_mismatch(2_000_000, 88172645463325252)
     assert bad / 2_000_000 < 2e-4
+
+
+def test_shared_reciprocal_division_is_exact(lib):
+    """dg_div(a, b, 1/b) -- one correctly rounded reciprocal shared by all
+    quotients with divisor b, then Markstein's FMA correction inside a
+    guarded exponent range, a true division outside it -- equals a / b bit
+    for bit (Markstein, IA-64 and Elementary Functions, 2000: the corrected
+    quotient is correctly rounded when neither step under- or overflows)."""
+    assert lib.h_div_mismatch(20_000_000, 0x9E3779B97F4A7C15) == 0
 
 
 def test_integer_powers(lib):
