@@ -44,6 +44,7 @@ EXPORTS = r'''
 using Net = dgnet_primordial::Net;
 namespace dg {
 %(gauss)s
+%(jacput)s
 }
 extern "C" void hx_gauss(double *A, double *x) { dg::gauss_elim_fast<Net::N, 1>(dg::Slots<1>{A}, *(double (*)[Net::N])x); }
 extern "C" int hx_mixed(double *A, const double *g, double *x)
@@ -88,6 +89,22 @@ struct Put {
     void operator()(int q, int v, double jv) const { J[v * Net::N + q] = jv; }
     void zero(int q, int v) const { J[v * Net::N + q] = 0.0; }
 };
+/* The engines' scaled Newton matrix of one cell: I - dt diag(1/sc) J
+ * diag(sc), each entry stored by JacPut as it is produced (structural
+ * zeros written directly) */
+extern "C" int hx_jacput(const double *y, const double *R, const double *sc, double dt,
+                         double *A)
+{
+    double yy[Net::N], T, Tge, inv[Net::N], scv[Net::N];
+    for (int i = 0; i < Net::N; i++) {
+        yy[i] = y[i];
+        scv[i] = sc[i];
+        inv[i] = 1.0 / sc[i];
+    }
+    Net::temperature(yy, 1.0, 1e9, T, Tge);
+    dg::JacPut<Net::N, 1> put{dg::Slots<1>{A}, dg::Slots<1>{inv}, dg::Slots<1>{scv}, -dt, false};
+    return Net::jac(yy, Rates{R}, Tge, T, -1.0, put) ? 1 : 0;
+}
 /* raw Jacobian of one cell (number densities + ge) at rates R */
 extern "C" int hx_jac(const double *y, const double *R, double *J)
 {
@@ -124,10 +141,12 @@ def _build_hx(tmp_path_factory, strict):
     gauss = _cut(os.path.join(CSRC, "dg_engine.cuh"),
                  r"^template <int N, int BLOCK>\n__device__ __forceinline__ void gauss_elim_fast"
                  r".*?^\}$")
+    jacput = _cut(os.path.join(CSRC, "dg_engine.cuh"),
+                  r"^template <int N, int BLOCK>\nstruct JacPut \{.*?^\};$")
     d = tmp_path_factory.mktemp("hx")
     src = d / "hx.cpp"
     src.write_text(SHIMS + "namespace dgnet_primordial {\n" + net + "\n}\n" +
-                   EXPORTS % dict(gauss=gauss))
+                   EXPORTS % dict(gauss=gauss, jacput=jacput))
     so = d / "hx.so"
     subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-w",
                            "-DDG_MIXED_STRICT=%d" % int(strict),
@@ -142,10 +161,11 @@ def _build_hx(tmp_path_factory, strict):
     lib.hx_f64_scaled.argtypes = [C.c_float, C.c_int]
     lib.hx_f64_scaled.restype = C.c_double
     lib.hx_jac.argtypes = [P_D, P_D, P_D]
+    lib.hx_jacput.argtypes = [P_D, P_D, P_D, C.c_double, P_D]
     return lib
 
 
-def _newton_matrices(hx, count=60, seed=99):
+def _newton_matrices(hx, count=60, seed=99, pieces=False):
     """(A, g) pairs: the scaled I - dt J of BE_Resid_Jac at seeded config-1
     and config-3 cells, rates interpolated as the engine does, dt from 1e3
     to 1e15 s, and right-hand sides of the state's magnitude."""
@@ -185,7 +205,7 @@ def _newton_matrices(hx, count=60, seed=99):
                 x = -dt * x
                 A[v * N + q] = x + 1.0 if q == v else x
         g = rng.standard_normal(N) * 10.0 ** rng.uniform(-8, 0, N)
-        out.append((A, g))
+        out.append((A, g) if not pieces else (A, y, R, sc, dt))
     return out
 
 
@@ -210,6 +230,18 @@ def _exact(A, g):
     for i in reversed(range(N)):
         x[i] = (M[i][N] - sum(M[i][j] * x[j] for j in range(i + 1, N))) / M[i][i]
     return np.array([float(v) for v in x])
+
+
+def test_scaled_newton_matrix_equals_the_references(hx):
+    """JacPut stores BE_Resid_Jac's scaled I - dt J (BE_chem_solve.C:301-318:
+    x / scale_eq, then x scale_var, then -dt x, +1 on the diagonal) bit for
+    bit, signs of zeros included: structural zeros are written directly as
+    the -0.0 (1.0 on the diagonal) the reference's operations give."""
+    for A, y, R, sc, dt in _newton_matrices(hx, count=40, pieces=True):
+        Ad = np.full(N * N, np.nan)
+        assert hx.hx_jacput(y.ctypes.data_as(P_D), R.ctypes.data_as(P_D), sc.ctypes.data_as(P_D),
+                            dt, Ad.ctypes.data_as(P_D))
+        assert np.array_equal(Ad.view(np.int64), A.view(np.int64))
 
 
 def test_fp64_elimination_equals_the_references(hx):
