@@ -48,6 +48,13 @@
  *
  * All computation runs on the GPU; there is no CPU fallback.  Functions that
  * take host pointers copy to and from the device inside the call.
+ *
+ * A data context holds, besides the tables, a work-queue counter and scratch
+ * (cell order, suspension records) that a solve uses on the GPU, so calls
+ * that share a context must not overlap on the GPU: issue them on one
+ * stream, or give each concurrent stream (each host thread, as with the
+ * reference's per-thread data struct) its own context.  Contexts are
+ * independent of one another.
  */
 #ifndef DENGO_GB300_H
 #define DENGO_GB300_H
