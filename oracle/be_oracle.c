@@ -281,6 +281,22 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
                   int dims, const dgo_config *cfg, double *ttot_out,
                   double *dt_out, dgo_stats *st)
 {
+    return dgo_run_strip_traj(net, data, tf, niter, z, input, rtol, atol, dims, cfg, ttot_out,
+                              dt_out, st, NULL, NULL, NULL, NULL, NULL);
+}
+
+/* The same loop recording, per iteration taken, what the Cython driver's
+ * intermediate arrays hold (run.pyx.template:146-175): the state after
+ * BE_chem_solve (traj[(iter * dims + cell) * N + s]), the last temperature
+ * computed (traj_T[iter * dims + cell]), the success flag, ttot and dt
+ * before this iteration's update.  Each pointer may be NULL; entries of
+ * iterations not taken are left as they are. */
+int dgo_run_strip_traj(const dgo_network *net, void *data, double tf, int niter,
+                       double z, double *input, double *rtol, double *atol,
+                       int dims, const dgo_config *cfg, double *ttot_out,
+                       double *dt_out, dgo_stats *st, double *traj, double *traj_T,
+                       unsigned char *traj_ok, double *traj_t, double *traj_dt)
+{
     const int N = net->nchem;
     const long long n = (long long)dims * N;
     long long i;
@@ -300,6 +316,15 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
         int status = dgo_BE_chem_solve(net->rhs, net->jac, input, dt, rtol, atol, dims, N,
                                        scale, data, u0, s, gu, Ju, cfg->max_sweeps,
                                        st ? &st->sweeps : NULL);
+        if (traj)
+            for (i = 0; i < n; i++) traj[(long long)iter * n + i] = input[i];
+        if (traj_T) {
+            const double *Ts = net->Ts(data);
+            for (i = 0; i < dims; i++) traj_T[(long long)iter * dims + i] = Ts[i];
+        }
+        if (traj_ok) traj_ok[iter] = status == 0 ? 1 : 0;
+        if (traj_t) traj_t[iter] = ttot;
+        if (traj_dt) traj_dt[iter] = dt;
         if (status == 0) {
             if (st) st->substeps_ok++;
             for (i = 0; i < n; i++) prev[i] = input[i];
@@ -326,15 +351,16 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
     return iter < niter ? iter + 1 : niter;
 }
 
-/* dgo_run_strip on a data object built from `tables` (freed on return). */
+/* dgo_run_strip_traj on a data object built from `tables` (freed on return). */
 int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, double tf,
                          int niter, double z, double *input, double *rtol, double *atol,
                          int dims, const dgo_config *cfg, double *ttot_out, double *dt_out,
-                         dgo_stats *st)
+                         dgo_stats *st, double *traj, double *traj_T, unsigned char *traj_ok,
+                         double *traj_t, double *traj_dt)
 {
     void *data = net->alloc_data(tables);
-    int it = dgo_run_strip(net, data, tf, niter, z, input, rtol, atol, dims, cfg, ttot_out,
-                           dt_out, st);
+    int it = dgo_run_strip_traj(net, data, tf, niter, z, input, rtol, atol, dims, cfg, ttot_out,
+                                dt_out, st, traj, traj_T, traj_ok, traj_t, traj_dt);
     net->free_data(data);
     return it;
 }

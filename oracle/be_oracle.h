@@ -90,11 +90,21 @@ int dgo_run_strip(const dgo_network *net, void *data, double tf, int niter,
                   int dims, const dgo_config *cfg, double *ttot_out,
                   double *dt_out, dgo_stats *st);
 
-/* dgo_run_strip on a data object built from the tables (freed on return). */
+/* dgo_run_strip recording the Cython driver's intermediate arrays
+ * (run.pyx.template:146-175); each trajectory pointer may be NULL. */
+int dgo_run_strip_traj(const dgo_network *net, void *data, double tf, int niter,
+                       double z, double *input, double *rtol, double *atol,
+                       int dims, const dgo_config *cfg, double *ttot_out,
+                       double *dt_out, dgo_stats *st, double *traj, double *traj_T,
+                       unsigned char *traj_ok, double *traj_t, double *traj_dt);
+
+/* dgo_run_strip_traj on a data object built from the tables (freed on
+ * return). */
 int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, double tf,
                          int niter, double z, double *input, double *rtol, double *atol,
                          int dims, const dgo_config *cfg, double *ttot_out, double *dt_out,
-                         dgo_stats *st);
+                         dgo_stats *st, double *traj, double *traj_T, unsigned char *traj_ok,
+                         double *traj_t, double *traj_dt);
 
 /* log x correctly rounded (long double log rounded to double) */
 double dgo_crlog(double x);

@@ -101,10 +101,14 @@ class Stats(C.Structure):
                 ("sweeps", C.c_longlong), ("status", C.c_int)]
 
 
-def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0):
-    """The Cython driver's loop (dgo_run_strip) on one strip of number
-    densities (already divided by the weights).  Returns a dict."""
+def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0, trajectories=False):
+    """The Cython driver's loop (dgo_run_strip_traj) on one strip of number
+    densities (already divided by the weights).  Returns a dict; with
+    ``trajectories`` also the driver's intermediate arrays: ``traj``
+    (niter, cells, N), ``traj_T`` (niter, cells), ``successful``, ``t``,
+    ``dt`` (niter), zeros after the last iteration taken."""
     inp = np.ascontiguousarray(input_number, np.float64).copy()
+    dims, n = inp.shape
     rt = np.full_like(inp, 1e-06)
     at = inp * 1e-06
     keep, tp = orc._tables(tables_in_order)
@@ -114,11 +118,20 @@ def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0):
     fn.restype = C.c_int
     fn.argtypes = [C.c_void_p, C.POINTER(P_D), C.c_double, C.c_int, C.c_double, P_D, P_D, P_D,
                    C.c_int, C.POINTER(Config), C.POINTER(C.c_double), C.POINTER(C.c_double),
-                   C.POINTER(Stats)]
+                   C.POINTER(Stats), P_D, P_D, C.c_void_p, P_D, P_D]
+    tr = dict(traj=np.zeros((niter, dims, n)), traj_T=np.zeros((niter, dims)),
+              successful=np.zeros(niter, np.uint8), t=np.zeros(niter),
+              dt=np.zeros(niter)) if trajectories else None
+    args = ([_dp(tr["traj"]), _dp(tr["traj_T"]), tr["successful"].ctypes.data, _dp(tr["t"]),
+             _dp(tr["dt"])] if tr else [None] * 5)
     it = fn(orc.net_addr, tp, float(tf), int(niter), float(z), _dp(inp), _dp(rt), _dp(at),
-            inp.shape[0], C.byref(cfg), C.byref(ttot), C.byref(dt), C.byref(st))
-    return dict(state=inp, atol=at, ttot=ttot.value, dt=dt.value, iterations=it,
-                substeps_ok=st.substeps_ok, substeps_fail=st.substeps_fail, sweeps=st.sweeps)
+            dims, C.byref(cfg), C.byref(ttot), C.byref(dt), C.byref(st), *args)
+    out = dict(state=inp, atol=at, ttot=ttot.value, dt=dt.value, iterations=it,
+               substeps_ok=st.substeps_ok, substeps_fail=st.substeps_fail, sweeps=st.sweeps)
+    if tr:
+        tr["successful"] = tr["successful"].astype(bool)
+        out["trajectories"] = tr
+    return out
 
 
 class Reference:

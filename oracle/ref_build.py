@@ -29,11 +29,19 @@ Recipe (runs only where the reference checkout exists):
    ``g++ -O2 -ffp-contract=off -fopenmp -shared``.
 
 Output: ``oracle/_ref/libref_<name>.so`` exporting ``ref_*`` functions.
+
+``build_cython_driver(name)`` also compiles the reference's Cython driver
+as its ``write_solver`` rendered it (``<name>_solver_run.pyx``, from
+rates_and_rate_tables_run.pyx.template): Cython with ``language_level=2``
+(the template is Python-2 code) in C++ mode, linked with the rendered solver
+and ``BE_chem_solve.C`` into ``oracle/_ref/<name>/<name>_solver_run<ext>``,
+importable as the reference's own ``run_<name>``.
 """
 
 import os
 import subprocess
 import sys
+import sysconfig
 import types
 
 import numpy as np
@@ -309,6 +317,28 @@ def build(name="primordial"):
            harness, "-o", lib, "-lm"]
     subprocess.check_call(cmd)
     return lib
+
+
+def build_cython_driver(name="primordial"):
+    """Compile the reference's rendered Cython driver (see the module
+    docstring); returns the extension's directory (import
+    ``<name>_solver_run`` from there, with that directory as the working
+    directory so the solver finds its tables)."""
+    odir = os.path.join(OUT, name)
+    pyx = os.path.join(odir, "%s_solver_run.pyx" % name)
+    if not os.path.exists(pyx):
+        build(name)
+    cpp = os.path.join(odir, "%s_solver_run.cpp" % name)
+    subprocess.check_call([sys.executable, "-m", "cython", "-2", "--cplus", pyx, "-o", cpp],
+                          stdout=subprocess.DEVNULL)
+    so = os.path.join(odir, "%s_solver_run%s" % (name, sysconfig.get_config_var("EXT_SUFFIX")))
+    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+                           "-I", sysconfig.get_paths()["include"], "-I", np.get_include(),
+                           "-I", os.path.join(HERE, "hdf5_shim"), "-I", odir, cpp,
+                           os.path.join(odir, "%s_solver.C" % name),
+                           os.path.join(REF_ROOT, "dengo", "solvers", "BE_chem_solve.C"),
+                           "-o", so, "-lm"])
+    return odir
 
 
 if __name__ == "__main__":

@@ -206,11 +206,52 @@ def make_ion(name="oxygen", zs=(None,), cells=None):
     print("wrote %s golden vectors" % name)
 
 
+RUN_CASES = ((1e8, 3000), (1e10, 3000), (1e9, 40))
+
+
+def make_run():
+    """Golden vectors of the reference's own Cython driver run_primordial
+    (rates_and_rate_tables_run.pyx.template:81-205, compiled by
+    oracle/ref_build.py build_cython_driver) on one 16-cell config-1 strip:
+    for each (tf, niter) the final state (rv), the per-iteration success
+    flags, times and steps, and the temperature and ge trajectories."""
+    import importlib
+    import ref_build
+    from dengo_gb300.workloads import PRIMORDIAL_ORDER, PRIMORDIAL_WEIGHTS
+    odir = ref_build.build_cython_driver("primordial")
+    W = np.array([PRIMORDIAL_WEIGHTS.get(s, 1.0) for s in PRIMORDIAL_ORDER])
+    st, _ = primordial_cells(16, "config1", seed=31)
+    num = st / (W * 1.67e-24)
+    num[:, -1] = st[:, -1]
+    ics = {s: np.ascontiguousarray(num[:, j] * W[j]) for j, s in enumerate(PRIMORDIAL_ORDER)}
+    out = {"ics": np.stack([ics[s] for s in PRIMORDIAL_ORDER], axis=1),
+           "cases": np.array(RUN_CASES, dtype=float)}
+    cwd = os.getcwd()
+    sys.path.insert(0, odir)
+    os.chdir(odir)
+    try:
+        m = importlib.import_module("primordial_solver_run")
+        for k, (tf, niter) in enumerate(RUN_CASES):
+            rv, rv_t = m.run_primordial({s: a.copy() for s, a in ics.items()}, tf, niter=niter,
+                                        intermediate=1)
+            out["run%d_rv" % k] = np.stack([rv[s] for s in PRIMORDIAL_ORDER], axis=1)
+            for key in ("successful", "t", "dt"):
+                out["run%d_%s" % (k, key)] = np.asarray(rv_t[key])
+            out["run%d_T" % k] = np.asarray(rv_t["T"])
+            out["run%d_ge" % k] = np.asarray(rv_t["ge"])
+    finally:
+        os.chdir(cwd)
+    np.savez_compressed(os.path.join(HERE, "primordial_run_golden.npz"), **out)
+    print("wrote primordial_run_golden.npz")
+
+
 if __name__ == "__main__" and len(sys.argv) > 1:
     if sys.argv[1] == "oxygen":
         make_ion("oxygen")
     elif sys.argv[1] == "oxygen_uvb":
         make_ion("oxygen_uvb", zs=(0.0, 2.5, 9.0, 20.0))
+    elif sys.argv[1] == "run":
+        make_run()
     elif sys.argv[1] == "primordial_compton":
         make_ion("primordial_compton", zs=(-1.0, 0.0, 3.0, 9.0, 19.0),
                  cells=compton_cells())

@@ -30,6 +30,35 @@ def test_oracle_run_strip_reaches_tf_or_stops(tables_in_order, oracle):
     assert r["ttot"] < 1e10 and r["dt"] < 1e-30 * 1e10      # the dt floor ends the loop
 
 
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_oracle_run_strip_matches_reference_cython_driver(tables_in_order, oracle, case):
+    """The oracle's loop against the reference's own Cython driver
+    run_primordial (compiled from its rendered .pyx; goldens from
+    tests/golden/make_golden.py run): final values, and per iteration the
+    success flags, times, steps, temperatures and energies, bit for bit."""
+    import os
+    import platform
+    from oracle import run_strip
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "primordial_run_golden.npz"))
+    tf, niter = g["cases"][case]
+    niter = int(niter)
+    inp = g["ics"] / W
+    r = run_strip(oracle, tables_in_order, inp, tf, niter, trajectories=True)
+    tr = r["trajectories"]
+    ige = PRIMORDIAL_ORDER.index("ge")
+    got = dict(rv=r["state"] * W, successful=tr["successful"], t=tr["t"], dt=tr["dt"],
+               T=tr["traj_T"].T, ge=tr["traj"][:, :, ige].T)
+    for key, a in got.items():
+        b = g["run%d_%s" % (case, key)]
+        assert a.shape == b.shape, key
+        if platform.machine() == "x86_64" or key in ("successful",):
+            a = np.ascontiguousarray(a, b.dtype)
+            assert np.array_equal(a.view(np.uint8), np.ascontiguousarray(b).view(np.uint8)), key
+        else:
+            assert np.allclose(a, b, rtol=1e-12, atol=0), key
+    assert r["iterations"] == int(np.count_nonzero(g["run%d_dt" % case]))
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("tf,niter", [(1e8, 3000), (1e10, 3000), (1e9, 40)])
 def test_gpu_run_strip_matches_oracle(solver, oracle, tables_in_order, tf, niter):
