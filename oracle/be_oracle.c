@@ -365,6 +365,13 @@ int dgo_run_strip_tables(const dgo_network *net, const double *const *tables, do
     return it;
 }
 
-/* log x correctly rounded to double (through long double; checked against
- * a 200-bit log in tests/test_oracle_golden.py) */
+/* log x correctly rounded to double: a quad-precision log rounded once to
+ * double (x86-64: libquadmath's logq, as its long double has only 64 bits
+ * and rounding its log to double would round twice; AArch64: long double is
+ * quad).  Checked against a 200-bit log in tests/test_oracle_golden.py. */
+#if defined(__x86_64__)
+#include <quadmath.h>
+double dgo_crlog(double x) { return (double)logq((__float128)x); }
+#else
 double dgo_crlog(double x) { return (double)logl(x); }
+#endif

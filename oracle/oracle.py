@@ -7,6 +7,7 @@ tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -35,7 +36,8 @@ def build_oracle(name="primordial", force=False, crlog=False):
     if force or not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out)
                                                for s in srcs):
         extra = ["-DDGO_LOG=dgo_crlog"] if crlog else []
-        subprocess.check_call(["gcc"] + CFLAGS + extra + srcs + ["-o", out, "-lm"])
+        libs = ["-lquadmath"] if platform.machine() == "x86_64" else []
+        subprocess.check_call(["gcc"] + CFLAGS + extra + srcs + ["-o", out, "-lm"] + libs)
     return out
 
 

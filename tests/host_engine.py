@@ -1,0 +1,192 @@
+"""The single-lane CUDA engine (dengo_gb300/csrc/dg_engine.cuh, evolve_kernel)
+compiled for the host, for tests that need no GPU.
+
+The kernel source is compiled unchanged with g++ against CUDA's host headers;
+the few device built-ins it uses are given host meanings: ``threadIdx`` /
+``blockIdx`` / ``gridDim`` are set by the driver below, which runs the 32
+lanes of one CTA one after another; ``atomicAdd`` is a plain add (one lane
+runs at a time); ``__shfl_sync`` hands lane 0's value to the later lanes (lane
+0 runs first); ``__ldg`` is a load; the FP32 bit casts and ``__clz`` are
+their definitions.  IEEE double and single arithmetic, ``fma`` and ``fmaf``
+round the same way on the host as on the GPU (the CUDA build uses
+``--fmad=false``, this one ``-ffp-contract=off``), so every cell's result is
+the device's.  Which lane takes which cell differs from the GPU; no cell's
+result depends on that.
+
+``hx_evolve`` is one solve of a batch of cells (AoS, mass densities + ge)
+through the same launches as ``<n>_solve_cells_device``: one launch, or with
+a sweep budget the three launches of the stiff-cell redistribution, the
+resume list built on the host.
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "dengo_gb300", "csrc")
+CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+P_D = C.POINTER(C.c_double)
+P_I = C.POINTER(C.c_int)
+
+PRELUDE = r'''
+#include <math.h>
+#include <string.h>
+#include <vector>
+#include <cuda_runtime.h>
+struct hx_dim3 { unsigned x, y, z; };
+static hx_dim3 threadIdx, blockIdx, gridDim, blockDim;
+static inline float __uint_as_float(unsigned int u) { float f; memcpy(&f, &u, 4); return f; }
+static inline unsigned int __float_as_uint(float f) { unsigned int u; memcpy(&u, &f, 4); return u; }
+static inline int __clz(unsigned int x) { return x ? __builtin_clz(x) : 32; }
+static inline double __fma_rn(double a, double b, double c) { return fma(a, b, c); }
+static inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v)
+{
+    const unsigned long long o = *p;
+    *p += v;
+    return o;
+}
+static unsigned long long hx_lane0;
+static inline unsigned long long __shfl_sync(unsigned, unsigned long long v, int)
+{
+    if ((threadIdx.x & 31) == 0) hx_lane0 = v;
+    return hx_lane0;
+}
+template <class T> static inline T __ldg(const T *p) { return *p; }
+#define __launch_bounds__(...)
+namespace dg { double dg_smem[1 << 16]; }  /* the CTA's dynamic shared memory */
+#include "dg_engine.cuh"
+'''
+
+DRIVER = r'''
+using Net = dgnet_%(name)s::Net;
+constexpr int NN = Net::N;
+constexpr int NT = Net::NT;
+constexpr int B = 32;
+
+template <bool MIXED>
+static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned long long *queue)
+{
+    static_assert(dg::Lane<Net, B, MIXED>::SLOTS * B <= (1 << 16), "host shared memory");
+    blockIdx.x = 0;
+    gridDim.x = 1;
+    blockDim.x = B;
+    for (unsigned t = 0; t < B; t++) {
+        threadIdx.x = t;
+        dg::evolve_kernel<Net, B, MIXED>(io, ts, cfg, queue);
+    }
+}
+
+static void launch(bool mixed, dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg,
+                   unsigned long long *queue)
+{
+    if (mixed) launch<true>(io, ts, cfg, queue);
+    else launch<false>(io, ts, cfg, queue);
+}
+
+/* One solve of ncells cells (AoS, mass densities + ge), rtol = rtol_scalar,
+ * per-cell dtf, tables in the solver's order; the redistribution's three
+ * launches when sweep_budget > 0 (as solve_redistributed in dg_api.cuh). */
+extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long long ncells,
+                         double rtol_scalar, double z, int mixed, int schedule_queue,
+                         int sweep_budget, int max_sweeps, const double *const *tables,
+                         int *status, int *substeps, int *sweeps, int *failures, double *ttot,
+                         double *dt)
+{
+    static Net::Data data;
+    Net::setup_bins(&data);
+    const int nbins = Net::NT_LEN - 1;
+    std::vector<double2> pairs((size_t)nbins * NT);
+    for (int b = 0; b < nbins; b++)
+        for (int k = 0; k < NT; k++)
+            pairs[(size_t)b * NT + k] = make_double2(tables[k][b], tables[k][b + 1] - tables[k][b]);
+    std::vector<double> zvals(NT, 0.0);
+    dg::TableSet ts{pairs.data(), zvals.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
+                    data.bounds[0], data.bounds[1], z};
+    dg::CellIO io{state, atol, nullptr, rtol_scalar, dtf, 0.0, dt, ttot, status, substeps, sweeps,
+                  failures, nullptr, NN, 1, ncells};
+    dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1};
+    unsigned long long queue = 0;
+    unsigned long long *q = schedule_queue ? &queue : nullptr;
+    if (sweep_budget <= 0) {
+        launch(mixed, io, ts, kc, q);
+        return 0;
+    }
+    std::vector<double> rec((size_t)dg::rec_len<NN>() * ncells);
+    kc.sweep_budget = sweep_budget;
+    kc.rec = rec.data();
+    launch(mixed, io, ts, kc, q);
+    const int budgets[2] = {sweep_budget < (1 << 26) ? sweep_budget * 16 : 0, 0};
+    int resumed = 0;
+    for (int r = 0; r < 2; r++) {
+        std::vector<int> list;
+        for (long long c = 0; c < ncells; c++)
+            if (status[c] == dg::ST_SUSPENDED) list.push_back((int)c);
+        const unsigned int count = (unsigned int)list.size();
+        resumed += (int)count;
+        list.resize((size_t)ncells, -1);
+        dg::CellIO io2 = io;
+        io2.order = list.data();
+        dg::KernelCfg k2 = kc;
+        k2.resume = 1;
+        k2.resume_count = &count;
+        k2.sweep_budget = budgets[r];
+        queue = 0;
+        launch(mixed, io2, ts, k2, &queue);
+    }
+    return resumed;
+}
+'''
+
+
+def _cut_net(name):
+    from dengo_gb300.build import network_dir
+    with open(os.path.join(network_dir(name), "%s_solver.cu" % name)) as f:
+        src = f.read()
+    m = re.search(r"^struct Net \{.*?^\};$", src, re.S | re.M)
+    assert m, "no Net struct in the generated source of %s" % name
+    return "namespace dgnet_%s {\n%s\n}\n" % (name, m.group(0))
+
+
+def build(name, out_dir, strict=False):
+    """Compile the host engine for network ``name`` into ``out_dir``;
+    returns the ctypes library."""
+    from dengo_gb300.build import network_dir
+    src = os.path.join(str(out_dir), "hx_%s.cpp" % name)
+    with open(src, "w") as f:
+        f.write(PRELUDE + '#include "%s_solver.h"\n' % name + _cut_net(name) +
+                DRIVER % dict(name=name))
+    so = os.path.join(str(out_dir), "hx_%s%s.so" % (name, "_strict" if strict else ""))
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                           "-w", "-DDG_MIXED_STRICT=%d" % int(strict), "-I", CUDA_INCLUDE,
+                           "-I", CSRC, "-I", os.path.join(ROOT, "include"),
+                           "-I", network_dir(name), src, "-o", so])
+    lib = C.CDLL(so)
+    lib.hx_evolve.restype = C.c_int
+    lib.hx_evolve.argtypes = [P_D, P_D, P_D, C.c_longlong, C.c_double, C.c_double, C.c_int,
+                              C.c_int, C.c_int, C.c_int, C.POINTER(P_D), P_I, P_I, P_I, P_I,
+                              P_D, P_D]
+    return lib
+
+
+def evolve(lib, tables, state, dtf, z=-1.0, mixed=False, queue=True, sweep_budget=0,
+           max_sweeps=10, rtol=1e-6):
+    """Solve ``state`` (cells x N, mass densities + ge) for ``dtf`` with
+    atol = 1e-6 x state; returns a dict like ``Solver.solve_host``."""
+    import numpy as np
+    st = np.ascontiguousarray(state, np.float64).copy()
+    at = st * 1e-6
+    n = st.shape[0]
+    d = np.ascontiguousarray(np.broadcast_to(np.asarray(dtf, np.float64), (n,)))
+    out = dict(state=st, atol=at, status=np.zeros(n, np.int32), substeps=np.zeros(n, np.int32),
+               sweeps=np.zeros(n, np.int32), failures=np.zeros(n, np.int32),
+               ttot=np.zeros(n), dt=np.full(n, -1.0))
+    tabs = [np.ascontiguousarray(t, np.float64) for t in tables]
+    tp = (P_D * len(tabs))(*[t.ctypes.data_as(P_D) for t in tabs])
+    ip = lambda a: a.ctypes.data_as(P_I)
+    out["resumed"] = lib.hx_evolve(
+        st.ctypes.data_as(P_D), at.ctypes.data_as(P_D), d.ctypes.data_as(P_D), n, rtol, z,
+        int(mixed), int(queue), int(sweep_budget), int(max_sweeps), tp, ip(out["status"]),
+        ip(out["substeps"]), ip(out["sweeps"]), ip(out["failures"]),
+        out["ttot"].ctypes.data_as(P_D), out["dt"].ctypes.data_as(P_D))
+    return out

@@ -1,0 +1,139 @@
+"""The single-lane CUDA engine compiled for the host (tests/host_engine.py)
+against the oracle: the GPU tests' parity checks, run on the CPU from the
+kernel's own source -- the FP64 path, the mixed path (default and strict
+builds), the three-launch stiff-cell redistribution, and the Compton
+network at several redshifts."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import host_engine as he
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+RTOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def engines(tmp_path_factory):
+    d = tmp_path_factory.mktemp("host_engine")
+    return {"default": he.build("primordial", d), "strict": he.build("primordial", d, strict=True)}
+
+
+@pytest.fixture(scope="module")
+def tables():
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    with open(os.path.join(ROOT, "tests", "golden", "primordial_expressions.json")) as f:
+        order = json.load(f)["tables"]
+    t = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
+    return [np.ascontiguousarray(t[k]) for k in order]
+
+
+@pytest.fixture(scope="module")
+def crlog_oracle():
+    from oracle import Oracle
+    return Oracle("primordial", crlog=True)
+
+
+def _rel(a, b):
+    with np.errstate(invalid="ignore", divide="ignore"):
+        r = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    r[a == b] = 0.0
+    return r
+
+
+@pytest.mark.parametrize("config,seed", [("config1", 31337), ("config3", 31337)])
+@pytest.mark.parametrize("queue", [True, False])
+def test_fp64_engine_matches_oracle(engines, tables, crlog_oracle, config, seed, queue):
+    """Same status everywhere; on converged cells the oracle's substep,
+    sweep and failure counts and its state within 1e-10, at least 90 % of
+    them bit for bit (the rest differ by libm's pow(x, 3) rounding)."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(96, config, seed=seed)
+    h = he.evolve(engines["default"], tables, st, dtf, queue=queue)
+    ref = crlog_oracle.evolve_cells(tables, st, dtf, nthreads=0)
+    assert np.array_equal(h["status"], ref["status"])
+    ok = ref["status"] == 0
+    for k in ("substeps", "sweeps", "failures"):
+        assert np.array_equal(h[k][ok], ref[k][ok]), k
+    assert _rel(h["state"][ok], ref["state"][ok]).max(initial=0.0) <= RTOL
+    assert _rel(h["atol"][ok], ref["atol"][ok]).max(initial=0.0) <= RTOL
+    same = np.all(h["state"][ok].view(np.int64) == ref["state"][ok].view(np.int64), axis=1)
+    assert same.mean() >= 0.9
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("budget", [7, 150])
+def test_redistribution_is_bit_identical(engines, tables, mixed, budget):
+    """Cells set aside at the sweep budget, resumed, set aside again at 16x
+    and finished by a third launch end exactly as in one launch: state,
+    atol, dt, ttot, status and counters."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(64, "config3", seed=78)
+    one = he.evolve(engines["default"], tables, st, dtf, mixed=mixed)
+    three = he.evolve(engines["default"], tables, st, dtf, mixed=mixed, sweep_budget=budget)
+    assert three["resumed"] > 0
+    for k in ("state", "atol", "dt", "ttot"):
+        assert np.array_equal(one[k].view(np.int64), three[k].view(np.int64)), k
+    for k in ("status", "substeps", "sweeps", "failures"):
+        assert np.array_equal(one[k], three[k]), k
+
+
+@pytest.mark.parametrize("build", ["default", "strict"])
+@pytest.mark.parametrize("config,seed,n,min_frac", [("config1", 404, 96, 1.0),
+                                                     ("config3", 407, 128, 0.97)])
+def test_mixed_engine_within_1e6(engines, tables, crlog_oracle, build, config, seed, n, min_frac):
+    """Every oracle-converged cell converges; floored relative error
+    (atol = 1e-6 x input) within 1e-6 on every config-1 cell and >= 97 % of
+    config-3 cells -- the GPU test's cells and bar -- for both mixed
+    builds."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(n, config, seed=seed)
+    h = he.evolve(engines[build], tables, st, dtf, mixed=True)
+    ref = crlog_oracle.evolve_cells(tables, st, dtf, nthreads=0)
+    conv = ref["status"] == 0
+    assert np.all(h["status"][conv] == 0)
+    err = np.abs(h["state"][conv] - ref["state"][conv]) / np.maximum(
+        np.abs(ref["state"][conv]), 1e-6 * np.abs(st[conv]))
+    assert np.mean(err.max(axis=1) <= 1e-6) >= min_frac
+
+
+def test_strict_build_changes_almost_nothing_in_real_solves(engines, tables):
+    """On 256 config-3 cells the strict mixed build (refinements that stop
+    short of 2^-40 handed to the FP64 elimination) ends every cell with the
+    default build's status and sweep count, and with its state on all but
+    a few cells: in the solver's own Newton systems the refinement almost
+    always meets its criterion."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(256, "config3", seed=77)
+    a = he.evolve(engines["default"], tables, st, dtf, mixed=True)
+    b = he.evolve(engines["strict"], tables, st, dtf, mixed=True)
+    assert np.array_equal(a["status"], b["status"])
+    assert np.array_equal(a["sweeps"], b["sweeps"])
+    differ = ~np.all(a["state"].view(np.int64) == b["state"].view(np.int64), axis=1)
+    assert differ.sum() <= 3
+
+
+@pytest.mark.parametrize("z", [0.0, 3.0, 19.0])
+def test_compton_engine_matches_oracle(tmp_path_factory, z):
+    """The Compton network through the kernel's source, at redshifts where
+    its term matters, against its oracle and the reference's goldens."""
+    from oracle import Oracle
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "primordial_compton_golden.npz")))
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    t = read_table_file(os.path.join(network_dir("primordial_compton"),
+                                     "primordial_compton_tables.dgt"))
+    tabs = [np.ascontiguousarray(t[k]) for k in g["table_order"]]
+    lib = he.build("primordial_compton", tmp_path_factory.mktemp("compton"))
+    st, dtf = g["evolve_in"], g["evolve_dtf"]
+    h = he.evolve(lib, tabs, st, dtf, z=z)
+    ref = Oracle("primordial_compton", crlog=True).evolve_cells(tabs, st, dtf, z=z, nthreads=0)
+    assert np.array_equal(h["status"], ref["status"])
+    ok = ref["status"] == 0
+    assert _rel(h["state"][ok], ref["state"][ok]).max(initial=0.0) <= RTOL
+    assert np.array_equal(h["sweeps"][ok], ref["sweeps"][ok])
+    gs = g["evolve_z%g_state" % z]
+    assert _rel(h["state"][ok], gs[ok]).max(initial=0.0) <= RTOL
