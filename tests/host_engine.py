@@ -17,6 +17,15 @@ result depends on that.
 through the same launches as ``<n>_solve_cells_device``: one launch, or with
 a sweep budget the three launches of the stiff-cell redistribution, the
 resume list built on the host.
+
+The split engine (dg_split.cuh, evolve_split_kernel: 32 cells per CTA, each
+cell's sweep shared by NP warps that meet at __syncthreads) is built the
+same way with ``engine="split"``, but its 32 x NP lanes run as that many host
+threads: ``__syncthreads`` is a barrier across them, ``__syncthreads_or``,
+``__ballot_sync`` and ``__shfl_sync`` (warp 0 only) reductions between
+barriers, and the atomics take a lock.  One CTA runs the whole batch from
+the work queue.  A build that hangs is cut off by the caller's timeout
+(``evolve_in_subprocess``).
 """
 import ctypes as C
 import os
@@ -58,15 +67,130 @@ namespace dg { double dg_smem[1 << 16]; }  /* the CTA's dynamic shared memory */
 #include "dg_engine.cuh"
 '''
 
-DRIVER = r'''
-using Net = dgnet_%(name)s::Net;
-constexpr int NN = Net::N;
-constexpr int NT = Net::NT;
-constexpr int B = 32;
+PRELUDE_SPLIT = r'''
+#include <math.h>
+#include <string.h>
+#include <atomic>
+#include <mutex>
+#include <thread>
+#include <vector>
+#include <cuda_runtime.h>
+struct hx_dim3 { unsigned x, y, z; };
+static thread_local hx_dim3 threadIdx;
+static hx_dim3 blockIdx, gridDim, blockDim;
+static inline float __uint_as_float(unsigned int u) { float f; memcpy(&f, &u, 4); return f; }
+static inline unsigned int __float_as_uint(float f) { unsigned int u; memcpy(&u, &f, 4); return u; }
+static inline int __clz(unsigned int x) { return x ? __builtin_clz(x) : 32; }
+static inline double __fma_rn(double a, double b, double c) { return fma(a, b, c); }
+static std::mutex hx_atomic_lock;
+static inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v)
+{
+    std::lock_guard<std::mutex> g(hx_atomic_lock);
+    const unsigned long long o = *p;
+    *p += v;
+    return o;
+}
+static inline int atomicAnd(int *p, int v)
+{
+    std::lock_guard<std::mutex> g(hx_atomic_lock);
+    const int o = *p;
+    *p = o & v;
+    return o;
+}
+static inline int atomicMax(int *p, int v)
+{
+    std::lock_guard<std::mutex> g(hx_atomic_lock);
+    const int o = *p;
+    if (v > o) *p = v;
+    return o;
+}
+/* A reusable barrier whose waiters yield the core (the lanes far outnumber
+ * the host's cores, so sleeping and waking them costs more). */
+struct hx_barrier {
+    explicit hx_barrier(int n) : count(n), left(n), gen(0) {}
+    void arrive_and_wait()
+    {
+        const unsigned g = gen.load(std::memory_order_acquire);
+        if (left.fetch_sub(1, std::memory_order_acq_rel) == 1) {
+            left.store(count, std::memory_order_relaxed);
+            gen.store(g + 1, std::memory_order_release);
+        } else {
+            while (gen.load(std::memory_order_acquire) == g) std::this_thread::yield();
+        }
+    }
+    const int count;
+    std::atomic<int> left;
+    std::atomic<unsigned> gen;
+};
+static hx_barrier *hx_cta;    /* all lanes of the CTA */
+static hx_barrier *hx_warp0;  /* the 32 lanes of warp 0 */
+static inline void __syncthreads() { hx_cta->arrive_and_wait(); }
+static std::atomic<int> hx_or;
+static inline int __syncthreads_or(int p)
+{
+    hx_cta->arrive_and_wait();
+    if (threadIdx.x == 0) hx_or = 0;
+    hx_cta->arrive_and_wait();
+    if (p) hx_or |= 1;
+    hx_cta->arrive_and_wait();
+    return hx_or.load();
+}
+static std::atomic<unsigned> hx_ballot;
+static inline unsigned __ballot_sync(unsigned, int p)
+{
+    hx_warp0->arrive_and_wait();
+    if (threadIdx.x == 0) hx_ballot = 0;
+    hx_warp0->arrive_and_wait();
+    if (p) hx_ballot |= 1u << (threadIdx.x & 31);
+    hx_warp0->arrive_and_wait();
+    return hx_ballot.load();
+}
+static unsigned long long hx_shfl;
+static inline unsigned long long __shfl_sync(unsigned, unsigned long long v, int)
+{
+    hx_warp0->arrive_and_wait();
+    if (threadIdx.x == 0) hx_shfl = v;
+    hx_warp0->arrive_and_wait();
+    const unsigned long long r = hx_shfl;
+    hx_warp0->arrive_and_wait();
+    return r;
+}
+template <class T> static inline T __ldg(const T *p) { return *p; }
+#define __launch_bounds__(...)
+#ifndef __noinline__
+#define __noinline__ __attribute__((noinline))
+#endif
+namespace dg { double dg_smem[1 << 16]; }  /* the CTA's dynamic shared memory */
+%(split_source)s
+'''
 
+DRIVER_SPLIT_LAUNCH = r'''
+constexpr int NP = 4;
 template <bool MIXED>
 static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned long long *queue)
 {
+    static_assert(dg::SplitLayout<Net, NP, MIXED>::bytes() <= sizeof(dg::dg_smem), "shared memory");
+    blockIdx.x = 0;
+    gridDim.x = 1;
+    blockDim.x = 32 * NP;
+    hx_barrier cta(32 * NP), warp0(32);
+    hx_cta = &cta;
+    hx_warp0 = &warp0;
+    std::vector<std::thread> lanes;
+    for (unsigned t = 0; t < 32 * NP; t++)
+        lanes.emplace_back([=]() {
+            threadIdx.x = t;
+            dg::evolve_split_kernel<Net, NP, MIXED>(io, ts, cfg, queue);
+        });
+    for (auto &th : lanes) th.join();
+}
+'''
+
+DRIVER_LANE_LAUNCH = r'''
+template <bool MIXED>
+static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned long long *queue)
+{
+    constexpr int B = 32;
     static_assert(dg::Lane<Net, B, MIXED>::SLOTS * B <= (1 << 16), "host shared memory");
     blockIdx.x = 0;
     gridDim.x = 1;
@@ -76,6 +200,13 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
         dg::evolve_kernel<Net, B, MIXED>(io, ts, cfg, queue);
     }
 }
+'''
+
+DRIVER = r'''
+using Net = dgnet_%(name)s::Net;
+constexpr int NN = Net::N;
+constexpr int NT = Net::NT;
+%(launch)s
 
 static void launch(bool mixed, dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg,
                    unsigned long long *queue)
@@ -148,20 +279,39 @@ def _cut_net(name):
     return "namespace dgnet_%s {\n%s\n}\n" % (name, m.group(0))
 
 
-def build(name, out_dir, strict=False):
-    """Compile the host engine for network ``name`` into ``out_dir``;
-    returns the ctypes library."""
+def build(name, out_dir, strict=False, engine="lane"):
+    """Compile the host engine (``engine`` "lane" or "split") for network
+    ``name`` into ``out_dir``; returns the ctypes library."""
+    lib = C.CDLL(compile_engine(name, out_dir, strict, engine))
+    return _bind(lib)
+
+
+def compile_engine(name, out_dir, strict=False, engine="lane"):
     from dengo_gb300.build import network_dir
-    src = os.path.join(str(out_dir), "hx_%s.cpp" % name)
+    tag = "%s_%s%s" % (name, engine, "_strict" if strict else "")
+    src = os.path.join(str(out_dir), "hx_%s.cpp" % tag)
+    if engine == "split":
+        # The kernel's block-shared scalars (``__shared__ int s_any;``) become
+        # statics: one CTA runs at a time, and its lanes are threads that
+        # must see one copy.  (The dynamic array is dg::dg_smem above.)
+        with open(os.path.join(CSRC, "dg_split.cuh")) as f:
+            split_source = re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
+        prelude, launch = (PRELUDE_SPLIT.replace("%(split_source)s", split_source),
+                           DRIVER_SPLIT_LAUNCH)
+    else:
+        prelude, launch = PRELUDE, DRIVER_LANE_LAUNCH
     with open(src, "w") as f:
-        f.write(PRELUDE + '#include "%s_solver.h"\n' % name + _cut_net(name) +
-                DRIVER % dict(name=name))
-    so = os.path.join(str(out_dir), "hx_%s%s.so" % (name, "_strict" if strict else ""))
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
-                           "-w", "-DDG_MIXED_STRICT=%d" % int(strict), "-I", CUDA_INCLUDE,
-                           "-I", CSRC, "-I", os.path.join(ROOT, "include"),
+        f.write(prelude + '#include "%s_solver.h"\n' % name + _cut_net(name) +
+                DRIVER % dict(name=name, launch=launch))
+    so = os.path.join(str(out_dir), "hx_%s.so" % tag)
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                           "-w", "-pthread", "-DDG_MIXED_STRICT=%d" % int(strict),
+                           "-I", CUDA_INCLUDE, "-I", CSRC, "-I", os.path.join(ROOT, "include"),
                            "-I", network_dir(name), src, "-o", so])
-    lib = C.CDLL(so)
+    return so
+
+
+def _bind(lib):
     lib.hx_evolve.restype = C.c_int
     lib.hx_evolve.argtypes = [P_D, P_D, P_D, C.c_longlong, C.c_double, C.c_double, C.c_int,
                               C.c_int, C.c_int, C.c_int, C.POINTER(P_D), P_I, P_I, P_I, P_I,
@@ -190,3 +340,26 @@ def evolve(lib, tables, state, dtf, z=-1.0, mixed=False, queue=True, sweep_budge
         ip(out["substeps"]), ip(out["sweeps"]), ip(out["failures"]),
         out["ttot"].ctypes.data_as(P_D), out["dt"].ctypes.data_as(P_D))
     return out
+
+
+def evolve_in_subprocess(so, tables, state, dtf, timeout=600, **kw):
+    """``evolve`` with the library at path ``so``, run in a child process
+    that is killed after ``timeout`` seconds (a host build of a kernel that
+    waits on a barrier forever must not hang the test run)."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        inp, out = os.path.join(d, "in.npz"), os.path.join(d, "out.npz")
+        np.savez(inp, state=state, dtf=np.broadcast_to(np.asarray(dtf, np.float64),
+                                                       (len(state),)),
+                 **{"table%d" % k: t for k, t in enumerate(tables)})
+        code = ("import sys, json, ctypes, numpy as np; sys.path.insert(0, %r); "
+                "import host_engine as he; a = np.load(%r); "
+                "tabs = [a['table%%d' %% k] for k in range(%d)]; "
+                "r = he.evolve(he._bind(ctypes.CDLL(%r)), tabs, a['state'], a['dtf'], **%r); "
+                "np.savez(%r, **r)" % (os.path.dirname(os.path.abspath(__file__)), inp,
+                                       len(tables), so, kw, out))
+        subprocess.run([sys.executable, "-c", code], check=True, timeout=timeout)
+        with np.load(out) as r:
+            return {k: r[k] for k in r.files}

@@ -1,0 +1,75 @@
+"""The split CUDA engine (dg_split.cuh: 32 cells per CTA, each cell's sweep
+shared by 4 warps -- the default engine) compiled for the host, its 128
+lanes run as threads that meet at barriers (tests/host_engine.py), against
+the single-lane engine compiled the same way: the two must agree bit for bit,
+as they do on the GPU.  This covers the split engine's FP64 and mixed paths,
+its suspension and resumption under a sweep budget, and its strict-mixed
+variant, which no GPU has run yet.  Each solve runs in a child process with
+a time limit."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import host_engine as he
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def tables():
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    with open(os.path.join(ROOT, "tests", "golden", "primordial_expressions.json")) as f:
+        order = json.load(f)["tables"]
+    t = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
+    return [np.ascontiguousarray(t[k]) for k in order]
+
+
+@pytest.fixture(scope="module")
+def libs(tmp_path_factory):
+    d = tmp_path_factory.mktemp("split_engine")
+    return {"split": he.compile_engine("primordial", d, engine="split"),
+            "split_strict": he.compile_engine("primordial", d, strict=True, engine="split"),
+            "lane": he.build("primordial", d),
+            "lane_strict": he.build("primordial", d, strict=True)}
+
+
+def _same(a, b):
+    for k in ("state", "atol", "dt", "ttot"):
+        assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k
+    for k in ("status", "substeps", "sweeps", "failures"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_split_equals_lane(libs, tables, mixed):
+    """32 cold cells (a few hundred sweeps each), one launch and with a
+    sweep budget of 100 (cells set aside and resumed twice)."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(32, "cold", seed=11)
+    lane = he.evolve(libs["lane"], tables, st, dtf, mixed=mixed)
+    split = he.evolve_in_subprocess(libs["split"], tables, st, dtf, timeout=600, mixed=mixed)
+    _same(split, lane)
+    budget = he.evolve_in_subprocess(libs["split"], tables, st, dtf, timeout=600, mixed=mixed,
+                                     sweep_budget=100)
+    assert budget["resumed"] > 0
+    _same(budget, lane)
+
+
+def test_split_strict_equals_lane_strict(libs, tables):
+    """Three config-3 cells whose mixed refinement sometimes stops short of
+    2^-40: the strict split engine hands those systems to the FP64
+    elimination exactly as the strict single-lane engine does (and so ends
+    differently from the default build)."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(256, "config3", seed=78)
+    pick = [8, 174, 218]
+    st, dtf = st[pick], dtf[pick]
+    lane = he.evolve(libs["lane_strict"], tables, st, dtf, mixed=True)
+    split = he.evolve_in_subprocess(libs["split_strict"], tables, st, dtf, timeout=900,
+                                    mixed=True)
+    _same(split, lane)
+    default = he.evolve(libs["lane"], tables, st, dtf, mixed=True)
+    assert not np.array_equal(default["state"].view(np.int64), lane["state"].view(np.int64))
