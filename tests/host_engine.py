@@ -83,10 +83,10 @@ static inline unsigned int __float_as_uint(float f) { unsigned int u; memcpy(&u,
 static inline int __clz(unsigned int x) { return x ? __builtin_clz(x) : 32; }
 static inline double __fma_rn(double a, double b, double c) { return fma(a, b, c); }
 static std::mutex hx_atomic_lock;
-static inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v)
+template <class T> static inline T atomicAdd(T *p, T v)
 {
     std::lock_guard<std::mutex> g(hx_atomic_lock);
-    const unsigned long long o = *p;
+    const T o = *p;
     *p += v;
     return o;
 }
@@ -102,6 +102,13 @@ static inline int atomicMax(int *p, int v)
     std::lock_guard<std::mutex> g(hx_atomic_lock);
     const int o = *p;
     if (v > o) *p = v;
+    return o;
+}
+static inline int atomicMin(int *p, int v)
+{
+    std::lock_guard<std::mutex> g(hx_atomic_lock);
+    const int o = *p;
+    if (v < o) *p = v;
     return o;
 }
 /* A reusable barrier whose waiters yield the core (the lanes far outnumber
@@ -161,7 +168,7 @@ template <class T> static inline T __ldg(const T *p) { return *p; }
 #define __noinline__ __attribute__((noinline))
 #endif
 namespace dg { double dg_smem[1 << 16]; }  /* the CTA's dynamic shared memory */
-%(split_source)s
+%(kernel_source)s
 '''
 
 DRIVER_SPLIT_LAUNCH = r'''
@@ -199,6 +206,59 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
         threadIdx.x = t;
         dg::evolve_kernel<Net, B, MIXED>(io, ts, cfg, queue);
     }
+}
+'''
+
+DRIVER_STRIP = r'''
+using Net = dgnet_%(name)s::Net;
+constexpr int NN = Net::N;
+constexpr int NT = Net::NT;
+
+/* <n>_run_strip (dg_api.cuh): the Cython driver's loop on one strip of
+ * number densities, one CTA of ceil(nstrip / 32) x 32 lanes. */
+extern "C" int hx_run_strip(double *input, const double *rtol, double *atol, int nstrip,
+                            double tf, int niter, double z, const double *const *tables,
+                            double *ttot, double *dt, double *traj, double *traj_T,
+                            unsigned char *traj_ok, double *traj_t, double *traj_dt)
+{
+    static Net::Data data;
+    Net::setup_bins(&data);
+    const int nbins = Net::NT_LEN - 1;
+    std::vector<double2> pairs((size_t)nbins * NT);
+    for (int b = 0; b < nbins; b++)
+        for (int k = 0; k < NT; k++)
+            pairs[(size_t)b * NT + k] = make_double2(tables[k][b], tables[k][b + 1] - tables[k][b]);
+    std::vector<double> zvals(NT, 0.0);
+    dg::TableSet ts{pairs.data(), zvals.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
+                    data.bounds[0], data.bounds[1], z};
+    double sc[3] = {0, 0, 0};
+    int iters[16] = {0};
+    dg::RunOut o{};
+    o.ttot = sc;
+    o.dt = sc + 1;
+    o.iters = iters;
+    o.traj = traj;
+    o.traj_T = traj_T;
+    o.traj_ok = traj_ok;
+    o.traj_t = traj_t;
+    o.traj_dt = traj_dt;
+    const int threads = ((nstrip + 31) / 32) * 32;
+    blockIdx.x = 0;
+    gridDim.x = 1;
+    blockDim.x = threads;
+    hx_barrier cta(threads), warp0(32);
+    hx_cta = &cta;
+    hx_warp0 = &warp0;
+    std::vector<std::thread> lanes;
+    for (int t = 0; t < threads; t++)
+        lanes.emplace_back([=]() {
+            threadIdx.x = t;
+            dg::run_strip_kernel<Net>(input, rtol, atol, nstrip, tf, niter, ts, 10, o);
+        });
+    for (auto &th : lanes) th.join();
+    *ttot = sc[0];
+    *dt = sc[1];
+    return iters[0];
 }
 '''
 
@@ -290,19 +350,19 @@ def compile_engine(name, out_dir, strict=False, engine="lane"):
     from dengo_gb300.build import network_dir
     tag = "%s_%s%s" % (name, engine, "_strict" if strict else "")
     src = os.path.join(str(out_dir), "hx_%s.cpp" % tag)
-    if engine == "split":
+    if engine in ("split", "strip"):
         # The kernel's block-shared scalars (``__shared__ int s_any;``) become
         # statics: one CTA runs at a time, and its lanes are threads that
         # must see one copy.  (The dynamic array is dg::dg_smem above.)
-        with open(os.path.join(CSRC, "dg_split.cuh")) as f:
-            split_source = re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
-        prelude, launch = (PRELUDE_SPLIT.replace("%(split_source)s", split_source),
-                           DRIVER_SPLIT_LAUNCH)
+        with open(os.path.join(CSRC, "dg_%s.cuh" % engine)) as f:
+            kernel_source = re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
+        prelude = PRELUDE_SPLIT.replace("%(kernel_source)s", kernel_source)
+        driver = (DRIVER_STRIP % dict(name=name) if engine == "strip" else
+                  DRIVER % dict(name=name, launch=DRIVER_SPLIT_LAUNCH))
     else:
-        prelude, launch = PRELUDE, DRIVER_LANE_LAUNCH
+        prelude, driver = PRELUDE, DRIVER % dict(name=name, launch=DRIVER_LANE_LAUNCH)
     with open(src, "w") as f:
-        f.write(prelude + '#include "%s_solver.h"\n' % name + _cut_net(name) +
-                DRIVER % dict(name=name, launch=launch))
+        f.write(prelude + '#include "%s_solver.h"\n' % name + _cut_net(name) + driver)
     so = os.path.join(str(out_dir), "hx_%s.so" % tag)
     subprocess.check_call(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
                            "-w", "-pthread", "-DDG_MIXED_STRICT=%d" % int(strict),
@@ -360,6 +420,48 @@ def evolve_in_subprocess(so, tables, state, dtf, timeout=600, **kw):
                 "r = he.evolve(he._bind(ctypes.CDLL(%r)), tabs, a['state'], a['dtf'], **%r); "
                 "np.savez(%r, **r)" % (os.path.dirname(os.path.abspath(__file__)), inp,
                                        len(tables), so, kw, out))
+        subprocess.run([sys.executable, "-c", code], check=True, timeout=timeout)
+        with np.load(out) as r:
+            return {k: r[k] for k in r.files}
+
+
+def run_strip_in_subprocess(so, tables, input_number, tf, niter, z=-1.0, timeout=600):
+    """``<n>_run_strip`` (the Cython driver's loop, run_strip_kernel) from the
+    host build at path ``so`` on one strip of number densities, in a child
+    process killed after ``timeout`` seconds.  Returns the final state,
+    atol, ttot, dt, iterations and the per-iteration arrays (``traj``
+    [niter][cells][N], ``traj_T`` [niter][cells], ``successful``, ``t``,
+    ``dt_traj``)."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        inp, out = os.path.join(d, "in.npz"), os.path.join(d, "out.npz")
+        np.savez(inp, state=input_number, **{"table%d" % k: t for k, t in enumerate(tables)})
+        code = r'''
+import ctypes as C, numpy as np
+a = np.load(%(inp)r)
+tabs = [np.ascontiguousarray(a["table%%d" %% k]) for k in range(%(nt)d)]
+P = C.POINTER(C.c_double)
+lib = C.CDLL(%(so)r)
+f = lib.hx_run_strip
+f.restype = C.c_int
+f.argtypes = [P, P, P, C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(P), P, P, P, P,
+              C.c_void_p, P, P]
+st = np.ascontiguousarray(a["state"], np.float64).copy()
+dims, n = st.shape
+rt = np.full_like(st, 1e-06)
+at = st * 1e-06
+ttot, dt = np.zeros(1), np.zeros(1)
+traj, traj_T = np.zeros((%(niter)d, dims, n)), np.zeros((%(niter)d, dims))
+ok, t, dtt = np.zeros(%(niter)d, np.uint8), np.zeros(%(niter)d), np.zeros(%(niter)d)
+tp = (P * len(tabs))(*[x.ctypes.data_as(P) for x in tabs])
+p = lambda x: x.ctypes.data_as(P)
+it = f(p(st), p(rt), p(at), dims, %(tf)r, %(niter)d, %(z)r, tp, p(ttot), p(dt), p(traj),
+       p(traj_T), ok.ctypes.data, p(t), p(dtt))
+np.savez(%(out)r, state=st, atol=at, ttot=ttot[0], dt=dt[0], iterations=it, traj=traj,
+         traj_T=traj_T, successful=ok.astype(bool), t=t, dt_traj=dtt)
+''' % dict(inp=inp, nt=len(tables), so=so, niter=int(niter), tf=float(tf), z=float(z), out=out)
         subprocess.run([sys.executable, "-c", code], check=True, timeout=timeout)
         with np.load(out) as r:
             return {k: r[k] for k in r.files}

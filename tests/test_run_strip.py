@@ -120,3 +120,35 @@ def test_main_driver_matches_evolve(solver, tmp_path):
         assert np.array_equal(sol[s].view(np.int64), ref[:, j].view(np.int64)), s
     assert sol["time"][0] == ttot and sol["timestep"][0] == dt
     assert np.array_equal(sol["T"], solver.temperature_from_mass_density(ref))
+
+
+@pytest.fixture(scope="module")
+def strip_so(tmp_path_factory):
+    import host_engine as he
+    return he.compile_engine("primordial", tmp_path_factory.mktemp("strip"), engine="strip")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_run_strip_kernel_on_host_matches_reference_cython_driver(tables_in_order, case,
+                                                                  strip_so):
+    """run_strip_kernel (dg_strip.cuh, the GPU's <n>_run_strip) compiled for
+    the host from its own source (tests/host_engine.py, its lanes as threads
+    at barriers) against the reference's own Cython driver: final values and
+    every per-iteration array, bit for bit."""
+    import os
+    import platform
+    import host_engine as he
+    if platform.machine() != "x86_64":
+        pytest.skip("the goldens were made on x86-64")
+    so = strip_so
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "primordial_run_golden.npz"))
+    tf, niter = g["cases"][case]
+    r = he.run_strip_in_subprocess(so, tables_in_order, g["ics"] / W, tf, int(niter), timeout=600)
+    ige = PRIMORDIAL_ORDER.index("ge")
+    got = dict(rv=r["state"] * W, successful=r["successful"], t=r["t"], dt=r["dt_traj"],
+               T=r["traj_T"].T, ge=r["traj"][:, :, ige].T)
+    for key, a in got.items():
+        b = np.ascontiguousarray(g["run%d_%s" % (case, key)])
+        a = np.ascontiguousarray(a, b.dtype)
+        assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), key
+    assert int(r["iterations"]) == int(np.count_nonzero(g["run%d_dt" % case]))
