@@ -9,6 +9,7 @@
 #ifndef PRIMORDIAL_COMPTON_SOLVER_H
 #define PRIMORDIAL_COMPTON_SOLVER_H
 
+#define DENGO_GENERATED_HEADER 1
 #include "dengo_gb300.h"
 
 #define MAX_NCELLS DENGO_MAX_NCELLS

@@ -236,8 +236,13 @@ int BE_chem_solve(rhs_f f, jac_f J, double *u, double dt, double *rtol,
                   double *atol, int nstrip, int nchem, double *scaling,
                   void *sdata, double *u0, double *s, double *gu, double *Ju);
 
+/* The primordial network's entry points, for callers that include this
+ * header alone; a generated <n>_solver.h declares its own network instead
+ * (so that no declaration is repeated, which C99 does not allow). */
+#ifndef DENGO_GENERATED_HEADER
 DENGO_DECLARE_NETWORK(primordial)
 DENGO_DECLARE_NETWORK_NOALLOC(primordial)
+#endif
 
 #ifdef __cplusplus
 }

@@ -57,3 +57,56 @@ def test_runtime_fails_loudly_without_library(tmp_path):
     from dengo_gb300.runtime import load_library
     with pytest.raises(RuntimeError, match="not built"):
         load_library("primordial", path=str(tmp_path / "missing.so"))
+
+
+HOST_C = r'''
+/* An Enzo-style host code, as INTEGRATION.md shows it: plain C99 against the
+ * generated header, linked with the network library. */
+#include <stdio.h>
+#include "primordial_solver.h"
+
+int evolve_grid(double dtf, double z, double *fields, double *rtol, double *atol,
+                long long ncells)
+{
+    int nf = 0;
+    char **names = NULL;
+    primordial_data *data = primordial_setup_data(&nf, &names);
+    if (!data) {
+        fprintf(stderr, "%s\n", primordial_last_error());
+        return -1;
+    }
+    double dt = -1.0;
+    double ttot = dengo_evolve_primordial(dtf, &dt, z, fields, rtol, atol, ncells, data);
+    dengo_cell_batch b = {0};
+    b.ncells = ncells;
+    b.cell_stride = 10;
+    b.species_stride = 1;
+    b.state = fields;
+    b.atol = atol;
+    b.rtol_scalar = 1e-6;
+    b.dtf_scalar = dtf;
+    dengo_solver_config cfg;
+    dengo_default_config(&cfg);
+    cfg.precision = DENGO_MIXED;
+    int rc = primordial_solve_cells_host(data, &b, z, &cfg);
+    primordial_free_data(data);
+    return (ttot < dtf || rc != 0) ? 1 : 0;
+}
+
+int main(void) { return 0; }
+'''
+
+
+def test_header_serves_a_c99_host_code(libpath, tmp_path):
+    """A C99 program using the reference's entry points and the batch API
+    compiles against the generated header and links against the library
+    (nothing is run: that needs a GPU)."""
+    from dengo_gb300.build import network_dir
+    src = tmp_path / "host.c"
+    src.write_text(HOST_C)
+    exe = tmp_path / "host"
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic",
+                           "-I", os.path.join(ROOT, "include"), "-I", network_dir("primordial"),
+                           str(src), "-o", str(exe), "-L", os.path.dirname(libpath),
+                           "-lprimordial_solver", "-Wl,-rpath," + os.path.dirname(libpath)])
+    assert exe.exists()
