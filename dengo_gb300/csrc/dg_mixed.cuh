@@ -28,16 +28,18 @@
  * false and the caller runs the FP64 elimination instead (which then
  * reproduces the reference's NaN propagation).
  *
- * Built with DG_MIXED_STRICT=1, a refinement that ends without meeting the
- * 2^-40 criterion (its correction stopped halving, or MAX_REFINE steps were
- * taken) also hands the system to the FP64 elimination; by default such a
- * solution is kept and Newton's own convergence test judges the sweep.
+ * A refinement that ends without meeting the 2^-40 criterion (its
+ * correction stopped halving, or MAX_REFINE steps were taken) also hands the
+ * system to the FP64 elimination, so no solve is kept less accurate than the
+ * FP64 path's.  In the solver's own Newton systems that happens in well under
+ * 0.1 % of solves.  Built with DG_MIXED_STRICT=0 such a solution is kept
+ * instead and Newton's convergence test judges the sweep.
  */
 #ifndef DG_MIXED_CUH
 #define DG_MIXED_CUH
 
 #ifndef DG_MIXED_STRICT
-#define DG_MIXED_STRICT 0
+#define DG_MIXED_STRICT 1
 #endif
 
 #include "dg_math.h"
@@ -287,8 +289,8 @@ struct MixedSolve {
         return ed == 0 || ed <= ex - 40;
     }
 
-    /* x = A^-1 g; false: A or g holds inf/NaN or the FP32 solve broke down
-     * (with DG_MIXED_STRICT also: the refinement stopped short of 2^-40),
+    /* x = A^-1 g; false: A or g holds inf/NaN, the FP32 solve broke down
+     * or (unless DG_MIXED_STRICT=0) the refinement stopped short of 2^-40;
      * x undefined, A and g untouched. */
     __device__ __forceinline__ bool operator()(const double (&g)[N], double (&x)[N]) const
     {

@@ -339,16 +339,16 @@ def _cut_net(name):
     return "namespace dgnet_%s {\n%s\n}\n" % (name, m.group(0))
 
 
-def build(name, out_dir, strict=False, engine="lane"):
+def build(name, out_dir, strict=True, engine="lane"):
     """Compile the host engine (``engine`` "lane" or "split") for network
     ``name`` into ``out_dir``; returns the ctypes library."""
     lib = C.CDLL(compile_engine(name, out_dir, strict, engine))
     return _bind(lib)
 
 
-def compile_engine(name, out_dir, strict=False, engine="lane"):
+def compile_engine(name, out_dir, strict=True, engine="lane"):
     from dengo_gb300.build import network_dir
-    tag = "%s_%s%s" % (name, engine, "_strict" if strict else "")
+    tag = "%s_%s%s" % (name, engine, "" if strict else "_lenient")
     src = os.path.join(str(out_dir), "hx_%s.cpp" % tag)
     if engine in ("split", "strip"):
         # The kernel's block-shared scalars (``__shared__ int s_any;``) become

@@ -1,7 +1,8 @@
 """The single-lane CUDA engine compiled for the host (tests/host_engine.py)
 against the oracle: the GPU tests' parity checks, run on the CPU from the
-kernel's own source -- the FP64 path, the mixed path (default and strict
-builds), the three-launch stiff-cell redistribution, and the Compton
+kernel's own source -- the FP64 path, the mixed path (the shipped build,
+and the lenient one that keeps unfinished refinements), the three-launch
+stiff-cell redistribution, and the Compton
 network at several redshifts."""
 import json
 import os
@@ -18,7 +19,8 @@ RTOL = 1e-10
 @pytest.fixture(scope="module")
 def engines(tmp_path_factory):
     d = tmp_path_factory.mktemp("host_engine")
-    return {"default": he.build("primordial", d), "strict": he.build("primordial", d, strict=True)}
+    return {"default": he.build("primordial", d),
+            "lenient": he.build("primordial", d, strict=False)}
 
 
 @pytest.fixture(scope="module")
@@ -81,7 +83,7 @@ def test_redistribution_is_bit_identical(engines, tables, mixed, budget):
         assert np.array_equal(one[k], three[k]), k
 
 
-@pytest.mark.parametrize("build", ["default", "strict"])
+@pytest.mark.parametrize("build", ["default", "lenient"])
 @pytest.mark.parametrize("config,seed,n,min_frac", [("config1", 404, 96, 1.0),
                                                      ("config3", 407, 128, 0.97)])
 def test_mixed_engine_within_1e6(engines, tables, crlog_oracle, build, config, seed, n, min_frac):
@@ -100,16 +102,16 @@ def test_mixed_engine_within_1e6(engines, tables, crlog_oracle, build, config, s
     assert np.mean(err.max(axis=1) <= 1e-6) >= min_frac
 
 
-def test_strict_build_changes_almost_nothing_in_real_solves(engines, tables):
-    """On 256 config-3 cells the strict mixed build (refinements that stop
+def test_fp64_fallback_for_unfinished_refinements_changes_almost_nothing(engines, tables):
+    """On 256 config-3 cells the shipped mixed build (refinements that stop
     short of 2^-40 handed to the FP64 elimination) ends every cell with the
-    default build's status and sweep count, and with its state on all but
-    a few cells: in the solver's own Newton systems the refinement almost
+    lenient build's status and sweep count, and with its state on all but a
+    few cells: in the solver's own Newton systems the refinement almost
     always meets its criterion."""
     from dengo_gb300.workloads import primordial_cells
     st, dtf = primordial_cells(256, "config3", seed=77)
-    a = he.evolve(engines["default"], tables, st, dtf, mixed=True)
-    b = he.evolve(engines["strict"], tables, st, dtf, mixed=True)
+    a = he.evolve(engines["lenient"], tables, st, dtf, mixed=True)
+    b = he.evolve(engines["default"], tables, st, dtf, mixed=True)
     assert np.array_equal(a["status"], b["status"])
     assert np.array_equal(a["sweeps"], b["sweeps"])
     differ = ~np.all(a["state"].view(np.int64) == b["state"].view(np.int64), axis=1)

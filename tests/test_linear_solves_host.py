@@ -126,11 +126,14 @@ def _cut(path, pattern):
 
 @pytest.fixture(scope="module")
 def hx(tmp_path_factory):
+    """Built with DG_MIXED_STRICT=0: MixedSolve keeps a refinement that stops
+    short, so its solutions can be studied."""
     return _build_hx(tmp_path_factory, strict=False)
 
 
 @pytest.fixture(scope="module")
 def hx_strict(tmp_path_factory):
+    """The shipped build."""
     return _build_hx(tmp_path_factory, strict=True)
 
 
@@ -265,9 +268,9 @@ def test_mixed_solve_accuracy_where_refinement_converges(hx):
     (most systems), the refined FP32 solve is within 2^-38 of the exact
     solution's largest component, or no further from it than FP64
     elimination.  The loop the harness runs is MixedSolve's own (same
-    solution bits).  Where it stops early -- the correction stopped halving,
-    or four steps were taken -- the engine currently keeps the solution; on
-    these seeded systems that is about one in six, some of them far off."""
+    solution bits, lenient build).  On these harsh seeded systems it stops
+    early on about one in six, some far off: the shipped build hands those
+    to the FP64 elimination (next test)."""
     counts = [0, 0, 0, 0]
     for A, g in _newton_matrices(hx, count=120):
         xm, xs = np.zeros(N), np.zeros(N)
@@ -290,10 +293,10 @@ def test_mixed_solve_accuracy_where_refinement_converges(hx):
     assert counts[0] == 0 and counts[1] >= 0.7 * sum(counts), counts
 
 
-def test_strict_build_hands_unfinished_refinements_to_fp64(hx, hx_strict):
-    """Built with DG_MIXED_STRICT=1 the solve declines (so the engine runs
-    the FP64 elimination) exactly the systems whose refinement stopped short
-    of 2^-40, and returns the same bits as the default build on the rest."""
+def test_shipped_build_hands_unfinished_refinements_to_fp64(hx, hx_strict):
+    """The shipped build (DG_MIXED_STRICT=1) declines -- so the engine runs
+    the FP64 elimination -- exactly the systems whose refinement stopped
+    short of 2^-40, and returns the lenient build's bits on the rest."""
     seen = set()
     for A, g in _newton_matrices(hx, count=120):
         x0, x1 = np.zeros(N), np.zeros(N)
