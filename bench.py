@@ -165,6 +165,18 @@ def cpu_baseline(state, dtf, seconds, nthreads=0):
                       "%.1f s wall" % (m, elapsed)}, res, m
 
 
+def metric_name(precision):
+    """The metric both arms report."""
+    return ("converged cell-steps/s (primordial, per-cell BE Newton, %s path)"
+            % ("FP64 plain" if precision == "fp64" else "mixed FP32-LU"))
+
+
+def workload_name(cells, steps):
+    return ("primordial network, %d cells per GPU drawn from the 128^3 configuration's "
+            "distributions, %d consecutive hydro steps, state resident on the device"
+            % (cells, steps))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -194,13 +206,14 @@ def run_reference(args):
         ok_total += int((r["status"] == 0).sum())
         cur = r["state"]
     value = ok_total / t_total
-    line = {"impl": "reference", "metric": "converged cell-steps/s (primordial, per-cell BE Newton)",
+    line = {"impl": "reference", "metric": metric_name("fp64"),
             "value": value, "unit": "cells/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": "%s-distribution primordial cells, %d-cell seeded sample per "
-                                   "step on the host cores" % (args.config, m),
+            "config": {"workload": workload_name(args.cells, args.steps),
+                       "sample": "%d of the cells per step (%s distributions), on the host "
+                                 "cores" % (m, args.config),
                        "cells_per_step": m},
             "cpu_baseline": dict(base, value=value,
                                  sample="%d cells per step x %d steps" % (m, args.steps)),
@@ -337,16 +350,13 @@ def run_ours(args):
     peak = measure_fp64_peak()
     achieved = flops / (total_ms / 1e3) / 1e12
     line = {
-        "metric": "converged cell-steps/s (primordial, per-cell BE Newton, %s path)"
-                  % ("FP64 plain" if args.precision == "fp64" else "mixed FP32-LU"),
+        "metric": metric_name(args.precision),
         "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f64 residual + f32 LU",
         "data": "synthetic (seeded)",
-        "config": {"workload": "primordial network, %d cells per GPU drawn from the 128^3 "
-                               "configuration's distributions, %d consecutive hydro steps, "
-                               "state resident on the device" % (n, args.steps),
+        "config": {"workload": workload_name(n, args.steps),
                    "cells_per_gpu": n, "precision": args.precision, "schedule": args.schedule,
                    "order": "costliest first" if args.order else "input order",
                    "warps_per_cell": args.warps_per_cell,
