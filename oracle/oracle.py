@@ -45,6 +45,20 @@ def _dp(a):
     return a.ctypes.data_as(P_D)
 
 
+_STRIP_F = C.CFUNCTYPE(C.c_int, P_D, P_D, C.c_int, C.c_int, C.c_void_p)
+
+
+class Network(C.Structure):
+    """``dgo_network`` (be_oracle.h): one network's strip functions."""
+    _fields_ = [("name", C.c_char_p), ("nchem", C.c_int), ("ige", C.c_int), ("unit", P_D),
+                ("input_is_number", C.c_int), ("rhs", _STRIP_F), ("jac", _STRIP_F),
+                ("electrons", C.CFUNCTYPE(None, P_D, C.c_int, C.c_int)),
+                ("alloc_data", C.CFUNCTYPE(C.c_void_p, C.POINTER(P_D))),
+                ("free_data", C.CFUNCTYPE(None, C.c_void_p)),
+                ("set_z", C.CFUNCTYPE(None, C.c_void_p, C.c_double)),
+                ("Ts", C.CFUNCTYPE(P_D, C.c_void_p))]
+
+
 class Oracle:
     """The C restatement of the reference solver for one network."""
 
@@ -101,6 +115,26 @@ class Oracle:
 class Stats(C.Structure):
     _fields_ = [("substeps_ok", C.c_longlong), ("substeps_fail", C.c_longlong),
                 ("sweeps", C.c_longlong), ("status", C.c_int)]
+
+
+def evolve_strip(orc, tables_in_order, state, dtf, z=-1.0, dt=-1.0):
+    """dengo_evolve_<name> over one strip in lockstep (dims = the number of
+    cells; the reference's own semantics for dims > 1): one dt and one
+    Newton loop for the whole strip.  Returns a dict."""
+    st = np.ascontiguousarray(state, np.float64).copy()
+    rt = np.full_like(st, 1e-6)
+    at = 1e-6 * st
+    keep, tp = orc._tables(tables_in_order)
+    net = Network.in_dll(orc.lib, "dgo_%s_network" % orc.name)
+    data = net.alloc_data(tp)
+    try:
+        d = C.c_double(dt)
+        cfg = orc.config()
+        ttot = orc.lib.dgo_evolve(orc.net_addr, data, float(dtf), C.byref(d), float(z), _dp(st),
+                                  _dp(rt), _dp(at), st.shape[0], C.byref(cfg), None)
+    finally:
+        net.free_data(data)
+    return dict(state=st, atol=at, ttot=ttot, dt=d.value)
 
 
 def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0, trajectories=False):

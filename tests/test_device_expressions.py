@@ -22,19 +22,6 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 P_D = C.POINTER(C.c_double)
-_STRIP_F = C.CFUNCTYPE(C.c_int, P_D, P_D, C.c_int, C.c_int, C.c_void_p)
-
-
-class _DgoNetwork(C.Structure):
-    """``dgo_network`` (oracle/be_oracle.h)."""
-    _fields_ = [("name", C.c_char_p), ("nchem", C.c_int), ("ige", C.c_int), ("unit", P_D),
-                ("input_is_number", C.c_int), ("rhs", _STRIP_F), ("jac", _STRIP_F),
-                ("electrons", C.CFUNCTYPE(None, P_D, C.c_int, C.c_int)),
-                ("alloc_data", C.CFUNCTYPE(C.c_void_p, C.POINTER(P_D))),
-                ("free_data", C.CFUNCTYPE(None, C.c_void_p)),
-                ("set_z", C.CFUNCTYPE(None, C.c_void_p, C.c_double)),
-                ("Ts", C.CFUNCTYPE(P_D, C.c_void_p))]
-
 HARNESS = r'''
 #include <math.h>
 #define __device__
@@ -176,7 +163,8 @@ def test_device_expressions_match_oracle(name, z, tmp_path_factory):
     assert ok.all()
 
     # the oracle's strip functions (one strip of all cells)
-    onet = _DgoNetwork.in_dll(orc.lib, "dgo_%s_network" % name)
+    from oracle import Network
+    onet = Network.in_dll(orc.lib, "dgo_%s_network" % name)
     data = onet.alloc_data(tptr)
     try:
         onet.set_z(data, z)

@@ -60,3 +60,13 @@ def test_oracle_correctly_rounded_log():
     xs = np.exp(np.random.default_rng(5).uniform(0.0, np.log(2e9), 5000))
     for x in xs:
         assert lib.dgo_crlog(float(x)) == float(mpmath.log(mpmath.mpf(float(x)))), x
+
+
+def test_oracle_lockstep_strip_matches_reference(golden, tables_in_order, oracle):
+    """dengo_evolve over an 8-cell strip in lockstep (the reference's dims > 1
+    semantics: one dt, one Newton loop for the strip), bit for bit."""
+    from oracle import evolve_strip
+    g = golden
+    r = evolve_strip(oracle, tables_in_order, g["lock_in"], float(g["lock_dtf"]))
+    assert _same(r["state"], g["lock_state"]) and _same(r["atol"], g["lock_atol"])
+    assert _same(np.array(r["ttot"]), g["lock_ttot"]) and _same(np.array(r["dt"]), g["lock_dt"])
