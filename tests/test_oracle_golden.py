@@ -70,3 +70,62 @@ def test_oracle_lockstep_strip_matches_reference(golden, tables_in_order, oracle
     r = evolve_strip(oracle, tables_in_order, g["lock_in"], float(g["lock_dtf"]))
     assert _same(r["state"], g["lock_state"]) and _same(r["atol"], g["lock_atol"])
     assert _same(np.array(r["ttot"]), g["lock_ttot"]) and _same(np.array(r["dt"]), g["lock_dt"])
+
+
+def _strip(oracle, tables_in_order):
+    from oracle import Network
+    net = Network.in_dll(oracle.lib, "dgo_%s_network" % oracle.name)
+    keep, tp = oracle._tables(tables_in_order)
+    return net, net.alloc_data(tp), keep
+
+
+def test_oracle_strip_functions_match_reference(golden, tables_in_order, oracle):
+    """calculate_rhs (with its temperature and rate interpolation),
+    calculate_jacobian and ensure_electron_consistency on a 32-cell strip."""
+    import ctypes as C
+    g = golden
+    P = C.POINTER(C.c_double)
+    net, data, keep = _strip(oracle, tables_in_order)
+    try:
+        num = g["strip_in"].copy()
+        rhs = np.zeros_like(num)
+        assert net.rhs(num.ctypes.data_as(P), rhs.ctypes.data_as(P), 32, 10, data) == \
+            int(g["strip_rhs_rv"])
+        assert _same(rhs, g["strip_rhs"])
+        assert _same(np.ctypeslib.as_array(net.Ts(data), (32,)), g["strip_Ts"])
+        jac = np.zeros((32, 10, 10))
+        assert net.jac(num.ctypes.data_as(P), jac.ctypes.data_as(P), 32, 10, data) == \
+            int(g["strip_jac_rv"])
+        assert _same(jac, g["strip_jac"])
+    finally:
+        net.free_data(data)
+    el = g["strip_in"].copy()
+    net.electrons(el.ctypes.data_as(P), 32, 10)
+    assert _same(el, g["strip_electrons"])
+
+
+def test_oracle_be_chem_solve_lockstep_matches_reference(golden, tables_in_order, oracle):
+    """One BE_chem_solve over an 8-cell strip (BE_chem_solve.C:79-241)."""
+    import ctypes as C
+    from oracle import Network
+    g = golden
+    P = C.POINTER(C.c_double)
+    fn = oracle.lib.dgo_BE_chem_solve
+    fn.restype = C.c_int
+    F = Network._fields_[5][1]
+    fn.argtypes = [F, F, P, C.c_double, P, P, C.c_int, C.c_int, P, C.c_void_p, P, P, P, P,
+                   C.c_int, C.c_void_p]
+    net, data, keep = _strip(oracle, tables_in_order)
+    try:
+        u = g["be_in"].copy()
+        rtol = np.full_like(u, 1e-6)
+        atol = g["be_atol_in"].copy()
+        scale = u.copy()
+        scratch = [np.zeros(80), np.zeros(10), np.zeros(80), np.zeros(800)]
+        rv = fn(net.rhs, net.jac, u.ctypes.data_as(P), float(g["be_dt"]),
+                rtol.ctypes.data_as(P), atol.ctypes.data_as(P), 8, 10, scale.ctypes.data_as(P),
+                data, *[a.ctypes.data_as(P) for a in scratch], 10, None)
+    finally:
+        net.free_data(data)
+    assert rv == int(g["be_rv"])
+    assert _same(u, g["be_u"]) and _same(atol, g["be_atol"])
