@@ -263,6 +263,13 @@ extern "C" int hx_run_strip(double *input, const double *rtol, double *atol, int
 '''
 
 DRIVER = r'''
+/* z_values of dg_api.cuh (cut from its source) */
+template <class Net>
+struct hx_z {
+    using Data = typename Net::Data;
+    static constexpr int NT = Net::NT;
+%(z_values)s
+};
 using Net = dgnet_%(name)s::Net;
 constexpr int NN = Net::N;
 constexpr int NT = Net::NT;
@@ -288,10 +295,18 @@ extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long lo
     Net::setup_bins(&data);
     const int nbins = Net::NT_LEN - 1;
     std::vector<double2> pairs((size_t)nbins * NT);
-    for (int b = 0; b < nbins; b++)
-        for (int k = 0; k < NT; k++)
+    for (int k = 0; k < NT; k++) {
+        double *dst = Net::host_table(&data, k);
+        const int len = Net::zdep(k) ? Net::NZ_LEN : Net::NT_LEN;
+        for (int b = 0; b < len; b++) dst[b] = tables[k][b];
+        if (Net::zdep(k)) continue;
+        for (int b = 0; b < nbins; b++)
             pairs[(size_t)b * NT + k] = make_double2(tables[k][b], tables[k][b + 1] - tables[k][b]);
-    std::vector<double> zvals(NT, 0.0);
+    }
+    /* the redshift tables' values at z, as the library computes them on the
+     * host before a launch */
+    std::vector<double> zvals(NT, 0.0), dzvals(NT, 0.0);
+    hx_z<Net>::z_values(&data, z, zvals.data(), dzvals.data());
     dg::TableSet ts{pairs.data(), zvals.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
                     data.bounds[0], data.bounds[1], z};
     dg::CellIO io{state, atol, nullptr, rtol_scalar, dtf, 0.0, dt, ttot, status, substeps, sweeps,
@@ -330,6 +345,14 @@ extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long lo
 '''
 
 
+def _cut_z_values():
+    with open(os.path.join(CSRC, "dg_api.cuh")) as f:
+        src = f.read()
+    m = re.search(r"^    static void z_values\(.*?^    \}$", src, re.S | re.M)
+    assert m, "no z_values in dg_api.cuh"
+    return m.group(0)
+
+
 def _cut_net(name):
     from dengo_gb300.build import network_dir
     with open(os.path.join(network_dir(name), "%s_solver.cu" % name)) as f:
@@ -358,9 +381,10 @@ def compile_engine(name, out_dir, strict=True, engine="lane"):
             kernel_source = re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
         prelude = PRELUDE_SPLIT.replace("%(kernel_source)s", kernel_source)
         driver = (DRIVER_STRIP % dict(name=name) if engine == "strip" else
-                  DRIVER % dict(name=name, launch=DRIVER_SPLIT_LAUNCH))
+                  DRIVER % dict(name=name, launch=DRIVER_SPLIT_LAUNCH, z_values=_cut_z_values()))
     else:
-        prelude, driver = PRELUDE, DRIVER % dict(name=name, launch=DRIVER_LANE_LAUNCH)
+        prelude, driver = PRELUDE, DRIVER % dict(name=name, launch=DRIVER_LANE_LAUNCH,
+                                                 z_values=_cut_z_values())
     with open(src, "w") as f:
         f.write(prelude + '#include "%s_solver.h"\n' % name + _cut_net(name) + driver)
     so = os.path.join(str(out_dir), "hx_%s.so" % tag)
