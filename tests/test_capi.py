@@ -89,6 +89,9 @@ int evolve_grid(double dtf, double z, double *fields, double *rtol, double *atol
     dengo_default_config(&cfg);
     cfg.precision = DENGO_MIXED;
     int rc = primordial_solve_cells_host(data, &b, z, &cfg);
+    /* a GPU-resident code passes device pointers and a stream instead */
+    rc |= primordial_solve_cells_device(data, &b, z, &cfg, NULL);
+    rc |= primordial_solve_cells_device_noalloc(data, &b, z, &cfg, NULL);
     primordial_free_data(data);
     return (ttot < dtf || rc != 0) ? 1 : 0;
 }
