@@ -75,21 +75,29 @@ def test_tables_equal_reference(net, golden):
             assert np.allclose(arr, ref, rtol=1e-13, atol=0), name
 
 
-def test_generated_sources_up_to_date(net):
+SHIPPED = ("primordial", "primordial_compton", "oxygen", "oxygen_uvb")
+
+
+@pytest.mark.parametrize("name", SHIPPED)
+def test_generated_sources_up_to_date(name):
+    """The committed generated sources are what the templates render now."""
     from dengo_gb300.codegen import render_solver
-    gen = os.path.join(ROOT, "dengo_gb300", "generated", "primordial")
+    from dengo_gb300.networks import SHIPPED_NETWORKS, build_network
+    assert SHIPPED == tuple(SHIPPED_NETWORKS)
+    gen = os.path.join(ROOT, "dengo_gb300", "generated", name)
     with tempfile.TemporaryDirectory() as d:
-        for p in render_solver(net, "primordial", d):
+        for p in render_solver(build_network(name), name, d):
             with open(p) as f, open(os.path.join(gen, os.path.basename(p))) as g:
                 assert f.read() == g.read(), os.path.basename(p)
 
 
-def test_oracle_sources_up_to_date():
+@pytest.mark.parametrize("name", SHIPPED)
+def test_oracle_sources_up_to_date(name):
     import sys
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import gen_oracle
-    with open(os.path.join(ROOT, "oracle", "gen", "primordial_oracle.c")) as f:
-        assert f.read() == gen_oracle.render("primordial")
+    with open(os.path.join(ROOT, "oracle", "gen", "%s_oracle.c" % name)) as f:
+        assert f.read() == gen_oracle.render(name)
 
 
 def test_table_file_roundtrip(tmp_path):
