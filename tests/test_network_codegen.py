@@ -166,3 +166,16 @@ def test_unknown_names_raise_the_references_exceptions():
     with pytest.raises(UnknownSpecies):
         ensure_species("no_such_species")
     assert issubclass(Species, ComparableMixin)
+
+
+def test_shipped_primordial_tables_are_the_references(golden):
+    """The .dgt bundle the primordial library loads holds the reference's
+    tables, bit for bit."""
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    t = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
+    names = list(golden["table_names"])
+    assert sorted(t) == sorted(names)
+    for name in names:
+        ref = golden["tables"][names.index(name)]
+        assert np.array_equal(t[name].view(np.int64), ref.view(np.int64)), name
