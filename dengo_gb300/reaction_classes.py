@@ -31,7 +31,6 @@ the printed order.  Two details matter for that:
 
 import functools
 
-import numpy as np
 import sympy
 
 from .periodic_table import periodic_table_by_name
