@@ -2,22 +2,33 @@
 """Benchmark of the GB300 chemistry solver.
 
 Workload: the primordial network (10 equations) on seeded cells drawn from
-the 128^3 configuration's distributions (nH ~ logU(1, 1e6) cm^-3,
-T ~ logU(10, 1e8) K, dtf = 0.1 t_ff per cell, rtol = 1e-6, atol = 1e-6 x),
-SoA state resident on the device.  One "step" is one hydro step: one
-solver launch over every cell, each cell integrated to its dtf with the
-reference's per-cell backward-Euler driver; the state carries over from step
-to step (atol is reset to 1e-6 x before each step).
+the 128^3-cell configuration's distributions (nH ~ logU(1, 1e6) cm^-3,
+T ~ logU(10, 1e8) K, dtf = 0.1 t_ff per cell, rtol = 1e-6, atol = 1e-6 x);
+``--config config3`` draws the heterogeneous-stiffness population instead
+(nH ~ logU(1e-3, 1e12), T ~ logU(10, 1e9), 5 % in the thermally unstable
+band).  One "step" is one hydro step: every cell integrated to its dtf with
+the reference's per-cell backward-Euler driver; each step starts from the
+previous step's state (atol reset to 1e-6 x before each step).
 
-Metric: converged cell-steps per second -- cells whose solve ended with
-status OK, summed over the timed steps, divided by the summed device time of
-the solver launches (CUDA events on the launching stream, L2 flushed before
-every step).  A seeded sample of the first step is checked against the
-oracle (C restatement of the reference) and the fraction within 1e-6 and
-1e-10 relative is reported.
+Every timed step is one call of the C entry point
+``primordial_solve_cells_host`` with pinned host buffers: the call copies
+the step's inputs to the device, solves, and copies the results back.
+  * value: converged cell-steps per second of device time -- the solve's
+    kernels between the copies, CUDA events recorded on the call's stream
+    (``primordial_last_solve_ms``) -- counting cells whose solve ended OK and,
+    by the seeded parity sample, within 1e-6 of the FP64 oracle;
+  * e2e: the same count per second of wall time of the host calls (copies,
+    launches, synchronisation included);
+  * mixed: the same measurement with precision = DENGO_MIXED.
+L2 is flushed (a 256 MB device write) before every step, outside the call.
 
---impl reference times the reference's CPU algorithm (the oracle, the
-reference's own code when it was built here) on the host cores instead.
+Parity: the first ``--parity-sample`` cells are evolved through the same
+steps by the oracle (the C restatement of the reference, pinned bit for bit
+to the reference's own compiled solver) on the host cores; per step, cells
+the oracle solved OK (in this and every earlier step) are compared.
+
+--impl reference times the reference's CPU algorithm (the oracle) on the
+host cores on a seeded subsample of the same cells, on the same config.
 """
 import argparse
 import ctypes as C
@@ -39,6 +50,16 @@ sys.path.insert(0, ROOT)
 # generated expressions and exact LU flop count, N = 10).
 F_SWEEP = 2090.0
 NSPECIES = 10
+METRIC = "cells/s at <=1e-6 rel err vs FP64 oracle (mixed vs plain)"
+
+# DRAM bytes per cell of one solver launch, from the ncu captures of the
+# split engine on 14 592 cells (read + write; the state and tolerances, the
+# tables stay in L2).
+DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592}
+# solver kernels per hydro step with a cost hint and a sweep budget: the
+# three order kernels, the first launch, and two resume launches each after
+# two list kernels
+LAUNCHES_PER_STEP = 3 + 1 + 2 * (2 + 1)
 
 
 def parse():
@@ -48,22 +69,21 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cells", type=int, default=32768, help="cells per GPU")
-    p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--config", default="config2")
+    p.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     p.add_argument("--schedule", type=int, default=3, help="1 per-thread, 2 stride, 3 queue")
     p.add_argument("--block", type=int, default=0)
-    p.add_argument("--parity-sample", type=int, default=48)
+    p.add_argument("--parity-sample", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--order", type=int, default=1, help="start the costliest cells first")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--warps-per-cell", type=int, default=4, choices=[1, 2, 4])
     p.add_argument("--sweep-budget", type=int, default=2000,
                    help="> 0: redistribute cells still running after this many Newton "
-                        "sweeps into a second, densely packed launch (same results)")
+                        "sweeps into later, densely packed launches (same results)")
     p.add_argument("--tail-grid", type=int, default=0)
     p.add_argument("--max-substeps", type=int, default=50000,
                    help="the reference's cap; lower only to profile a short launch")
-    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-parity", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -110,12 +130,6 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-# DRAM bytes per cell of one solver launch, from the ncu captures of the
-# split engine on 14 592 cells (read + write; the state and tolerances, the
-# tables stay in L2).
-DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592}
-
-
 def temperatures(state):
     """Gas temperature of each cell (mass densities + ge), gamma = 5/3."""
     from dengo_gb300.workloads import KB, MH, PRIMORDIAL_ORDER, PRIMORDIAL_WEIGHTS
@@ -137,18 +151,46 @@ def measure_fp64_peak():
     return best
 
 
-def cpu_baseline(state, dtf, seconds, nthreads=0):
-    """The oracle on a bounded sample of the workload, all host cores."""
+def config_dict(args):
+    """The workload both arms report (identical keys and values)."""
+    return {"workload": "primordial network (10 equations), %d cells per GPU drawn from the "
+                        "%s distributions (the 128^3 = 2,097,152-cell configuration's; a full "
+                        "128^3 hydro step is minutes of device time because ~30%% of cells need "
+                        "the 50,000-substep cap, so a seeded power-of-two subsample is timed), "
+                        "%d consecutive hydro steps, per-cell dt control"
+                        % (args.cells, args.config, args.steps),
+            "network": "primordial", "cells": args.cells, "distributions": args.config,
+            "hydro_steps": args.steps, "rtol": 1e-6, "atol": "1e-6 x state",
+            "max_newton_sweeps": 10, "max_substeps": args.max_substeps,
+            "l2": "flushed (256 MB device write) before every step"}
+
+
+def oracle_tables():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
-    from dengo_gb300.tablefile import read_table_file
-    from dengo_gb300.build import network_dir
-    from dengo_gb300.runtime import load_library
-    lib = load_library("primordial")
-    order = [lib.primordial_table_name(k).decode() for k in range(lib.primordial_ntables())]
-    tabs = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
-    tables = [tabs[k] for k in order]
     orc = Oracle("primordial")
+    path = os.path.join(ROOT, "dengo_gb300", "generated", "primordial", "primordial_tables.dgt")
+    return orc, orc.tables_from_bundle(path)
+
+
+def oracle_steps(state, dtf, steps, nthreads=0):
+    """The oracle through `steps` hydro steps (atol = 1e-6 x state at each
+    step's start).  Returns per-step states and statuses and the wall time."""
+    orc, tables = oracle_tables()
+    cur = np.array(state, copy=True)
+    out, t = [], 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r = orc.evolve_cells(tables, cur, dtf, nthreads=nthreads)
+        t += time.perf_counter() - t0
+        out.append((r["state"].copy(), r["status"].copy()))
+        cur = r["state"]
+    return out, t
+
+
+def cpu_baseline(state, dtf, seconds, nthreads=0):
+    """The oracle on a bounded sample of the first step, all host cores."""
+    orc, tables = oracle_tables()
     cores = nthreads or os.cpu_count()
     m, elapsed, res = 64, 0.0, None
     while True:
@@ -161,40 +203,128 @@ def cpu_baseline(state, dtf, seconds, nthreads=0):
         m *= 2
     ok = int((res["status"] == 0).sum())
     return {"value": ok / elapsed, "unit": "cells/s", "cores": cores, "kind": "port",
-            "sample": "%d cells of the first step (seeded subsample), one hydro step each, "
-                      "%.1f s wall" % (m, elapsed)}, res, m
+            "sample": "the first %d of the cells, first hydro step, %.1f s wall" % (m, elapsed)}, m
 
 
-def metric_name(precision):
-    """The metric both arms report."""
-    return ("converged cell-steps/s (primordial, per-cell BE Newton, %s path)"
-            % ("FP64 plain" if precision == "fp64" else "mixed FP32-LU"))
+def parity(gpu_steps, ref_steps, first_in):
+    """Per step, the cells the oracle solved OK in this and every earlier
+    step: relative error (and error floored at the solve's absolute
+    tolerance, 1e-6 x the step's input) of the GPU's state."""
+    alive = np.ones(len(first_in), bool)
+    inp = first_in
+    n_ok = n_ok_gpu = n6 = n10 = nbit = 0
+    worst, worst_f = 0.0, 0.0
+    for (g_st, g_status), (r_st, r_status) in zip(gpu_steps, ref_steps):
+        alive &= r_status == 0
+        sel = alive & (g_status == 0)
+        if sel.any():
+            d = np.abs(g_st[sel] - r_st[sel])
+            with np.errstate(invalid="ignore", divide="ignore"):
+                rel = np.where(d == 0, 0.0, d / np.abs(r_st[sel]))
+                fl = np.where(d == 0, 0.0, d / np.maximum(np.abs(r_st[sel]), 1e-6 * np.abs(inp[sel])))
+            rel = np.nan_to_num(rel, nan=np.inf)
+            fl = np.nan_to_num(fl, nan=np.inf)
+            worst = max(worst, float(rel.max()))
+            worst_f = max(worst_f, float(fl.max()))
+            n6 += int(np.all(fl <= 1e-6, axis=1).sum())
+            n10 += int(np.all(rel <= 1e-10, axis=1).sum())
+            nbit += int(np.all(g_st[sel] == r_st[sel], axis=1).sum())
+        n_ok += int(alive.sum())
+        n_ok_gpu += int(sel.sum())
+        inp = r_st
+    return {"sample_cells": int(len(first_in)), "steps": len(gpu_steps),
+            "oracle_ok_cell_steps": n_ok, "gpu_ok_cell_steps": n_ok_gpu,
+            "within_1e-6": n6, "within_1e-10": n10, "bit_identical": nbit,
+            "frac_within_1e-6": (n6 / n_ok_gpu) if n_ok_gpu else None,
+            "max_rel_err": worst, "max_floored_err": worst_f}
 
 
-def workload_name(cells, steps):
-    return ("primordial network, %d cells per GPU drawn from the 128^3 configuration's "
-            "distributions, %d consecutive hydro steps, state resident on the device"
-            % (cells, steps))
+class HostArm:
+    """K hydro steps of one precision through primordial_solve_cells_host
+    with pinned host buffers."""
+
+    def __init__(self, solver, state0, dtf, args, precision, torch):
+        from dengo_gb300.runtime import CellBatch, DENGO_MIXED, DENGO_FP64
+        self.solver, self.args, self.torch = solver, args, torch
+        n = len(dtf)
+        self.n = n
+        pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+        self.st = pin((n, NSPECIES), torch.float64)
+        self.st[:] = state0
+        self.at = pin((n, NSPECIES), torch.float64)
+        self.dtf = pin((n,), torch.float64)
+        self.dtf[:] = dtf
+        self.dt = pin((n,), torch.float64)
+        self.ttot = pin((n,), torch.float64)
+        self.status = pin((n,), torch.int32)
+        self.sweeps = pin((n,), torch.int32)
+        self.hint = pin((n,), torch.int32)
+        self.hint[:] = np.minimum(temperatures(state0), 2e9).astype(np.int32)
+        cfg = solver.default_config()
+        cfg.schedule, cfg.block = args.schedule, args.block
+        cfg.precision = DENGO_MIXED if precision == "mixed" else DENGO_FP64
+        cfg.warps_per_cell = args.warps_per_cell
+        cfg.sweep_budget, cfg.tail_grid = args.sweep_budget, args.tail_grid
+        cfg.max_substeps = args.max_substeps
+        self.cfg = cfg
+        a = lambda x: x.ctypes.data
+        self.batch = CellBatch(n, NSPECIES, 1, a(self.st), a(self.at), None, 1e-6, a(self.dtf),
+                               0.0, a(self.dt), a(self.ttot), a(self.status), None,
+                               a(self.sweeps), None, a(self.hint) if args.order else None)
+        self.fn = getattr(solver.lib, "primordial_solve_cells_host")
+        self.ms = getattr(solver.lib, "primordial_last_solve_ms")
+        # bytes the call copies per step: state, atol, dtf, dt, cost hint in;
+        # state, atol, dt, ttot, status, sweeps out
+        self.h2d = 2 * n * NSPECIES * 8 + 2 * n * 8 + (n * 4 if args.order else 0)
+        self.d2h = 2 * n * NSPECIES * 8 + 2 * n * 8 + 2 * n * 4
+
+    def step(self, first):
+        """One hydro step; returns (wall seconds of the call, device ms of
+        its solve)."""
+        np.multiply(self.st, 1e-6, out=self.at)
+        self.dt[:] = -1.0
+        if not first and self.args.order:
+            self.hint[:] = self.sweeps
+        t0 = time.perf_counter()
+        rc = self.fn(self.solver.data, C.byref(self.batch), -1.0, C.byref(self.cfg))
+        t1 = time.perf_counter()
+        if rc != 0:
+            raise RuntimeError("primordial_solve_cells_host failed: " + self.solver.last_error())
+        return t1 - t0, float(self.ms(self.solver.data))
+
+
+def run_arm(solver, state0, dtf, args, precision, torch, flush, sample):
+    """Warm-up on a 4096-cell copy, then the timed steps.  Returns a dict."""
+    wn = min(len(dtf), 4096)
+    warm = HostArm(solver, state0[:wn], dtf[:wn], args, precision, torch)
+    for k in range(args.warmup):
+        warm.step(k == 0)
+    arm = HostArm(solver, state0, dtf, args, precision, torch)
+    wall, dev, ok, sw = [], [], 0, 0
+    samples = []
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        w, d = arm.step(k == 0)
+        wall.append(w)
+        dev.append(d)
+        ok += int((arm.status == 0).sum())
+        sw += int(arm.sweeps.astype(np.int64).sum())
+        samples.append((arm.st[:sample].copy(), arm.status[:sample].copy()))
+    return {"wall_s": wall, "dev_ms": dev, "ok": ok, "sweeps": sw, "samples": samples,
+            "h2d": arm.h2d, "d2h": arm.d2h}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from dengo_gb300.workloads import primordial_cells
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    state, dtf = primordial_cells(args.cells, args.config)
+    from dengo_gb300.workloads import primordial_cells, PRIMORDIAL_CONFIGS
+    state, dtf = primordial_cells(args.cells, args.config,
+                                  seed=PRIMORDIAL_CONFIGS[args.config]["seed"])
     per_step = max(2.0, 150.0 / max(1, args.steps + args.warmup))
-    base, _, m = cpu_baseline(state, dtf, per_step * 3)
-    from oracle import Oracle
-    from dengo_gb300.tablefile import read_table_file
-    from dengo_gb300.build import network_dir
-    from dengo_gb300.runtime import load_library
-    lib = load_library("primordial")
-    order = [lib.primordial_table_name(k).decode() for k in range(lib.primordial_ntables())]
-    tabs = read_table_file(os.path.join(network_dir("primordial"), "primordial_tables.dgt"))
-    tables = [tabs[k] for k in order]
-    orc = Oracle("primordial")
+    base, m = cpu_baseline(state, dtf, per_step * 3)
+    orc, tables = oracle_tables()
     cur = state[:m].copy()
     for _ in range(args.warmup):
         orc.evolve_cells(tables, cur[:8], dtf[:8], nthreads=base["cores"])
@@ -206,17 +336,15 @@ def run_reference(args):
         ok_total += int((r["status"] == 0).sum())
         cur = r["state"]
     value = ok_total / t_total
-    line = {"impl": "reference", "metric": metric_name("fp64"),
+    sample = ("the first %d of the same seeded cells (a subsample of the GPU arm's %d), "
+              "%d hydro steps, all %d host cores (OpenMP over cells)"
+              % (m, args.cells, args.steps, base["cores"]))
+    line = {"impl": "reference", "metric": METRIC,
             "value": value, "unit": "cells/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)",
-            "config": {"workload": workload_name(args.cells, args.steps),
-                       "sample": "%d of the cells per step (%s distributions), on the host "
-                                 "cores" % (m, args.config),
-                       "cells_per_step": m},
-            "cpu_baseline": dict(base, value=value,
-                                 sample="%d cells per step x %d steps" % (m, args.steps)),
+            "data": "synthetic (seeded)", "config": config_dict(args),
+            "cpu_baseline": dict(base, value=value, sample=sample),
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -238,167 +366,104 @@ def run_ours(args):
     from dengo_gb300.runtime import Solver
     from dengo_gb300.workloads import PRIMORDIAL_CONFIGS, primordial_cells
 
-    n, N = args.cells, NSPECIES
+    n = args.cells
     seed = PRIMORDIAL_CONFIGS[args.config]["seed"] + 1000 * rank
     state0, dtf = primordial_cells(n, args.config, seed=seed)
     solver = Solver("primordial")
-    stream = torch.cuda.current_stream()
-    cfg = Solver.default_config()
-    cfg.schedule, cfg.block = args.schedule, args.block
-    cfg.precision = 1 if args.precision == "mixed" else 0
-    cfg.warps_per_cell = args.warps_per_cell
-    cfg.sweep_budget, cfg.tail_grid = args.sweep_budget, args.tail_grid
-    cfg.max_substeps = args.max_substeps
-
-    def device_batch(st_host):
-        st = torch.tensor(np.ascontiguousarray(st_host.T), device=dev)   # SoA: [species][cell]
-        return st
-
-    st = device_batch(state0)
-    at = torch.empty_like(st)
-    d_dtf = torch.tensor(dtf, device=dev)
-    status = torch.zeros(n, dtype=torch.int32, device=dev)
-    sweeps = torch.zeros(n, dtype=torch.int32, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    sample = 0 if args.no_parity else min(args.parity_sample, n)
+    precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
 
-    def step(state, atol, cells, ld):
-        torch.mul(state, 1e-6, out=atol)
-        solver.solve_device(state, cells, 1, ld, atol, rtol_scalar=1e-6, dtf=d_dtf,
-                            status=status, sweeps=sweeps, config=cfg, stream=stream)
-
-    # warm-up: W steps over a subset copy (same kernel, same code path)
-    wn = min(n, 4096)
-    wst = st[:, :wn].contiguous()
-    wat = torch.empty_like(wst)
-    for _ in range(args.warmup):
-        step(wst, wat, wn, wn)
-    torch.cuda.synchronize()
-    del wst, wat
-
-    t_hint = torch.tensor(np.minimum(temperatures(state0), 2e9).astype(np.int32), device=dev)
-    ok_count = torch.zeros((), dtype=torch.int64, device=dev)
-    sweep_sum = torch.zeros((), dtype=torch.int64, device=dev)
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    sample = min(args.parity_sample, n)
-    step1_in = state0[:sample].copy()
-    step1_out = None
     clocks = Clocks(dev.index)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    wall0 = time.perf_counter()
-    for k in range(args.steps):
-        flush.zero_()
-        torch.mul(st, 1e-6, out=at)
-        ev0[k].record(stream)
-        # longest-first order: the previous step's sweep counts, or for the
-        # first step the initial temperature (the stiff cells are the hot ones)
-        solver.solve_device(st, n, 1, n, at, rtol_scalar=1e-6, dtf=d_dtf, status=status,
-                            sweeps=sweeps, config=cfg, stream=stream,
-                            cost_hint=(t_hint if k == 0 else sweeps) if args.order else None)
-        ev1[k].record(stream)
-        ok_count += (status == 0).sum()
-        sweep_sum += sweeps.sum(dtype=torch.int64)
-        if k == 0:
-            step1_out = st[:, :sample].T.contiguous().cpu().numpy()
+    arms = {p: run_arm(solver, state0, dtf, args, p, torch, flush, sample) for p in precisions}
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
     clk = clocks.stop()
-    if dist:
-        dist.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    total_ms = float(sum(step_ms))
-    ok_local = int(ok_count.item())
-    flops = float(sweep_sum.item()) * F_SWEEP
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        c = torch.tensor([ok_local], device=dev, dtype=torch.int64)
-        dist.all_reduce(c)
-        ok_all = int(c.item())
-    else:
-        ok_all = ok_local
-    value = ok_all / (total_ms / 1e3)
-
-    # end to end through the host-buffer C entry point
-    e2e = None
-    if not args.no_e2e:
-        hst = state0.copy()
-        e2e_ok, e2e_t = 0, 0.0
-        h2d = d2h = 0
-        e2e_steps = max(1, min(args.steps, args.e2e_steps))
-        for k in range(e2e_steps):
-            atol_h = 1e-6 * hst
-            t0 = time.perf_counter()
-            r = solver.solve_host(hst, dtf, atol=atol_h)
-            e2e_t += time.perf_counter() - t0
-            hst = r["state"]
-            e2e_ok += int((r["status"] == 0).sum())
-        h2d = 2 * n * N * 8 + 2 * n * 8              # state, atol, dtf, dt
-        d2h = 2 * n * N * 8 + 2 * n * 8 + n * 4      # state, atol, dt, ttot, status
-        e2e = {"value": e2e_ok * world / e2e_t, "unit": "cells/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "seconds": e2e_t, "steps": e2e_steps,
-               "path": "primordial_solve_cells_host (host buffers, copies inside the call)"}
-
+    # whole-job figures: device time and wall time are the max over ranks,
+    # converged cells the sum
+    for p, a in arms.items():
+        a["dev_total_ms"] = float(sum(a["dev_ms"]))
+        a["wall_total_s"] = float(sum(a["wall_s"]))
+        if dist:
+            t = torch.tensor([a["dev_total_ms"], a["wall_total_s"]], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            a["dev_total_ms"], a["wall_total_s"] = float(t[0]), float(t[1])
+            c = torch.tensor([a["ok"], a["sweeps"]], device=dev, dtype=torch.int64)
+            dist.all_reduce(c)
+            a["ok_all"], a["sweeps_all"] = int(c[0]), int(c[1])
+        else:
+            a["ok_all"], a["sweeps_all"] = a["ok"], a["sweeps"]
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
+
+    par = {}
+    if sample:
+        ref_steps, _ = oracle_steps(state0[:sample], dtf[:sample], args.steps)
+        for p, a in arms.items():
+            par[p] = parity(a["samples"], ref_steps, state0[:sample])
+
+    def figures(p):
+        a = arms[p]
+        frac = par[p]["frac_within_1e-6"] if p in par and par[p]["frac_within_1e-6"] is not None \
+            else 1.0
+        conv = a["ok_all"] / (a["dev_total_ms"] / 1e3)
+        return {"value": conv * frac, "converged_cells_per_s": conv,
+                "frac_within_1e-6": frac,
+                "ms_per_step": a["dev_total_ms"] / args.steps,
+                "step_ms": a["dev_ms"],
+                "e2e": {"value": a["ok_all"] * frac / a["wall_total_s"], "unit": "cells/s",
+                        "h2d_bytes_per_step": a["h2d"], "d2h_bytes_per_step": a["d2h"],
+                        "seconds": a["wall_total_s"], "steps": args.steps,
+                        "path": "primordial_solve_cells_host, pinned host buffers, the same "
+                                "steps and solver configuration as value"},
+                "parity": par.get(p)}
+
     peak = measure_fp64_peak()
-    achieved = flops / (total_ms / 1e3) / 1e12
+    main = precisions[0]
+    f = figures(main)
+    a = arms[main]
+    achieved = a["sweeps_all"] * F_SWEEP / (a["dev_total_ms"] / 1e3) / 1e12
+    engine = {"precision": main, "warps_per_cell": args.warps_per_cell,
+              "schedule": args.schedule, "sweep_budget": args.sweep_budget,
+              "order": "costliest first (cost hint)" if args.order else "input order",
+              "warmup": "%d steps over a 4096-cell copy" % args.warmup}
     line = {
-        "metric": metric_name(args.precision),
-        "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f64 residual + f32 LU",
-        "data": "synthetic (seeded)",
-        "config": {"workload": workload_name(n, args.steps),
-                   "cells_per_gpu": n, "precision": args.precision, "schedule": args.schedule,
-                   "order": "costliest first" if args.order else "input order",
-                   "warps_per_cell": args.warps_per_cell,
-                   "sweep_budget": args.sweep_budget,
-                   "l2": "flushed (256 MB write) before every step",
-                   "warmup": "%d steps over a %d-cell copy" % (args.warmup, wn)},
-        "wall_s": wall, "step_ms": step_ms, "gpu_launches": args.steps * ((4 if args.sweep_budget > 0 else 1) + (3 if args.order else 0)),
+        "metric": METRIC, "value": f["value"], "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if main == "fp64" else "f64 residual + f32 LU",
+        "data": "synthetic (seeded)", "config": config_dict(args), "engine": engine,
+        "converged_cells_per_s": f["converged_cells_per_s"],
+        "frac_within_1e-6": f["frac_within_1e-6"], "step_ms": f["step_ms"],
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps * len(precisions),
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "traffic": DRAM_BYTES_PER_CELL[args.precision] * n,
+                     "traffic": DRAM_BYTES_PER_CELL[main] * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "14 592-cell launch (profiles/evolve_split_%s_cold14592.md)"
-                                       ", scaled by cells" % args.precision,
-                     "peak_source": "measured FP64 FMA throughput (dg_peak.cu), this run",
+                                       ", scaled by cells" % main,
+                     "peak_source": "of measured: FP64 FMA throughput of this GPU "
+                                    "(dg_peak.cu), this run; MEASURED_PEAKS.json has no "
+                                    "FP64 figure; the path cannot contract its multiply-adds "
+                                    "(the reference's rounding), so peak/2 is its ceiling",
                      "flop_per_sweep": F_SWEEP},
+        "e2e": f["e2e"], "parity": f["parity"],
     }
-    if e2e:
-        line["e2e"] = e2e
-    # parity sample and CPU baseline (oracle on the host cores)
+    if "mixed" in arms and main != "mixed":
+        m = figures("mixed")
+        m["speedup_vs_fp64"] = m["value"] / f["value"] if f["value"] else None
+        m["e2e_speedup_vs_fp64"] = (m["e2e"]["value"] / f["e2e"]["value"]
+                                    if f["e2e"]["value"] else None)
+        line["mixed"] = m
     if not args.no_cpu_baseline:
-        base, res, m = cpu_baseline(state0, dtf, args.cpu_seconds)
+        base, _ = cpu_baseline(state0, dtf, args.cpu_seconds)
         line["cpu_baseline"] = base
-        ref = res["state"][:sample]
-        okm = res["status"][:sample] == 0
-        with np.errstate(invalid="ignore", divide="ignore"):
-            rel = np.abs(step1_out - ref) / np.maximum(np.abs(ref), 1e-300)
-        rel[step1_out == ref] = 0
-        r_ok = rel[okm]
-        # relative error with entries below the solve's absolute tolerance
-        # (1e-6 x the input) measured against that tolerance
-        floored = (np.abs(step1_out - ref) / np.maximum(np.abs(ref), 1e-6 * np.abs(step1_in)))[okm]
-        line["parity"] = {"sample_cells": int(sample), "ok_in_oracle": int(okm.sum()),
-                          "max_rel_err_ok": float(r_ok.max(initial=0.0)),
-                          "max_floored_err_ok": float(floored.max(initial=0.0)),
-                          "frac_floored_within_1e-6": float(np.mean(np.all(floored <= 1e-6, axis=1)))
-                          if okm.any() else None,
-                          "frac_within_1e-6": float(np.mean(np.all(r_ok <= 1e-6, axis=1)))
-                          if okm.any() else None,
-                          "frac_within_1e-10": float(np.mean(np.all(r_ok <= 1e-10, axis=1)))
-                          if okm.any() else None,
-                          "bit_identical": int(np.all(step1_out == ref, axis=1).sum())}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -37,16 +37,24 @@ namespace dg {
 /* ST_SUSPENDED: set aside by the sweep budget; finished by a resume launch */
 enum : int { ST_OK = 0, ST_MAX_SUBSTEPS = 1, ST_DT_UNDERFLOW = 2, ST_SUSPENDED = 3 };
 
+/* Most tables a network with redshift tables may have: their values at a
+ * call's z travel inside the kernel parameter (zvals below). */
+#define DG_MAX_TABLES 64
+
 /* Rate/cooling tables on the device, bin-major: for bin b and table k the
  * pair (r_k[b], r_k[b+1] - r_k[b]).  The difference is the reference's own
- * subtraction (rates_and_rate_tables.C.template:406-408) done once. */
+ * subtraction (rates_and_rate_tables.C.template:406-408) done once.
+ * Passed by value to every kernel, so a launch carries its own z and its own
+ * redshift-table values: no device buffer is written between calls and no
+ * call waits for an earlier one. */
 struct TableSet {
     const double2 *pairs;   /* [nbins][NT] */
-    const double *zvals;    /* [NT] values of the redshift tables at this call's z */
     int nbins;              /* table length - 1 */
     double lb, dbin, idbin; /* log(T_lo), bin width, 1/width (host-computed) */
     double Tlo, Thi;
     double z;               /* redshift of this call (only compton-like terms read it) */
+    double zvals[DG_MAX_TABLES]; /* [k]: value of redshift table k at z (host-computed;
+                                    unused for the other tables) */
 };
 
 /* Cell arrays: element (cell c, species s) at p[c*cs + s*ss]. */

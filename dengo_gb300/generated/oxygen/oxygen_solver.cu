@@ -1533,7 +1533,12 @@ int oxygen_solve_cells_device(oxygen_data *data, const dengo_cell_batch *batch, 
  * up once per device with cudaGetSymbolAddress, the first time the entry
  * point runs on that device: make that first call before any stream capture.
  * Calls share the array: calls that overlap on the GPU race on it; each call
- * clears the counters it uses before its kernels read them. */
+ * clears the counters it uses before its kernels read them.  The solve is
+ * one launch: the configuration's sweep_budget and tail_grid are ignored
+ * (the stiff-cell redistribution needs per-cell records that this array
+ * does not hold); the results are the same.  Nothing in a call waits for the
+ * stream or the device: a redshift-table network's values at z travel in the
+ * kernel parameter. */
 #define OXYGEN_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define OXYGEN_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char oxygen_noalloc_scratch[OXYGEN_NOALLOC_SCRATCH_BYTES];
@@ -1569,6 +1574,8 @@ int oxygen_solve_cells_host(oxygen_data *data, const dengo_cell_batch *batch, do
 {
     return dgnet_oxygen::Api::solve_host(data, batch, z, cfg);
 }
+
+double oxygen_last_solve_ms(oxygen_data *data) { return dgnet_oxygen::Api::last_solve_ms(data); }
 
 int oxygen_run_strip(oxygen_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

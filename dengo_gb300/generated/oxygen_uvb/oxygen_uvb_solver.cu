@@ -1643,7 +1643,12 @@ int oxygen_uvb_solve_cells_device(oxygen_uvb_data *data, const dengo_cell_batch 
  * up once per device with cudaGetSymbolAddress, the first time the entry
  * point runs on that device: make that first call before any stream capture.
  * Calls share the array: calls that overlap on the GPU race on it; each call
- * clears the counters it uses before its kernels read them. */
+ * clears the counters it uses before its kernels read them.  The solve is
+ * one launch: the configuration's sweep_budget and tail_grid are ignored
+ * (the stiff-cell redistribution needs per-cell records that this array
+ * does not hold); the results are the same.  Nothing in a call waits for the
+ * stream or the device: a redshift-table network's values at z travel in the
+ * kernel parameter. */
 #define OXYGEN_UVB_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define OXYGEN_UVB_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char oxygen_uvb_noalloc_scratch[OXYGEN_UVB_NOALLOC_SCRATCH_BYTES];
@@ -1679,6 +1684,8 @@ int oxygen_uvb_solve_cells_host(oxygen_uvb_data *data, const dengo_cell_batch *b
 {
     return dgnet_oxygen_uvb::Api::solve_host(data, batch, z, cfg);
 }
+
+double oxygen_uvb_last_solve_ms(oxygen_uvb_data *data) { return dgnet_oxygen_uvb::Api::last_solve_ms(data); }
 
 int oxygen_uvb_run_strip(oxygen_uvb_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

@@ -993,7 +993,12 @@ int primordial_solve_cells_device(primordial_data *data, const dengo_cell_batch 
  * up once per device with cudaGetSymbolAddress, the first time the entry
  * point runs on that device: make that first call before any stream capture.
  * Calls share the array: calls that overlap on the GPU race on it; each call
- * clears the counters it uses before its kernels read them. */
+ * clears the counters it uses before its kernels read them.  The solve is
+ * one launch: the configuration's sweep_budget and tail_grid are ignored
+ * (the stiff-cell redistribution needs per-cell records that this array
+ * does not hold); the results are the same.  Nothing in a call waits for the
+ * stream or the device: a redshift-table network's values at z travel in the
+ * kernel parameter. */
 #define PRIMORDIAL_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define PRIMORDIAL_NOALLOC_MAX_DEVICES 64
 static __device__ __align__(256) unsigned char primordial_noalloc_scratch[PRIMORDIAL_NOALLOC_SCRATCH_BYTES];
@@ -1029,6 +1034,8 @@ int primordial_solve_cells_host(primordial_data *data, const dengo_cell_batch *b
 {
     return dgnet_primordial::Api::solve_host(data, batch, z, cfg);
 }
+
+double primordial_last_solve_ms(primordial_data *data) { return dgnet_primordial::Api::last_solve_ms(data); }
 
 int primordial_run_strip(primordial_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

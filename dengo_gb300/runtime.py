@@ -69,6 +69,7 @@ def _declare(lib, n):
                                                 C.POINTER(SolverConfig), C.c_void_p]),
         "%s_solve_cells_host" % n: (C.c_int, [C.c_void_p, C.POINTER(CellBatch), C.c_double,
                                               C.POINTER(SolverConfig)]),
+        "%s_last_solve_ms" % n: (C.c_double, [C.c_void_p]),
         "calculate_rhs_%s" % n: (C.c_int, [P_D, P_D, C.c_int, C.c_int, C.c_void_p]),
         "calculate_jacobian_%s" % n: (C.c_int, [P_D, P_D, C.c_int, C.c_int, C.c_void_p]),
         "%s_calculate_temperature" % n: (None, [C.c_void_p, P_D, C.c_int, C.c_int]),
@@ -155,8 +156,8 @@ class Solver:
         cfg.max_newton_sweeps, cfg.max_substeps = 10, 50000
         cfg.dt_ratio_floor, cfg.floor_value = 1e-15, 1e-25
         cfg.precision, cfg.schedule, cfg.block, cfg.grid = DENGO_FP64, SCHED_AUTO, 0, 0
-        cfg.warps_per_cell = 1
-        cfg.sweep_budget, cfg.tail_grid = 0, 0
+        cfg.warps_per_cell = 4
+        cfg.sweep_budget, cfg.tail_grid = 2000, 0
         return cfg
 
     # ---- reference-shaped host entry points ----------------------------
@@ -193,15 +194,27 @@ class Solver:
             raise RuntimeError("solve_cells_device failed (%d): %s" % (rc, self.last_error()))
 
     def solve_host(self, state, dtf, rtol=None, atol=None, dt=None, z=-1.0, config=None,
-                   counters=False):
-        """``<name>_solve_cells_host`` on a (cells, N) AoS host array (copied).
+                   counters=False, cost_hint=None, copy=True):
+        """``<name>_solve_cells_host`` on a (cells, N) AoS host array.
 
-        Per-cell ``dtf``; returns a dict of the outputs."""
-        st = np.ascontiguousarray(state, np.float64).copy()
+        Per-cell ``dtf``; ``cost_hint`` (int32 per cell, e.g. the previous
+        step's sweeps) starts the costliest cells first.  With ``copy=False``
+        a C-contiguous float64 ``state`` (and ``atol``) is updated in place,
+        as the C entry point does.  Returns a dict of the outputs; its
+        ``solve_ms`` is the device time of the solve, copies excluded."""
+        st = np.ascontiguousarray(state, np.float64)
+        if copy or st is not state:
+            st = st.copy()
         n = st.shape[0]
-        at = (1e-6 * st) if atol is None else np.ascontiguousarray(atol, np.float64).copy()
+        if atol is None:
+            at = 1e-6 * st
+        else:
+            at = np.ascontiguousarray(atol, np.float64)
+            if copy or at is not atol:
+                at = at.copy()
         rt = None if rtol is None else np.ascontiguousarray(np.broadcast_to(rtol, st.shape), np.float64).copy()
         dtf = np.ascontiguousarray(np.broadcast_to(np.asarray(dtf, np.float64), (n,))).copy()
+        hint = None if cost_hint is None else np.ascontiguousarray(cost_hint, np.int32)
         dtv = np.full(n, -1.0) if dt is None else np.broadcast_to(np.asarray(dt, np.float64), (n,)).copy()
         out = dict(state=st, atol=at, dt=dtv, ttot=np.zeros(n), status=np.zeros(n, np.int32))
         if counters:
@@ -210,12 +223,13 @@ class Solver:
         addr = lambda a: None if a is None else a.ctypes.data
         b = CellBatch(n, self.N, 1, addr(st), addr(at), addr(rt), 1e-6, addr(dtf), 0.0, addr(dtv),
                       addr(out["ttot"]), addr(out["status"]), addr(out.get("substeps")),
-                      addr(out.get("sweeps")), addr(out.get("failures")))
+                      addr(out.get("sweeps")), addr(out.get("failures")), addr(hint))
         cfg = config or self.default_config()
         rc = getattr(self.lib, "%s_solve_cells_host" % self.name)(self.data, C.byref(b), float(z),
                                                                   C.byref(cfg))
         if rc != 0:
             raise RuntimeError("solve_cells_host failed (%d): %s" % (rc, self.last_error()))
+        out["solve_ms"] = getattr(self.lib, "%s_last_solve_ms" % self.name)(self.data)
         return out
 
     # ---- the reference's Cython driver ---------------------------------

@@ -33,6 +33,8 @@
  *   <n>_solve_cells_host    the same batch with host pointers (copies in and
  *                           out inside the call; per-cell dtf, unlike
  *                           dengo_evolve_<n> whose dtf is one scalar)
+ *   <n>_last_solve_ms       device time of the last <n>_solve_cells_host
+ *                           call's solve, copies excluded (CUDA events)
  *   <n>_run_strip           the reference's Cython driver run_<n>
  *                           (rates_and_rate_tables_run.pyx.template:114-205)
  *                           on one strip in lockstep: BE_chem_solve with its
@@ -83,7 +85,10 @@ enum dengo_precision {
 
 /* How cells are assigned to lanes. */
 enum dengo_schedule {
-    DENGO_SCHED_AUTO = 0,      /* autotuned choice                        */
+    DENGO_SCHED_AUTO = 0,      /* the default: the atomic work queue, the
+                                  fastest schedule measured on the shipped
+                                  workloads (dengo_gb300.batching tunes the
+                                  others per workload)                    */
     DENGO_SCHED_PER_THREAD = 1,/* one cell per thread, one launch         */
     DENGO_SCHED_STRIDE = 2,    /* lanes refill from a static stride       */
     DENGO_SCHED_QUEUE = 3      /* lanes refill from an atomic work queue  */
@@ -92,7 +97,10 @@ enum dengo_schedule {
 /* Solver constants.  dengo_default_config() returns the reference's values:
  * 10 Newton sweeps (BE_chem_solve.C:87), 50000 accepted substeps
  * (C.template:204), dt/dtf floor 1e-15 (C.template:251), value floor 1e-25
- * (C.template:187). */
+ * (C.template:187); and the fastest engine measured on the shipped
+ * workloads: FP64, the work queue, four warps per cell, stiff-cell
+ * redistribution after 2000 sweeps.  Every engine variant gives the same
+ * results. */
 typedef struct dengo_solver_config {
     int max_newton_sweeps;
     int max_substeps;
@@ -103,14 +111,14 @@ typedef struct dengo_solver_config {
     int block;                 /* threads per block, 0 = tuned default */
     int grid;                  /* blocks, 0 = tuned default             */
     int warps_per_cell;        /* warps sharing each cell's sweep: 1, 2 or
-                                  4 (32 cells per group of warps); 0 = tuned */
+                                  4 (32 cells per group of warps); 0 = 4 */
     int sweep_budget;          /* > 0: redistribute stiff cells -- a cell
                                   that has taken this many Newton sweeps is
                                   set aside at its next substep boundary and
                                   resumed by a later launch that spreads the
                                   set-aside cells over the SMs (again at 16x
                                   the budget, then finished); results are
-                                  unchanged.  0 = one launch */
+                                  unchanged.  0 = one launch; default 2000 */
     int tail_grid;             /* blocks of the resume launches, 0 = as
                                   many as the set-aside cells need (the
                                   allocation-free entry point always makes
@@ -191,6 +199,7 @@ typedef int (*jac_f)(double *, double *, int, int, void *);
                                void *stream);                                  \
     int n##_solve_cells_host(n##_data *data, const dengo_cell_batch *batch,    \
                              double z, const dengo_solver_config *cfg);        \
+    double n##_last_solve_ms(n##_data *data);                                  \
     int n##_run_strip(n##_data *data, double tf, int niter, double z,          \
                       double *input, double *rtol, double *atol, int nstrip,   \
                       double *ttot, double *dt, double *traj, double *traj_T,  \
@@ -218,6 +227,12 @@ typedef int (*jac_f)(double *, double *, int, int, void *);
  * first call on a device looks up that array's device address; make it
  * before any stream capture.  Calls share the array, so calls that overlap
  * on the GPU race; the counters are cleared at the start of every call.
+ * The solve is one launch: sweep_budget and tail_grid are ignored, because
+ * the stiff-cell redistribution keeps per-cell records this array does not
+ * hold (the results are the same; the stiffest cells' share of the run is
+ * longer).  No call waits for the stream or the device, redshift changes of
+ * the UV-background networks included.  The data context must belong to the
+ * current device (-1 otherwise, as for <n>_solve_cells_device).
  * The caller still passes the data context from <n>_setup_data* and every
  * input and output array. */
 #define DENGO_DECLARE_NETWORK_NOALLOC(n)                                       \

@@ -1199,3 +1199,67 @@ const dgo_network dgo_oxygen_uvb_network = {
 
 int dgo_oxygen_uvb_ntables(void) { return NTAB; }
 int dgo_oxygen_uvb_table_len(int k) { return zdep[k] ? NZ_LEN : NT_LEN; }
+
+/* table k's name in the table bundle (<name>_tables.dgt), so the oracle can
+ * order a bundle's tables itself */
+static const char *const table_names[NTAB > 0 ? NTAB : 1] = {
+    "H_1_i",
+    "H_1_pi",
+    "H_2_r",
+    "He_1_i",
+    "He_1_pi",
+    "He_2_i",
+    "He_2_pi",
+    "He_2_r",
+    "He_3_r",
+    "O_1_i",
+    "O_1_pi",
+    "O_2_i",
+    "O_2_pi",
+    "O_2_r",
+    "O_3_i",
+    "O_3_pi",
+    "O_3_r",
+    "O_4_i",
+    "O_4_pi",
+    "O_4_r",
+    "O_5_i",
+    "O_5_pi",
+    "O_5_r",
+    "O_6_i",
+    "O_6_pi",
+    "O_6_r",
+    "O_7_i",
+    "O_7_pi",
+    "O_7_r",
+    "O_8_i",
+    "O_8_pi",
+    "O_8_r",
+    "O_9_r",
+    "H_1_c_H_1_c",
+    "H_1_ph_H_1_ph",
+    "H_2_c_H_2_c",
+    "He_1_c_He_1_c",
+    "He_1_ph_He_1_ph",
+    "He_2_c_He_2_c",
+    "He_2_ph_He_2_ph",
+    "He_3_c_He_3_c",
+    "O_1_c_O_1_c",
+    "O_1_ph_O_1_ph",
+    "O_2_c_O_2_c",
+    "O_2_ph_O_2_ph",
+    "O_3_c_O_3_c",
+    "O_3_ph_O_3_ph",
+    "O_4_c_O_4_c",
+    "O_4_ph_O_4_ph",
+    "O_5_c_O_5_c",
+    "O_5_ph_O_5_ph",
+    "O_6_c_O_6_c",
+    "O_6_ph_O_6_ph",
+    "O_7_c_O_7_c",
+    "O_7_ph_O_7_ph",
+    "O_8_c_O_8_c",
+    "O_8_ph_O_8_ph",
+    "O_9_c_O_9_c",
+};
+const char *dgo_oxygen_uvb_table_name(int k) { return k >= 0 && k < NTAB ? table_names[k] : 0; }

@@ -729,3 +729,54 @@ const dgo_network dgo_primordial_compton_network = {
 
 int dgo_primordial_compton_ntables(void) { return NTAB; }
 int dgo_primordial_compton_table_len(int k) { return zdep[k] ? NZ_LEN : NT_LEN; }
+
+/* table k's name in the table bundle (<name>_tables.dgt), so the oracle can
+ * order a bundle's tables itself */
+static const char *const table_names[NTAB > 0 ? NTAB : 1] = {
+    "k01",
+    "k02",
+    "k03",
+    "k04",
+    "k05",
+    "k06",
+    "k07",
+    "k08",
+    "k09",
+    "k10",
+    "k11",
+    "k12",
+    "k13",
+    "k14",
+    "k15",
+    "k16",
+    "k17",
+    "k18",
+    "k19",
+    "k21",
+    "k22",
+    "k23",
+    "brem_brem",
+    "ceHI_ceHI",
+    "ceHeI_ceHeI",
+    "ceHeII_ceHeII",
+    "ciHI_ciHI",
+    "ciHeI_ciHeI",
+    "ciHeII_ciHeII",
+    "ciHeIS_ciHeIS",
+    "compton_comp",
+    "gammah_gammah",
+    "gloverabel08_gaH2",
+    "gloverabel08_gaHI",
+    "gloverabel08_gaHe",
+    "gloverabel08_gaHp",
+    "gloverabel08_gael",
+    "gloverabel08_gphdl",
+    "gloverabel08_gpldl",
+    "h2formation_h2mcool",
+    "h2formation_h2mheat",
+    "reHII_reHII",
+    "reHeII1_reHeII1",
+    "reHeII2_reHeII2",
+    "reHeIII_reHeIII",
+};
+const char *dgo_primordial_compton_table_name(int k) { return k >= 0 && k < NTAB ? table_names[k] : 0; }

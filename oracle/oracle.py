@@ -78,6 +78,18 @@ class Oracle:
         ntab = getattr(self.lib, "dgo_%s_table_len" % name)
         ntab.argtypes = [C.c_int]
         self.table_len = [ntab(k) for k in range(self.nt)]
+        tname = getattr(self.lib, "dgo_%s_table_name" % name)
+        tname.argtypes, tname.restype = [C.c_int], C.c_char_p
+        self.table_names = [tname(k).decode() for k in range(self.nt)]
+
+    def tables_from_bundle(self, path):
+        """The tables of a ``<name>_tables.dgt`` bundle in this network's
+        table order."""
+        import sys
+        sys.path.insert(0, os.path.dirname(HERE))
+        from dengo_gb300.tablefile import read_table_file
+        tabs = read_table_file(path)
+        return [tabs[k] for k in self.table_names]
 
     def config(self, max_sweeps=10, max_substeps=50000):
         c = self.lib.dgo_default_config()

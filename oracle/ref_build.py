@@ -3,7 +3,7 @@
 
 Recipe (runs only where the reference checkout exists):
 
-1. Import the reference package read-only from ``/root/reference`` with
+1. Import the reference package read-only from ``REF_ROOT`` (below) with
    compatibility shims that change no arithmetic:
    * ``h5py`` is replaced by a writer of raw float64 files (the container has
      no HDF5); ``docutils.utils.roman`` (imported, unused) is stubbed;
@@ -47,7 +47,12 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("DGO_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $DGO_REFERENCE_ROOT, else a "reference" directory
+# beside this repository's root.
+REF_ROOT = os.environ.get(
+    "DGO_REFERENCE_ROOT",
+    os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                 "reference"))
 OUT = os.path.join(HERE, "_ref")
 
 ALIASES = dict(HI="H_1", HII="H_2", HM="H_m0", HeI="He_1", HeII="He_2",

@@ -228,9 +228,8 @@ extern "C" int hx_run_strip(double *input, const double *rtol, double *atol, int
     for (int b = 0; b < nbins; b++)
         for (int k = 0; k < NT; k++)
             pairs[(size_t)b * NT + k] = make_double2(tables[k][b], tables[k][b + 1] - tables[k][b]);
-    std::vector<double> zvals(NT, 0.0);
-    dg::TableSet ts{pairs.data(), zvals.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
-                    data.bounds[0], data.bounds[1], z};
+    dg::TableSet ts{pairs.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
+                    data.bounds[0], data.bounds[1], z, {}};
     double sc[3] = {0, 0, 0};
     int iters[16] = {0};
     dg::RunOut o{};
@@ -307,8 +306,9 @@ extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long lo
      * host before a launch */
     std::vector<double> zvals(NT, 0.0), dzvals(NT, 0.0);
     hx_z<Net>::z_values(&data, z, zvals.data(), dzvals.data());
-    dg::TableSet ts{pairs.data(), zvals.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
-                    data.bounds[0], data.bounds[1], z};
+    dg::TableSet ts{pairs.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
+                    data.bounds[0], data.bounds[1], z, {}};
+    for (int k = 0; k < NT && k < DG_MAX_TABLES; k++) ts.zvals[k] = zvals[k];
     dg::CellIO io{state, atol, nullptr, rtol_scalar, dtf, 0.0, dt, ttot, status, substeps, sweeps,
                   failures, nullptr, NN, 1, ncells};
     dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1};

@@ -53,6 +53,20 @@ def test_library_loads_without_gpu(libpath):
     assert lib.primordial_species_name(9) == b"ge"
 
 
+def test_python_default_config_is_the_library_default(libpath):
+    """Solver.default_config() mirrors dengo_default_config() field by field
+    (the call needs no GPU)."""
+    from dengo_gb300.runtime import Solver, SolverConfig
+    lib = C.CDLL(libpath)
+    lib.dengo_default_config.argtypes = [C.POINTER(SolverConfig)]
+    c = SolverConfig()
+    lib.dengo_default_config(C.byref(c))
+    py = Solver.default_config()
+    for name, _ in SolverConfig._fields_:
+        assert getattr(c, name) == getattr(py, name), name
+    assert c.warps_per_cell == 4 and c.sweep_budget == 2000
+
+
 def test_runtime_fails_loudly_without_library(tmp_path):
     from dengo_gb300.runtime import load_library
     with pytest.raises(RuntimeError, match="not built"):
@@ -60,8 +74,8 @@ def test_runtime_fails_loudly_without_library(tmp_path):
 
 
 HOST_C = r'''
-/* An Enzo-style host code, as INTEGRATION.md shows it: plain C99 against the
- * generated header, linked with the network library. */
+/* An Enzo-style host code: plain C99 against the generated header, linked
+ * with the network library. */
 #include <stdio.h>
 #include "primordial_solver.h"
 

@@ -104,10 +104,6 @@ def test_redshift_changes_the_result():
 
 
 @pytest.mark.gpu
-@pytest.mark.xfail(reason="not yet run on a GPU since it reads the shipped tables (a first "
-                          "run, with tables recomputed on the GPU host, saw <= 3e-9 "
-                          "differences); the kernel source compiled for the host passes the "
-                          "same checks (tests/test_engine_host.py)", strict=False)
 @pytest.mark.parametrize("wpc", [1, 4])
 def test_gpu_matches_reference(wpc):
     """FP64 path at every redshift.  Against the oracle built with a

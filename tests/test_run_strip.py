@@ -155,9 +155,6 @@ def test_run_strip_kernel_on_host_matches_reference_cython_driver(tables_in_orde
 
 
 @pytest.mark.gpu
-@pytest.mark.xfail(reason="not yet run on a GPU; the kernel source compiled for the host passes "
-                          "the same comparison (test_run_strip_kernel_on_host_matches_reference"
-                          "_cython_driver)", strict=False)
 @pytest.mark.parametrize("case", [0, 1, 2])
 def test_gpu_run_strip_matches_reference_cython_driver(solver, case):
     """Solver.run (<n>_run_strip on the GPU) against the reference's own
