@@ -72,6 +72,7 @@ class NetworkSpec:
     rhs_part: dict = field(default_factory=dict)      # {NP: [part per row]}
     jac_part: dict = field(default_factory=dict)      # {NP: [var][eq] part}
     stop_time: str = "3.1557e13"   # literal: the network's stop_time (the main driver's dtf)
+    write_intermediate: bool = False  # the network's write_intermediate_solutions
 
     @property
     def N(self):
@@ -180,6 +181,7 @@ def network_spec(net, name):
         nz=(len(z) if z is not None else 0),
         input_is_number=bool(getattr(net, "input_is_number", False)),
         stop_time=repr(float(net.stop_time)),
+        write_intermediate=bool(getattr(net, "write_intermediate_solutions", False)),
         mass_density_ref=ccode_ref(md), mass_density_dev=ccode_device(md),
         T_ref=ccode_ref(T), T_dev=ccode_device(T),
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),

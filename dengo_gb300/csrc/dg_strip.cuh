@@ -404,6 +404,200 @@ be_strip_kernel(double *u, double dt, const double *rtol, double *atol, int nstr
     if (c == 0) *ret = rv;
 }
 
+/* Per-strip control state of a lockstep evolve (evolve_lockstep_kernel),
+ * kept in device memory so that a launch can stop after an accepted substep
+ * and the next launch resume. */
+struct LockStrip {
+    double dt, ttot;
+    int siter;
+    int status;   /* 0 running or integrated to dtf, 1 substep cap, 2 dt floor */
+    int done;     /* the strip's evolve has ended */
+    int dumped;   /* this launch ended at an accepted substep (dump written) */
+};
+
+/* Arguments of evolve_lockstep_kernel.  input/atol/rtol: the caller's AoS
+ * arrays (mass densities + ge unless the network takes number densities),
+ * cells [b*strip, min(dims, (b+1)*strip)) form strip b.  rec: per cell
+ * rec_len<N>() doubles (u, prev, scale, atol in number densities, then T)
+ * for a launch that stops after an accepted substep; dump: per cell N + 1
+ * doubles (prev and T at that substep). */
+struct LockIO {
+    double *input, *atol;
+    const double *rtol;
+    long long dims;
+    int strip;
+    double dtf;
+    LockStrip *ls;
+    double *rec, *dump;
+    int resume, stop_after_accept;
+};
+
+/* dengo_evolve_<n> (rates_and_rate_tables.C.template:149-274) over strips
+ * in lockstep, the reference's semantics for dims > 1: one CTA per strip,
+ * one thread per cell; mass -> number densities (input and atol), the
+ * electron consistency with the reference's running total over the strip,
+ * dt = dtf / 1e5 when the caller's dt < 0, scale = prev = input fixed for the
+ * call; then while ttot < dtf: BE_chem_solve over the whole strip (one dt,
+ * one Newton loop), any negative value anywhere fails the substep; on
+ * success: stop at the substep cap, siter++, ttot += dt,
+ * dt = min(1.1 dt, dtf - ttot), [intermediate dump of prev and T], prev =
+ * input, values below floor_value raised to it; on failure: dt /= 2,
+ * input = prev, stop when dt / dtf < dt_ratio_floor; finally number -> mass
+ * densities.  With stop_after_accept the launch returns after each accepted
+ * substep (its state in rec) so that the host can write the reference's
+ * <n>_intermediate_%06d file (C.template:212-241) before resuming. */
+template <class Net>
+__global__ void __launch_bounds__(DENGO_MAX_NCELLS)
+evolve_lockstep_kernel(LockIO io, TableSet ts, KernelCfg cfg)
+{
+    constexpr int N = Net::N;
+    constexpr int RL = rec_len<N>();
+    const long long first = (long long)blockIdx.x * io.strip;
+    const long long left = io.dims - first;
+    const int nstrip = (int)(left < io.strip ? left : io.strip);
+    const int c = threadIdx.x;
+    const bool act = c < nstrip;
+    const long long cell = first + c;
+    LockStrip &L = io.ls[blockIdx.x];
+    __shared__ int first_bad;
+    if (L.done) return;
+    double u[N], prev[N], sc[N], at[N], rt[N];
+    double T = 0;
+    double dt, ttot;
+    int siter;
+    if (!io.resume) {
+        if (act) {
+            for (int i = 0; i < N; i++) {
+                u[i] = io.input[cell * N + i];
+                at[i] = io.atol[cell * N + i];
+                rt[i] = io.rtol[cell * N + i];
+            }
+            to_number_density<Net>(u, at);
+            for (int i = 0; i < N; i++) io.input[cell * N + i] = u[i];
+        }
+        __syncthreads();
+        if (c == 0) {
+            /* ensure_electron_consistency: the running total over the strip */
+            double total = 0.0;
+            for (int k = 0; k < nstrip; k++) {
+                double y[N];
+                for (int i = 0; i < N; i++) y[i] = io.input[(first + k) * N + i];
+                total = Net::electron_sum(y, total);
+                if (Net::IDE >= 0) io.input[(first + k) * N + Net::IDE] = total;
+            }
+        }
+        __syncthreads();
+        if (act)
+            for (int i = 0; i < N; i++) {
+                u[i] = io.input[cell * N + i];
+                sc[i] = u[i];
+                prev[i] = u[i];
+            }
+        dt = L.dt < 0 ? io.dtf / 1e5 : L.dt;
+        ttot = 0.0;
+        siter = 0;
+    } else {
+        if (act) {
+            const double *r = io.rec + cell * RL;
+            for (int i = 0; i < N; i++) {
+                u[i] = r[i];
+                prev[i] = r[N + i];
+                sc[i] = r[2 * N + i];
+                at[i] = r[3 * N + i];
+                rt[i] = io.rtol[cell * N + i];
+            }
+        }
+        dt = L.dt;
+        ttot = L.ttot;
+        siter = L.siter;
+    }
+    /* every thread has read the strip record before thread 0 may write it */
+    __syncthreads();
+    int status = 0;
+    bool stopped = false;
+    while (ttot < io.dtf) {
+        int rv = be_strip_solve<Net>(act, c, nstrip, u, at, rt, sc, dt, ts, cfg.max_sweeps, T,
+                                     &first_bad);
+        bool neg = false;
+        if (act)
+            for (int i = 0; i < N; i++) neg = neg || dg_lt0(u[i]);
+        if (__syncthreads_or(neg)) rv = 1;
+        if (rv == 0) {
+            if (siter == cfg.max_substeps) {
+                status = 1;
+                break;
+            }
+            siter++;
+            ttot += dt;
+            const double grown = dt * 1.1, rest = io.dtf - ttot;
+            dt = grown < rest ? grown : rest;
+            if (io.stop_after_accept && act) {
+                double *dp = io.dump + cell * (N + 1);
+                for (int i = 0; i < N; i++) dp[i] = prev[i];
+                dp[N] = T;
+            }
+            if (act)
+                for (int i = 0; i < N; i++) {
+                    prev[i] = u[i];
+                    if (dg_lt_pos(u[i], cfg.floor_value)) u[i] = cfg.floor_value;
+                }
+            if (io.stop_after_accept && ttot < io.dtf) {
+                stopped = true;
+                break;
+            }
+        } else {
+            dt /= 2.0;
+            if (act)
+                for (int i = 0; i < N; i++) u[i] = prev[i];
+            if (dt / io.dtf < cfg.dt_ratio_floor) {
+                status = 2;
+                break;
+            }
+        }
+    }
+    if (stopped) {
+        if (act) {
+            double *r = io.rec + cell * RL;
+            for (int i = 0; i < N; i++) {
+                r[i] = u[i];
+                r[N + i] = prev[i];
+                r[2 * N + i] = sc[i];
+                r[3 * N + i] = at[i];
+            }
+        }
+        if (c == 0) {
+            L.dt = dt;
+            L.ttot = ttot;
+            L.siter = siter;
+            L.dumped = 1;
+        }
+        return;
+    }
+    if (act) {
+        if (!Net::INPUT_IS_NUMBER) {
+            for (int i = 0; i < N; i++) {
+                if (i == Net::IGE) continue;
+                u[i] = u[i] * Net::unit(i);
+                at[i] = at[i] * Net::unit(i);
+            }
+        }
+        for (int i = 0; i < N; i++) {
+            io.input[cell * N + i] = u[i];
+            io.atol[cell * N + i] = at[i];
+        }
+    }
+    if (c == 0) {
+        /* an evolve that ended right after an accepted substep still hands
+         * that substep's dump to the host */
+        L.dumped = io.stop_after_accept && status == 0 && siter > 0 && !(ttot < io.dtf) ? 1 : 0;
+        L.dt = dt;
+        L.ttot = ttot;
+        L.siter = siter;
+        L.status = status;
+        L.done = 1;
+    }
+}
+
 /* Outputs of run_strip_kernel; the trajectory arrays may be null. */
 struct RunOut {
     double *ttot, *dt;   /* [1] */

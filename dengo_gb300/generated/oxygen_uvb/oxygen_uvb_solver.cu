@@ -25,6 +25,9 @@ struct Net {
     static constexpr int NZ_LEN = 100;
     static constexpr bool INPUT_IS_NUMBER = false;
     static constexpr bool HAS_Z = true;
+    /* the network's write_intermediate_solutions: lockstep dengo_evolve
+     * writes oxygen_uvb_intermediate_%06d.dgt after every accepted substep */
+    static constexpr bool WRITE_INTERMEDIATE = false;
 
     /* weight * 1.67e-24, the mass <-> number density factor
      * (rates_and_rate_tables.C.template:158-169) */
@@ -1686,6 +1689,11 @@ int oxygen_uvb_solve_cells_host(oxygen_uvb_data *data, const dengo_cell_batch *b
 }
 
 double oxygen_uvb_last_solve_ms(oxygen_uvb_data *data) { return dgnet_oxygen_uvb::Api::last_solve_ms(data); }
+
+int oxygen_uvb_set_solver_config(oxygen_uvb_data *data, const dengo_solver_config *cfg)
+{
+    return dgnet_oxygen_uvb::Api::set_config(data, cfg);
+}
 
 int oxygen_uvb_run_strip(oxygen_uvb_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

@@ -25,6 +25,9 @@ struct Net {
     static constexpr int NZ_LEN = 0;
     static constexpr bool INPUT_IS_NUMBER = false;
     static constexpr bool HAS_Z = false;
+    /* the network's write_intermediate_solutions: lockstep dengo_evolve
+     * writes primordial_intermediate_%06d.dgt after every accepted substep */
+    static constexpr bool WRITE_INTERMEDIATE = false;
 
     /* weight * 1.67e-24, the mass <-> number density factor
      * (rates_and_rate_tables.C.template:158-169) */
@@ -1036,6 +1039,11 @@ int primordial_solve_cells_host(primordial_data *data, const dengo_cell_batch *b
 }
 
 double primordial_last_solve_ms(primordial_data *data) { return dgnet_primordial::Api::last_solve_ms(data); }
+
+int primordial_set_solver_config(primordial_data *data, const dengo_solver_config *cfg)
+{
+    return dgnet_primordial::Api::set_config(data, cfg);
+}
 
 int primordial_run_strip(primordial_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

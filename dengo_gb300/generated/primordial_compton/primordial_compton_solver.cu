@@ -25,6 +25,9 @@ struct Net {
     static constexpr int NZ_LEN = 0;
     static constexpr bool INPUT_IS_NUMBER = false;
     static constexpr bool HAS_Z = false;
+    /* the network's write_intermediate_solutions: lockstep dengo_evolve
+     * writes primordial_compton_intermediate_%06d.dgt after every accepted substep */
+    static constexpr bool WRITE_INTERMEDIATE = false;
 
     /* weight * 1.67e-24, the mass <-> number density factor
      * (rates_and_rate_tables.C.template:158-169) */
@@ -1041,6 +1044,11 @@ int primordial_compton_solve_cells_host(primordial_compton_data *data, const den
 }
 
 double primordial_compton_last_solve_ms(primordial_compton_data *data) { return dgnet_primordial_compton::Api::last_solve_ms(data); }
+
+int primordial_compton_set_solver_config(primordial_compton_data *data, const dengo_solver_config *cfg)
+{
+    return dgnet_primordial_compton::Api::set_config(data, cfg);
+}
 
 int primordial_compton_run_strip(primordial_compton_data *data, double tf, int niter, double z, double *input, double *rtol,
                       double *atol, int nstrip, double *ttot, double *dt, double *traj, double *traj_T,

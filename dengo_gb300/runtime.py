@@ -20,6 +20,7 @@ P_I = C.POINTER(C.c_int)
 
 DENGO_OK, DENGO_MAX_SUBSTEPS, DENGO_DT_UNDERFLOW = 0, 1, 2
 DENGO_FP64, DENGO_MIXED = 0, 1
+DENGO_EVOLVE_LOCKSTEP, DENGO_EVOLVE_PER_CELL = 0, 1
 SCHED_AUTO, SCHED_PER_THREAD, SCHED_STRIDE, SCHED_QUEUE = 0, 1, 2, 3
 
 
@@ -29,7 +30,8 @@ class SolverConfig(C.Structure):
                 ("dt_ratio_floor", C.c_double), ("floor_value", C.c_double),
                 ("precision", C.c_int), ("schedule", C.c_int),
                 ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int),
-                ("sweep_budget", C.c_int), ("tail_grid", C.c_int)]
+                ("sweep_budget", C.c_int), ("tail_grid", C.c_int),
+                ("evolve_mode", C.c_int), ("write_intermediate", C.c_int)]
 
 
 class CellBatch(C.Structure):
@@ -70,6 +72,7 @@ def _declare(lib, n):
         "%s_solve_cells_host" % n: (C.c_int, [C.c_void_p, C.POINTER(CellBatch), C.c_double,
                                               C.POINTER(SolverConfig)]),
         "%s_last_solve_ms" % n: (C.c_double, [C.c_void_p]),
+        "%s_set_solver_config" % n: (C.c_int, [C.c_void_p, C.POINTER(SolverConfig)]),
         "calculate_rhs_%s" % n: (C.c_int, [P_D, P_D, C.c_int, C.c_int, C.c_void_p]),
         "calculate_jacobian_%s" % n: (C.c_int, [P_D, P_D, C.c_int, C.c_int, C.c_void_p]),
         "%s_calculate_temperature" % n: (None, [C.c_void_p, P_D, C.c_int, C.c_int]),
@@ -158,11 +161,23 @@ class Solver:
         cfg.precision, cfg.schedule, cfg.block, cfg.grid = DENGO_FP64, SCHED_AUTO, 0, 0
         cfg.warps_per_cell = 4
         cfg.sweep_budget, cfg.tail_grid = 2000, 0
+        cfg.evolve_mode, cfg.write_intermediate = DENGO_EVOLVE_LOCKSTEP, -1
         return cfg
+
+    def set_config(self, config=None):
+        """``<name>_set_solver_config``: the configuration ``evolve`` (and the
+        other reference-named entry points) use; ``None`` restores the
+        default."""
+        fn = getattr(self.lib, "%s_set_solver_config" % self.name)
+        rc = fn(self.data, None if config is None else C.byref(config))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
 
     # ---- reference-shaped host entry points ----------------------------
     def evolve(self, state, dtf, dt=-1.0, z=-1.0, rtol=None, atol=None):
-        """``dengo_evolve_<name>`` on a (cells, N) AoS float64 array (copied).
+        """``dengo_evolve_<name>`` on a (cells, N) AoS float64 array (copied):
+        the reference's lockstep strips unless ``set_config`` chose per-cell
+        dt control.
 
         Returns ``(state, atol, ttot, dt)``; rtol/atol default to the
         reference's Cython rule: rtol = 1e-6, atol = 1e-6 * state."""

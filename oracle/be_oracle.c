@@ -155,6 +155,15 @@ int dgo_BE_chem_solve(dgo_rhs_f f, dgo_jac_f J, double *u, double dt,
     return unsolved ? 1 : 0;
 }
 
+static dgo_intermediate_f dgo_hook;
+static void *dgo_hook_ctx;
+
+void dgo_set_intermediate_hook(dgo_intermediate_f f, void *ctx)
+{
+    dgo_hook = f;
+    dgo_hook_ctx = ctx;
+}
+
 /* rates_and_rate_tables.C.template:149-274 */
 double dgo_evolve(const dgo_network *net, void *data, double dtf, double *dtp,
                   double z, double *input, double *rtol, double *atol,
@@ -210,6 +219,9 @@ double dgo_evolve(const dgo_network *net, void *data, double dtf, double *dtp,
             if (st) st->substeps_ok++;
             ttot += dt;
             dt = DGO_MIN(dt * 1.1, dtf - ttot);
+            /* C.template:212-241: the intermediate file holds prev (not yet
+             * updated), data->Ts, ttot and dt */
+            if (dgo_hook) dgo_hook(dgo_hook_ctx, siter, prev, net->Ts(data), dims, N, ttot, dt);
             for (i = 0; i < n; i++) prev[i] = input[i];
             for (i = 0; i < n; i++)
                 if (input[i] < floor_value) input[i] = floor_value;

@@ -72,6 +72,15 @@ double dgo_evolve(const dgo_network *net, void *data, double dtf, double *dt,
                   double z, double *input, double *rtol, double *atol,
                   long long dims, const dgo_config *cfg, dgo_stats *st);
 
+/* Called by dgo_evolve where the reference writes <name>_intermediate_%06d
+ * (rates_and_rate_tables.C.template:212-241), with what it writes: the
+ * accepted substep's number, prev (the state before that substep, number
+ * densities, dims x N), the data's Ts, ttot and the next dt.  NULL: off. */
+typedef void (*dgo_intermediate_f)(void *ctx, int siter, const double *prev,
+                                   const double *Ts, long long dims, int nchem,
+                                   double ttot, double dt);
+void dgo_set_intermediate_hook(dgo_intermediate_f f, void *ctx);
+
 /* Per-cell driver: every cell is its own strip (dims = 1), the reference's
  * dengo_evolve called once per cell.  AoS in/out like the reference.
  * dt[c] < 0 selects dtf[c]/1e5.  Runs cells on `nthreads` OpenMP threads. */

@@ -129,24 +129,49 @@ class Stats(C.Structure):
                 ("sweeps", C.c_longlong), ("status", C.c_int)]
 
 
-def evolve_strip(orc, tables_in_order, state, dtf, z=-1.0, dt=-1.0):
+_HOOK_F = C.CFUNCTYPE(None, C.c_void_p, C.c_int, P_D, P_D, C.c_longlong, C.c_int, C.c_double,
+                      C.c_double)
+
+
+def evolve_strip(orc, tables_in_order, state, dtf, z=-1.0, dt=-1.0, intermediate=False,
+                 rtol=None, atol=None, max_substeps=50000):
     """dengo_evolve_<name> over one strip in lockstep (dims = the number of
     cells; the reference's own semantics for dims > 1): one dt and one
-    Newton loop for the whole strip.  Returns a dict."""
+    Newton loop for the whole strip.  Returns a dict; with ``intermediate``
+    also ``intermediate``: one dict per accepted substep holding what the
+    reference writes to <name>_intermediate_%06d (siter, species = prev,
+    T, time, timestep)."""
     st = np.ascontiguousarray(state, np.float64).copy()
-    rt = np.full_like(st, 1e-6)
-    at = 1e-6 * st
+    rt = np.full_like(st, 1e-6) if rtol is None else np.ascontiguousarray(rtol, np.float64).copy()
+    at = (1e-6 * st) if atol is None else np.ascontiguousarray(atol, np.float64).copy()
     keep, tp = orc._tables(tables_in_order)
     net = Network.in_dll(orc.lib, "dgo_%s_network" % orc.name)
     data = net.alloc_data(tp)
+    dumps = []
+
+    def hook(ctx, siter, prev, Ts, dims, nchem, ttot, dt_next):
+        dumps.append(dict(siter=siter,
+                          species=np.ctypeslib.as_array(prev, (dims, nchem)).copy(),
+                          T=np.ctypeslib.as_array(Ts, (dims,)).copy(),
+                          time=ttot, timestep=dt_next))
+
+    cb = _HOOK_F(hook)
+    orc.lib.dgo_set_intermediate_hook.argtypes = [_HOOK_F, C.c_void_p]
+    if intermediate:
+        orc.lib.dgo_set_intermediate_hook(cb, None)
     try:
         d = C.c_double(dt)
-        cfg = orc.config()
+        cfg = orc.config(max_substeps=max_substeps)
         ttot = orc.lib.dgo_evolve(orc.net_addr, data, float(dtf), C.byref(d), float(z), _dp(st),
                                   _dp(rt), _dp(at), st.shape[0], C.byref(cfg), None)
     finally:
+        if intermediate:
+            orc.lib.dgo_set_intermediate_hook(_HOOK_F(), None)
         net.free_data(data)
-    return dict(state=st, atol=at, ttot=ttot, dt=d.value)
+    out = dict(state=st, atol=at, ttot=ttot, dt=d.value)
+    if intermediate:
+        out["intermediate"] = dumps
+    return out
 
 
 def run_strip(orc, tables_in_order, input_number, tf, niter, z=-1.0, trajectories=False):
@@ -186,11 +211,13 @@ class Reference:
     """The reference's own generated solver, built by oracle/ref_build.py
     (only where the reference checkout exists)."""
 
-    def __init__(self, name="primordial"):
-        path = os.path.join(REF, "libref_%s.so" % name)
+    def __init__(self, name="primordial", intermediate=False):
+        tag = name + ("_intermediate" if intermediate else "")
+        path = os.path.join(REF, "libref_%s.so" % tag)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
-        os.environ["DGO_REF_TABLE_DIR"] = os.path.join(REF, name)
+        # the tables, and (intermediate build) its intermediate files, live here
+        os.environ["DGO_REF_TABLE_DIR"] = os.path.join(REF, tag)
         self.lib = C.CDLL(path)
         self.lib.ref_evolve_cells.argtypes = [P_D, P_D, C.c_double, P_D, P_D, P_D, C.c_longlong,
                                               P_D, C.c_int]

@@ -287,23 +287,29 @@ void ref_evolve_cells(const double *dtf, double *dt, double z, double *input, do
 """
 
 
-def build(name="primordial"):
+def build(name="primordial", intermediate=False):
     """Render and compile one network in a fresh interpreter (the reference's
-    registries are module globals, so networks are built one per process)."""
+    registries are module globals, so networks are built one per process).
+    ``intermediate``: render it with ``write_intermediate_solutions`` set, so
+    that its dengo_evolve writes <name>_intermediate_%06d files (the
+    library is libref_<name>_intermediate.so)."""
     if name not in ("primordial", "primordial_compton", "oxygen", "oxygen_uvb"):
         raise ValueError("networks rendered with the reference here: primordial, "
                          "primordial_compton, oxygen, oxygen_uvb")
     if not os.path.isdir(os.path.join(REF_ROOT, "dengo")):
         raise FileNotFoundError("reference checkout not found at %s" % REF_ROOT)
+    tag = name + ("_intermediate" if intermediate else "")
     if "dengo" in sys.modules:
-        lib = os.path.join(OUT, "libref_%s.so" % name)
-        subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
+        lib = os.path.join(OUT, "libref_%s.so" % tag)
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), name] +
+                              (["intermediate"] if intermediate else []))
         return lib
     if name.startswith("primordial"):
         net = _reference_primordial(with_compton=(name == "primordial_compton"))
     else:
         net = _reference_oxygen("HM12" if name == "oxygen_uvb" else None)
-    odir = os.path.join(OUT, name)
+    net.write_intermediate_solutions = bool(intermediate)
+    odir = os.path.join(OUT, tag)
     os.makedirs(odir, exist_ok=True)
     net.write_solver(name, output_dir=odir, ode_solver_source=None)
     # offsets of the rs_* scratch arrays, in reaction-then-cooling order
@@ -314,7 +320,7 @@ def build(name="primordial"):
     harness = os.path.join(odir, "harness.cpp")
     with open(harness, "w") as f:
         f.write(HARNESS % dict(n=name, rs=rs))
-    lib = os.path.join(OUT, "libref_%s.so" % name)
+    lib = os.path.join(OUT, "libref_%s.so" % tag)
     cmd = ["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-w",
            "-I", os.path.join(HERE, "hdf5_shim"), "-I", odir,
            os.path.join(odir, "%s_solver.C" % name),
@@ -347,4 +353,5 @@ def build_cython_driver(name="primordial"):
 
 
 if __name__ == "__main__":
-    print(build(*(sys.argv[1:] or ["primordial"])))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else "primordial",
+                intermediate=sys.argv[2:] == ["intermediate"]))

@@ -19,6 +19,11 @@ Run where the reference checkout exists (it is read, never modified):
    * ``be_*``: one ``BE_chem_solve`` over an 8-cell strip in lockstep;
    * ``lock_*``: ``dengo_evolve_primordial`` over an 8-cell strip (dims = 8,
      the reference's lockstep semantics);
+   (``python tests/golden/make_golden.py intermediate`` writes
+   ``primordial_intermediate_golden.npz``: that strip's intermediate files,
+   from the reference rendered with ``write_intermediate_solutions``;
+   ``oxygen``, ``oxygen_uvb``, ``primordial_compton`` and ``run`` the other
+   networks' and the Cython driver's vectors)
    * ``tables``: every rate and cooling table the reference wrote.
 3. Stores the reference's printed expressions (RHS rows, Jacobian entries,
    T(ge), dT/dge, mass density) in ``primordial_expressions.json`` after
@@ -245,8 +250,51 @@ def make_run():
     print("wrote primordial_run_golden.npz")
 
 
+def make_intermediate():
+    """Golden vectors of the reference's intermediate files: the primordial
+    network rendered with ``write_intermediate_solutions`` set
+    (oracle/ref_build.py build(intermediate=True)); its
+    ``dengo_evolve_primordial`` over an 8-cell config-1 strip (dims = 8, the
+    ``lock_*`` inputs) writes ``primordial_intermediate_%06d.h5`` after every
+    accepted substep (rates_and_rate_tables.C.template:212-241).  Stored in
+    ``primordial_intermediate_golden.npz``: the inputs, the final state, and
+    per file its number, the species (the state before that substep, number
+    densities), T, and the time and timestep attributes."""
+    import glob
+    import shutil
+    import ref_build
+    from oracle import Reference
+    ref_build.build("primordial", intermediate=True)
+    ref = Reference("primordial", intermediate=True)
+    outdir = os.environ["DGO_REF_TABLE_DIR"]
+    for old in glob.glob(os.path.join(outdir, "primordial_intermediate_*.h5.d")):
+        shutil.rmtree(old)
+    d = ref.lib.ref_setup()
+    st, dtf = primordial_cells(8, "config1", seed=99)
+    x = st.copy()
+    rt = np.full_like(x, 1e-6)
+    at = 1e-6 * x
+    dt = C.c_double(-1.0)
+    ttot = ref.lib.ref_evolve(d, float(dtf.min()), C.byref(dt), -1.0, dp(x), dp(rt), dp(at), 8)
+    dirs = sorted(glob.glob(os.path.join(outdir, "primordial_intermediate_*.h5.d")))
+    species = ("H2_1", "H2_2", "H_1", "H_2", "H_m0", "He_1", "He_2", "He_3", "de", "ge")
+    out = dict(inp=st, dtf=np.array(dtf.min()), state=x, atol=at, ttot=np.array(ttot),
+               dt=np.array(dt.value))
+    out["siter"] = np.array([int(p.rsplit("_", 1)[1].split(".")[0]) for p in dirs])
+    out["species"] = np.array([np.stack([np.fromfile(os.path.join(p, s + ".f64"))
+                                         for s in species], axis=1) for p in dirs])
+    out["T"] = np.array([np.fromfile(os.path.join(p, "T.f64")) for p in dirs])
+    out["time"] = np.array([np.fromfile(os.path.join(p, "@time.f64"))[0] for p in dirs])
+    out["timestep"] = np.array([np.fromfile(os.path.join(p, "@timestep.f64"))[0] for p in dirs])
+    for p in dirs:
+        shutil.rmtree(p)
+    np.savez_compressed(os.path.join(HERE, "primordial_intermediate_golden.npz"), **out)
+
+
 if __name__ == "__main__" and len(sys.argv) > 1:
-    if sys.argv[1] == "oxygen":
+    if sys.argv[1] == "intermediate":
+        make_intermediate()
+    elif sys.argv[1] == "oxygen":
         make_ion("oxygen")
     elif sys.argv[1] == "oxygen_uvb":
         make_ion("oxygen_uvb", zs=(0.0, 2.5, 9.0, 20.0))

@@ -259,6 +259,69 @@ extern "C" int hx_run_strip(double *input, const double *rtol, double *atol, int
     *dt = sc[1];
     return iters[0];
 }
+
+/* dengo_evolve_<n> in lockstep (evolve_lockstep_kernel) on one strip of at
+ * most 1024 cells (AoS, mass densities + ge), launch after launch as the
+ * library runs it; with dump the kernel stops after every accepted substep
+ * and each of its dumps (prev, T, time, timestep, substep number) is
+ * appended to the output arrays (max_dumps of them).  Returns the number of
+ * dumps; *dt in: the initial step (< 0: dtf/1e5), out: the last. */
+extern "C" int hx_evolve_lockstep(double *input, const double *rtol, double *atol, int dims,
+                                  double dtf, double *dt, double z, const double *const *tables,
+                                  int dump, int max_dumps, double *d_species, double *d_T,
+                                  double *d_time, double *d_dt, int *d_siter, double *ttot,
+                                  int *status)
+{
+    static Net::Data data;
+    Net::setup_bins(&data);
+    const int nbins = Net::NT_LEN - 1;
+    std::vector<double2> pairs((size_t)nbins * NT);
+    for (int b = 0; b < nbins; b++)
+        for (int k = 0; k < NT; k++)
+            pairs[(size_t)b * NT + k] = make_double2(tables[k][b], tables[k][b + 1] - tables[k][b]);
+    dg::TableSet ts{pairs.data(), nbins, log(data.bounds[0]), data.dbin, data.idbin,
+                    data.bounds[0], data.bounds[1], z, {}};
+    constexpr int RL = dg::rec_len<NN>();
+    std::vector<double> rec((size_t)dims * RL), dbuf((size_t)dims * (NN + 1));
+    dg::LockStrip L{*dt, 0.0, 0, 0, 0, 0};
+    dg::LockIO io{input, atol, rtol, dims, 1024, dtf, &L, rec.data(), dbuf.data(), 0, dump};
+    const dg::KernelCfg kc{10, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 0};
+    const int threads = ((dims + 31) / 32) * 32;
+    int nd = 0;
+    for (int launch = 0;; launch++) {
+        io.resume = launch > 0;
+        blockIdx.x = 0;
+        gridDim.x = 1;
+        blockDim.x = threads;
+        hx_barrier cta(threads), warp0(32);
+        hx_cta = &cta;
+        hx_warp0 = &warp0;
+        std::vector<std::thread> lanes;
+        for (int t = 0; t < threads; t++)
+            lanes.emplace_back([=]() {
+                threadIdx.x = t;
+                dg::evolve_lockstep_kernel<Net>(io, ts, kc);
+            });
+        for (auto &th : lanes) th.join();
+        if (!dump) break;
+        if (L.dumped && nd < max_dumps) {
+            for (int c = 0; c < dims; c++) {
+                for (int i = 0; i < NN; i++)
+                    d_species[((size_t)nd * dims + c) * NN + i] = dbuf[(size_t)c * (NN + 1) + i];
+                d_T[(size_t)nd * dims + c] = dbuf[(size_t)c * (NN + 1) + NN];
+            }
+            d_time[nd] = L.ttot;
+            d_dt[nd] = L.dt;
+            d_siter[nd] = L.siter;
+            nd++;
+        }
+        if (L.done) break;
+    }
+    *ttot = L.ttot;
+    *dt = L.dt;
+    *status = L.status;
+    return nd;
+}
 '''
 
 DRIVER = r'''
@@ -444,6 +507,52 @@ def evolve_in_subprocess(so, tables, state, dtf, timeout=600, **kw):
                 "r = he.evolve(he._bind(ctypes.CDLL(%r)), tabs, a['state'], a['dtf'], **%r); "
                 "np.savez(%r, **r)" % (os.path.dirname(os.path.abspath(__file__)), inp,
                                        len(tables), so, kw, out))
+        subprocess.run([sys.executable, "-c", code], check=True, timeout=timeout)
+        with np.load(out) as r:
+            return {k: r[k] for k in r.files}
+
+
+def lockstep_in_subprocess(so, tables, state, dtf, dump=False, max_dumps=4096, z=-1.0,
+                           timeout=600):
+    """``dengo_evolve_<n>`` in lockstep (evolve_lockstep_kernel) from the host
+    build at path ``so`` on one strip (AoS mass densities + ge, at most 1024
+    cells), rtol = 1e-6, atol = 1e-6 x state, in a child process killed after
+    ``timeout`` seconds.  Returns the final state, atol, ttot, dt, status and
+    (``dump``) the intermediate dumps: ``siter``, ``species`` [k][cells][N],
+    ``T`` [k][cells], ``time``, ``timestep``."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        inp, out = os.path.join(d, "in.npz"), os.path.join(d, "out.npz")
+        np.savez(inp, state=state, **{"table%d" % k: t for k, t in enumerate(tables)})
+        code = r'''
+import ctypes as C, numpy as np
+a = np.load(%(inp)r)
+tabs = [np.ascontiguousarray(a["table%%d" %% k]) for k in range(%(nt)d)]
+P = C.POINTER(C.c_double)
+PI = C.POINTER(C.c_int)
+lib = C.CDLL(%(so)r)
+f = lib.hx_evolve_lockstep
+f.restype = C.c_int
+f.argtypes = [P, P, P, C.c_int, C.c_double, P, C.c_double, C.POINTER(P), C.c_int, C.c_int,
+              P, P, P, P, PI, P, PI]
+st = np.ascontiguousarray(a["state"], np.float64).copy()
+dims, n = st.shape
+rt = np.full_like(st, 1e-06)
+at = st * 1e-06
+m = %(maxd)d if %(dump)d else 1
+sp, T = np.zeros((m, dims, n)), np.zeros((m, dims))
+tm, ts, si = np.zeros(m), np.zeros(m), np.zeros(m, np.int32)
+ttot, dt, status = np.zeros(1), np.array([-1.0]), np.zeros(1, np.int32)
+tp = (P * len(tabs))(*[x.ctypes.data_as(P) for x in tabs])
+p = lambda x: x.ctypes.data_as(P)
+k = f(p(st), p(rt), p(at), dims, %(dtf)r, p(dt), %(z)r, tp, %(dump)d, m, p(sp), p(T), p(tm),
+      p(ts), si.ctypes.data_as(PI), p(ttot), status.ctypes.data_as(PI))
+np.savez(%(out)r, state=st, atol=at, ttot=ttot[0], dt=dt[0], status=status[0], siter=si[:k],
+         species=sp[:k], T=T[:k], time=tm[:k], timestep=ts[:k])
+''' % dict(inp=inp, nt=len(tables), so=so, maxd=int(max_dumps), dump=int(dump),
+             dtf=float(dtf), z=float(z), out=out)
         subprocess.run([sys.executable, "-c", code], check=True, timeout=timeout)
         with np.load(out) as r:
             return {k: r[k] for k in r.files}

@@ -82,10 +82,19 @@ def test_gpu_matches_oracle(solver, oracle, config, n):
 
 
 def test_dengo_evolve_scalar_dtf(solver, oracle):
+    """dengo_evolve_<n> in the per-cell evolve mode (tests/test_lockstep.py
+    covers the default, the reference's lockstep strips)."""
+    from dengo_gb300.runtime import DENGO_EVOLVE_PER_CELL, Solver
     from dengo_gb300.workloads import primordial_cells
     state, dtf = primordial_cells(16, "config1", seed=11)
     d = float(np.median(dtf))
-    st, at, ttot, dt = solver.evolve(state, d)
+    cfg = Solver.default_config()
+    cfg.evolve_mode = DENGO_EVOLVE_PER_CELL
+    solver.set_config(cfg)
+    try:
+        st, at, ttot, dt = solver.evolve(state, d)
+    finally:
+        solver.set_config(None)
     ref = oracle.evolve_cells(solver._tables, state, d)
     err = rel_err(st[ref["status"] == 0], ref["state"][ref["status"] == 0])
     assert err.max(initial=0.0) <= RTOL
