@@ -73,6 +73,10 @@ class NetworkSpec:
     jac_part: dict = field(default_factory=dict)      # {NP: [var][eq] part}
     stop_time: str = "3.1557e13"   # literal: the network's stop_time (the main driver's dtf)
     write_intermediate: bool = False  # the network's write_intermediate_solutions
+    # integer basis of the linear combinations of species the reactions
+    # conserve (left null space of the stoichiometry), one list of N
+    # coefficients per invariant (0 for ge)
+    conservation: list = field(default_factory=list)
 
     @property
     def N(self):
@@ -129,6 +133,38 @@ def _lit(v):
     return str(v)
 
 
+def conservation_basis(net, ordered):
+    """Integer basis of the species combinations every reaction conserves:
+    the null space of the stoichiometry matrix (reactions x species, ge
+    excluded), each vector scaled to coprime integers.  For the primordial
+    network these are the H and He nuclei; the reference's k12
+    (H2 + e -> 2 H+ + e, dengo/primordial_rates.py:191) does not conserve
+    charge, so charge is not among them, while the ion-by-ion networks also
+    conserve a charge combination."""
+    chem = [s.name for s in ordered if s.name != "ge"]
+    rows = []
+    for rn in sorted(net.reactions):
+        r = net.reactions[rn]
+        rows.append([sympy.nsimplify(sum(n for n, x in r.right_side if x.name == c) -
+                                     sum(n for n, x in r.left_side if x.name == c))
+                     for c in chem])
+    if not rows:
+        return []
+    out = []
+    for v in sympy.Matrix(rows).nullspace():
+        den = sympy.ilcm(*[sympy.fraction(x)[1] for x in v])
+        ints = [int(x * den) for x in v]
+        g = 0
+        for x in ints:
+            g = sympy.igcd(g, x)
+        ints = [x // g for x in ints]
+        if sum(ints) < 0:
+            ints = [-x for x in ints]
+        full = iter(ints)
+        out.append([0 if s.name == "ge" else next(full) for s in ordered])
+    return out
+
+
 def network_spec(net, name):
     species = []
     for i, s in enumerate(sorted(net.required_species)):
@@ -182,6 +218,7 @@ def network_spec(net, name):
         input_is_number=bool(getattr(net, "input_is_number", False)),
         stop_time=repr(float(net.stop_time)),
         write_intermediate=bool(getattr(net, "write_intermediate_solutions", False)),
+        conservation=conservation_basis(net, ordered),
         mass_density_ref=ccode_ref(md), mass_density_dev=ccode_device(md),
         T_ref=ccode_ref(T), T_dev=ccode_device(T),
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),

@@ -552,6 +552,7 @@ struct Api {
             io.order = g->order;
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
+        kc.cons_tol = cfg.conservation_tol > 0.0 ? cfg.conservation_tol : 0.0;
         if (cfg.sweep_budget <= 0 || b->ncells <= 0)
             return launch_engine<Net>(g, io, ts, kc, cfg, st, g->queue);
         return solve_redistributed(g, io, ts, kc, cfg, st);
@@ -667,6 +668,7 @@ struct Api {
             io.order = order;
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
+        kc.cons_tol = cfg.conservation_tol > 0.0 ? cfg.conservation_tol : 0.0;
         return launch_engine<Net>(g, io, ts, kc, cfg, st, queue);
     }
 
@@ -1278,6 +1280,9 @@ extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg)
      * as the network was generated */
     cfg->evolve_mode = DENGO_EVOLVE_LOCKSTEP;
     cfg->write_intermediate = -1;
+    /* mixed precision: FP64 re-solve of a converged cell whose invariants
+     * drifted by more than this (relative) */
+    cfg->conservation_tol = 1e-9;
 }
 
 #endif

@@ -92,13 +92,18 @@ struct KernelCfg {
      * than competing CTAs */
     const unsigned int *resume_count;
     int nsm;
+    /* mixed precision: the FP64 conservation check of every converged cell
+     * -- a relative drift of any invariant beyond cons_tol re-solves the
+     * cell with FP64 linear solves; 0: no check */
+    double cons_tol;
 };
 
 /* Suspension record of a cell at a substep boundary: state y, prev, scale,
  * atol (all unscaled number densities), dt, ttot, accepted substeps, sweeps,
- * failed substeps -- everything the driver carries between substeps. */
+ * failed substeps, and whether the cell is being re-solved in FP64 --
+ * everything the driver carries between substeps. */
 template <int N>
-__host__ __device__ constexpr int rec_len() { return 4 * N + 5; }
+__host__ __device__ constexpr int rec_len() { return 4 * N + 6; }
 
 template <class Net, int BLOCK, bool MIXED = false>
 struct Lane {
@@ -325,6 +330,40 @@ __device__ __forceinline__ void to_number_density(double (&y)[Net::N], double (&
     }
 }
 
+/* The FP64 conservation check of the mixed-precision solve: the invariants
+ * of the network (Net::invariants, the species combinations its reactions
+ * conserve) of a converged cell's final state y (number densities) against
+ * those of its input, re-read from io.state and converted as at the cell's
+ * start.  True when every relative drift |I(y) - I(y0)| / sum |c_s y0_s| is
+ * within tol (a drift of exactly 0 always is).  The reference's own FP64
+ * solve keeps these drifts near 1e-12 at most. */
+template <class Net>
+__device__ __forceinline__ bool conserved(const CellIO &io, long long cell,
+                                          const double (&y)[Net::N], double tol)
+{
+    constexpr int N = Net::N;
+    constexpr int NC = Net::NCONS > 0 ? Net::NCONS : 1;
+    if (Net::NCONS == 0) return true;
+    double y0[N], dummy[N];
+#pragma unroll
+    for (int s = 0; s < N; s++) {
+        y0[s] = io.state[cell * io.cs + s * io.ss];
+        dummy[s] = 0.0;
+    }
+    to_number_density<Net>(y0, dummy);
+    Net::electrons(y0);
+    double I0[NC], A0[NC], I1[NC], A1[NC];
+    Net::invariants(y0, I0, A0);
+    Net::invariants(y, I1, A1);
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < Net::NCONS; k++) {
+        const double d = fabs(I1[k] - I0[k]);
+        ok = ok && !(d > tol * A0[k]);
+    }
+    return ok;
+}
+
 /* MIXED = false: the reference's FP64 arithmetic throughout (bit-faithful).
  * MIXED = true: the Newton system is solved by MixedSolve (equilibrated FP32
  * LU + FP64 iterative refinement, dg_mixed.cuh), falling back to the FP64
@@ -372,6 +411,7 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
     }
     long long cell = 0;
     bool dense = false;   /* a scale is not a positive finite number */
+    bool fp64cell = false;  /* mixed: this cell is re-solved with FP64 linear solves */
 
     double u[N], u0[N], y[N];
     double dtf = 0, dt = 0, ttot = 0;
@@ -389,8 +429,10 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
         for (int i = 0; i < N; i++) u0[i] = u[i];
         isweep = 0;
     };
-    auto cell_begin = [&]() -> bool {
-        if (cfg.resume) {
+    /* from_record: continue a suspended cell (resume launch); else start it
+     * from the caller's input */
+    auto cell_begin = [&](bool from_record) -> bool {
+        if (from_record) {
             /* continue a suspended cell from its record */
             const double *rc = cfg.rec + cell * rec_len<N>();
             dense = false;
@@ -410,6 +452,7 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
             siter = (int)rc[4 * N + 2];
             nsweeps = (int)rc[4 * N + 3];
             nfail = (int)rc[4 * N + 4];
+            fp64cell = rc[4 * N + 5] != 0.0;
             if (!(ttot < dtf)) return false;
             substep_begin();
             return true;
@@ -478,13 +521,15 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
         rc[4 * N + 2] = siter;
         rc[4 * N + 3] = nsweeps;
         rc[4 * N + 4] = nfail;
+        rc[4 * N + 5] = fp64cell ? 1.0 : 0.0;
         io.status[cell] = ST_SUSPENDED;
     };
     auto fetch = [&]() {
         while (qi < io.ncells) {
             cell = io.order ? (long long)io.order[qi] : qi;
             if (cell < 0) break; /* end of a resume list */
-            if (cell_begin()) {
+            fp64cell = false;
+            if (cell_begin(cfg.resume != 0)) {
                 active = true;
                 return;
             }
@@ -526,7 +571,7 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 #pragma unroll
                     for (int i = 0; i < N; i++) u[i] = y[i] * INV[i];
                     bool solved = false;
-                    if (MIXED && !dense_j) {
+                    if (MIXED && !dense_j && !fp64cell) {
                         double xs[N];
                         solved = MixedSolve<Net, BLOCK>{J, JF}(f, xs);
                         if (solved) {
@@ -598,6 +643,12 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
         if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
             substep_begin();
             continue;
+        }
+        if (MIXED && done == ST_OK && cfg.cons_tol != 0.0 && !fp64cell &&
+            !conserved<Net>(io, cell, y, cfg.cons_tol)) {
+            /* start the cell again from its input, FP64 linear solves */
+            fp64cell = true;
+            if (cell_begin(false)) continue;
         }
         if (done < 0) suspend();
         else cell_end(done);

@@ -60,9 +60,11 @@ struct SplitLayout {
     static constexpr size_t bytes() { return sizeof(double) * SLOTS * 32 + sizeof(int) * NINTS * 32 + 64; }
 };
 
-/* per-cell int flags; F_MIX: 0 FP64 elimination, 1 refining, 2 refined */
+/* per-cell int flags; F_MIX: 0 FP64 elimination, 1 refining, 2 refined;
+ * F_FP64: mixed precision, the cell is re-solved with FP64 linear solves
+ * (it failed the conservation check) */
 enum : int { F_ACT = 0, F_BIN = 1, F_OKR = 2, F_OKJ = 3, F_DENSE = 4, F_PIV = 5, F_SWEEP = 6,
-             F_MIX = 7, F_EPREV = 8, F_ROW = 10 };
+             F_MIX = 7, F_EPREV = 8, F_FP64 = 9, F_ROW = 10 };
 
 /* The FP64 elimination for a cell the mixed solve hands back (dense or
  * non-finite system); kept out of line because it is rarely taken and large. */
@@ -134,8 +136,10 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         }
         isweep = 0;
     };
-    auto cell_begin = [&]() -> bool {
-        if (cfg.resume) {
+    /* from_record: continue a suspended cell (resume launch); else start it
+     * from the caller's input */
+    auto cell_begin = [&](bool from_record) -> bool {
+        if (from_record) {
             /* continue a suspended cell from its record */
             const double *rc = cfg.rec + cell * rec_len<N>();
             dense = false;
@@ -154,6 +158,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             siter = (int)rc[4 * N + 2];
             nsweeps = (int)rc[4 * N + 3];
             nfail = (int)rc[4 * N + 4];
+            F(F_FP64) = rc[4 * N + 5] != 0.0;
             if (!(ttot < dtf)) return false;
             substep_begin();
             return true;
@@ -216,13 +221,15 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         rc[4 * N + 2] = siter;
         rc[4 * N + 3] = nsweeps;
         rc[4 * N + 4] = nfail;
+        rc[4 * N + 5] = F(F_FP64) ? 1.0 : 0.0;
         io.status[cell] = ST_SUSPENDED;
     };
     auto fetch = [&]() {
         while (qi < io.ncells) {
             cell = io.order ? (long long)io.order[qi] : qi;
             if (cell < 0) break; /* end of a resume list */
-            if (cell_begin()) {
+            F(F_FP64) = 0;
+            if (cell_begin(cfg.resume != 0)) {
                 active = true;
                 return;
             }
@@ -344,7 +351,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         if (MIXED) {
             using MS = MixedSolve<Net, 32>;
             const MS ms{J, JF};
-            const bool eq = do_lu && !F(F_DENSE);
+            const bool eq = do_lu && !F(F_DENSE) && !F(F_FP64);
             /* M1 (rows i = w mod NP): row scale exponent s_i, finiteness of
              * the row and of g_i, and the row's share of each column's
              * largest scaled exponent (MI(N + j), reset to NONE in P3) */
@@ -593,6 +600,15 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                 for (int i = 0; i < N; i++) Y[i] = y[i];
                 if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
                     substep_begin();
+                } else if (MIXED && done == ST_OK && cfg.cons_tol != 0.0 && !F(F_FP64) &&
+                           !conserved<Net>(io, cell, y, cfg.cons_tol)) {
+                    /* start the cell again from its input, FP64 linear solves */
+                    F(F_FP64) = 1;
+                    if (!cell_begin(false)) {
+                        cell_end(ST_OK);
+                        qi = queue ? (long long)atomicAdd(queue, 1ull) : qi + stride;
+                        fetch();
+                    }
                 } else {
                     if (done < 0) suspend();
                     else cell_end(done);

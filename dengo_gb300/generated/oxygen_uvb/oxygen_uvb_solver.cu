@@ -29,6 +29,24 @@ struct Net {
      * writes oxygen_uvb_intermediate_%06d.dgt after every accepted substep */
     static constexpr bool WRITE_INTERMEDIATE = false;
 
+    /* The species combinations the reactions conserve (a basis of the left
+     * null space of the stoichiometry); the mixed-precision solve checks
+     * them in FP64 at the end of every converged cell. */
+    static constexpr int NCONS = 4;
+    __host__ __device__ __forceinline__ static void invariants(const double (&y)[N], double *I,
+                                                               double *A)
+    {
+        (void)y; (void)I; (void)A;
+        I[0] = 1.0 * y[0] + 1.0 * y[1];
+        A[0] = 1.0 * fabs(y[0]) + 1.0 * fabs(y[1]);
+        I[1] = 1.0 * y[2] + 1.0 * y[3] + 1.0 * y[4];
+        A[1] = 1.0 * fabs(y[2]) + 1.0 * fabs(y[3]) + 1.0 * fabs(y[4]);
+        I[2] = 1.0 * y[5] + 1.0 * y[6] + 1.0 * y[7] + 1.0 * y[8] + 1.0 * y[9] + 1.0 * y[10] + 1.0 * y[11] + 1.0 * y[12] + 1.0 * y[13];
+        A[2] = 1.0 * fabs(y[5]) + 1.0 * fabs(y[6]) + 1.0 * fabs(y[7]) + 1.0 * fabs(y[8]) + 1.0 * fabs(y[9]) + 1.0 * fabs(y[10]) + 1.0 * fabs(y[11]) + 1.0 * fabs(y[12]) + 1.0 * fabs(y[13]);
+        I[3] = 1.0 * y[0] + 2.0 * y[2] + 1.0 * y[3] + 8.0 * y[5] + 7.0 * y[6] + 6.0 * y[7] + 5.0 * y[8] + 4.0 * y[9] + 3.0 * y[10] + 2.0 * y[11] + 1.0 * y[12] + 1.0 * y[14];
+        A[3] = 1.0 * fabs(y[0]) + 2.0 * fabs(y[2]) + 1.0 * fabs(y[3]) + 8.0 * fabs(y[5]) + 7.0 * fabs(y[6]) + 6.0 * fabs(y[7]) + 5.0 * fabs(y[8]) + 4.0 * fabs(y[9]) + 3.0 * fabs(y[10]) + 2.0 * fabs(y[11]) + 1.0 * fabs(y[12]) + 1.0 * fabs(y[14]);
+    }
+
     /* weight * 1.67e-24, the mass <-> number density factor
      * (rates_and_rate_tables.C.template:158-169) */
     __host__ __device__ static constexpr double unit(int s)

@@ -29,6 +29,20 @@ struct Net {
      * writes primordial_intermediate_%06d.dgt after every accepted substep */
     static constexpr bool WRITE_INTERMEDIATE = false;
 
+    /* The species combinations the reactions conserve (a basis of the left
+     * null space of the stoichiometry); the mixed-precision solve checks
+     * them in FP64 at the end of every converged cell. */
+    static constexpr int NCONS = 2;
+    __host__ __device__ __forceinline__ static void invariants(const double (&y)[N], double *I,
+                                                               double *A)
+    {
+        (void)y; (void)I; (void)A;
+        I[0] = 2.0 * y[0] + 2.0 * y[1] + 1.0 * y[2] + 1.0 * y[3] + 1.0 * y[4];
+        A[0] = 2.0 * fabs(y[0]) + 2.0 * fabs(y[1]) + 1.0 * fabs(y[2]) + 1.0 * fabs(y[3]) + 1.0 * fabs(y[4]);
+        I[1] = 1.0 * y[5] + 1.0 * y[6] + 1.0 * y[7];
+        A[1] = 1.0 * fabs(y[5]) + 1.0 * fabs(y[6]) + 1.0 * fabs(y[7]);
+    }
+
     /* weight * 1.67e-24, the mass <-> number density factor
      * (rates_and_rate_tables.C.template:158-169) */
     __host__ __device__ static constexpr double unit(int s)

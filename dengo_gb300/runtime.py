@@ -31,7 +31,8 @@ class SolverConfig(C.Structure):
                 ("precision", C.c_int), ("schedule", C.c_int),
                 ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int),
                 ("sweep_budget", C.c_int), ("tail_grid", C.c_int),
-                ("evolve_mode", C.c_int), ("write_intermediate", C.c_int)]
+                ("evolve_mode", C.c_int), ("write_intermediate", C.c_int),
+                ("conservation_tol", C.c_double)]
 
 
 class CellBatch(C.Structure):
@@ -162,6 +163,7 @@ class Solver:
         cfg.warps_per_cell = 4
         cfg.sweep_budget, cfg.tail_grid = 2000, 0
         cfg.evolve_mode, cfg.write_intermediate = DENGO_EVOLVE_LOCKSTEP, -1
+        cfg.conservation_tol = 1e-9
         return cfg
 
     def set_config(self, config=None):

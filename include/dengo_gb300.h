@@ -151,6 +151,16 @@ typedef struct dengo_solver_config {
                                   was generated (write_intermediate_solutions,
                                   the default), 0 never, 1 always; one strip
                                   (dims <= DENGO_MAX_NCELLS) per call */
+    double conservation_tol;   /* DENGO_MIXED: at the end of every converged
+                                  cell the species combinations the
+                                  network's reactions conserve (nuclei of
+                                  each element; for the ion networks also a
+                                  charge combination) are compared in FP64
+                                  with the cell's input; a relative drift
+                                  above this re-solves the cell with FP64
+                                  linear solves.  <= 0: no check; default
+                                  1e-9 (the FP64 path's own drift stays near
+                                  1e-12) */
 } dengo_solver_config;
 
 void dengo_default_config(dengo_solver_config *cfg);

@@ -346,12 +346,14 @@ static void launch(bool mixed, dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg
 
 /* One solve of ncells cells (AoS, mass densities + ge), rtol = rtol_scalar,
  * per-cell dtf, tables in the solver's order; the redistribution's three
- * launches when sweep_budget > 0 (as solve_redistributed in dg_api.cuh). */
+ * launches when sweep_budget > 0 (as solve_redistributed in dg_api.cuh);
+ * cons_tol: the mixed solve's conservation check (0 off; negative: every
+ * converged cell fails it, so every one is re-solved with FP64 solves). */
 extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long long ncells,
                          double rtol_scalar, double z, int mixed, int schedule_queue,
                          int sweep_budget, int max_sweeps, const double *const *tables,
                          int *status, int *substeps, int *sweeps, int *failures, double *ttot,
-                         double *dt)
+                         double *dt, double cons_tol)
 {
     static Net::Data data;
     Net::setup_bins(&data);
@@ -374,7 +376,7 @@ extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long lo
     for (int k = 0; k < NT && k < DG_MAX_TABLES; k++) ts.zvals[k] = zvals[k];
     dg::CellIO io{state, atol, nullptr, rtol_scalar, dtf, 0.0, dt, ttot, status, substeps, sweeps,
                   failures, nullptr, NN, 1, ncells};
-    dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1};
+    dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1, cons_tol};
     unsigned long long queue = 0;
     unsigned long long *q = schedule_queue ? &queue : nullptr;
     if (sweep_budget <= 0) {
@@ -462,14 +464,15 @@ def _bind(lib):
     lib.hx_evolve.restype = C.c_int
     lib.hx_evolve.argtypes = [P_D, P_D, P_D, C.c_longlong, C.c_double, C.c_double, C.c_int,
                               C.c_int, C.c_int, C.c_int, C.POINTER(P_D), P_I, P_I, P_I, P_I,
-                              P_D, P_D]
+                              P_D, P_D, C.c_double]
     return lib
 
 
 def evolve(lib, tables, state, dtf, z=-1.0, mixed=False, queue=True, sweep_budget=0,
-           max_sweeps=10, rtol=1e-6):
+           max_sweeps=10, rtol=1e-6, cons_tol=0.0):
     """Solve ``state`` (cells x N, mass densities + ge) for ``dtf`` with
-    atol = 1e-6 x state; returns a dict like ``Solver.solve_host``."""
+    atol = 1e-6 x state; returns a dict like ``Solver.solve_host``.
+    ``cons_tol``: the mixed solve's conservation check (see hx_evolve)."""
     import numpy as np
     st = np.ascontiguousarray(state, np.float64).copy()
     at = st * 1e-6
@@ -485,7 +488,7 @@ def evolve(lib, tables, state, dtf, z=-1.0, mixed=False, queue=True, sweep_budge
         st.ctypes.data_as(P_D), at.ctypes.data_as(P_D), d.ctypes.data_as(P_D), n, rtol, z,
         int(mixed), int(queue), int(sweep_budget), int(max_sweeps), tp, ip(out["status"]),
         ip(out["substeps"]), ip(out["sweeps"]), ip(out["failures"]),
-        out["ttot"].ctypes.data_as(P_D), out["dt"].ctypes.data_as(P_D))
+        out["ttot"].ctypes.data_as(P_D), out["dt"].ctypes.data_as(P_D), float(cons_tol))
     return out
 
 
