@@ -41,6 +41,35 @@ class DeviceCodePrinter(C99CodePrinter):
         return super()._print_Pow(expr)
 
 
+class FloatDeviceCodePrinter(DeviceCodePrinter):
+    """The same expression in FP32: every floating literal is a float
+    literal (``1.0f``), rational coefficients are float quotients, and
+    other powers call ``powf``; integer coefficients stay integers (they
+    convert exactly)."""
+
+    def _print_Float(self, expr):
+        return super()._print_Float(expr) + "f"
+
+    def _print_Rational(self, expr):
+        return "%d.0f/%d.0f" % (expr.p, expr.q)
+
+    def _print_Pow(self, expr):
+        e = expr.exp
+        if e.is_Integer and int(e) >= 2:
+            return "dg_ipow<%d>(%s)" % (int(e), self._print(expr.base))
+        if e == -1:
+            return "1.0f/%s" % self.parenthesize(expr.base, sympy.printing.precedence.PRECEDENCE["Pow"])
+        return "powf(%s, %s)" % (self._print(expr.base), self._print(e))
+
+
+def ccode_device32(expr, assign_to=None):
+    """``expr`` for the FP32 Jacobian of the mixed-precision solve."""
+    printer = FloatDeviceCodePrinter()
+    if assign_to is not None and isinstance(assign_to, str):
+        assign_to = sympy.Symbol(assign_to)
+    return printer.doprint(expr, assign_to=assign_to)
+
+
 def ccode_device(expr, assign_to=None):
     """Print ``expr`` for the device: same operation order as ``ccode_ref``."""
     printer = DeviceCodePrinter()

@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 
 import sympy
 
-from .printers import ccode_device, ccode_ref
+from .printers import ccode_device, ccode_device32, ccode_ref
 
 
 @dataclass
@@ -65,6 +65,7 @@ class NetworkSpec:
     rhs_dev: list        # per species, "f[k] = ...;"
     jac_ref: list        # [var][eq] "Joutput[j] = ...;"
     jac_dev: list        # [var][eq] device statement or None for a structural zero
+    jac_dev32: list = field(default_factory=list)     # the same in FP32
     jac_nonzero: list = field(default_factory=list)   # [var][eq] bool
     # Work split of one Newton sweep over NP cooperating warps: part index of
     # every RHS row and every Jacobian entry, {NP: ...}, balanced by sympy
@@ -186,18 +187,20 @@ def network_spec(net, name):
         rhs_ref.append(ccode_ref(e, assign_to=sympy.Symbol("rhs[j]")))
         rhs_dev.append(ccode_device(e, assign_to=sympy.Symbol("f[%d]" % i)))
     rhs_cost = [float(sympy.count_ops(net.rhs_expression(s))) + 1.0 for s in ordered]
-    jac_ref, jac_dev, jac_nz, jac_cost = [], [], [], []
+    jac_ref, jac_dev, jac_dev32, jac_nz, jac_cost = [], [], [], [], []
     for v, s1 in enumerate(ordered):
-        cr, cd, cn = [], [], []
+        cr, cd, cd32, cn = [], [], [], []
         for q, s2 in enumerate(ordered):
             e = net.jacobian_expression(s2, s1)
             cr.append(ccode_ref(e, assign_to=sympy.Symbol("Joutput[j]")))
             nz = not (e == 0)
             cn.append(nz)
             cd.append(ccode_device(e, assign_to=sympy.Symbol("jv")) if nz else None)
+            cd32.append(ccode_device32(e, assign_to=sympy.Symbol("jv")) if nz else None)
             jac_cost.append(float(sympy.count_ops(e)) + 4.0 if nz else 0.5)
         jac_ref.append(cr)
         jac_dev.append(cd)
+        jac_dev32.append(cd32)
         jac_nz.append(cn)
     N = len(ordered)
     rhs_part, jac_part = {}, {}
@@ -224,5 +227,5 @@ def network_spec(net, name):
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),
         T_dev_div=gamma_div(ccode_device(T)), Tge_dev_div=gamma_div(ccode_device(Tg)),
         rhs_ref=rhs_ref, rhs_dev=rhs_dev,
-        jac_ref=jac_ref, jac_dev=jac_dev, jac_nonzero=jac_nz,
+        jac_ref=jac_ref, jac_dev=jac_dev, jac_dev32=jac_dev32, jac_nonzero=jac_nz,
         rhs_part=rhs_part, jac_part=jac_part)

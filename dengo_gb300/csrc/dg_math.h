@@ -206,6 +206,17 @@ DG_HD double dg_div(double a, double b, double rb)
 
 /* x^n, n >= 2: the exact power rounded once (up to ~2^-100 relative error
  * before that rounding). */
+/* x^n in FP32 for the mixed path's Jacobian: plain products (one
+ * rounding each; the Jacobian only steers Newton's iteration). */
+template <int n>
+DG_HD float dg_ipow(float x)
+{
+    float p = x;
+#pragma unroll
+    for (int k = 1; k < n; k++) p = p * x;
+    return p;
+}
+
 template <int n>
 DG_HD double dg_ipow(double x)
 {

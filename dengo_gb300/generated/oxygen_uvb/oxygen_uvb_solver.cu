@@ -1567,6 +1567,460 @@ struct Net {
         }
         return true;
     }
+
+    /* The same Jacobian in FP32 arithmetic (the mixed-precision solve):
+     * y and the rates rounded to FP32 by the caller, put(eq, var, value)
+     * for the structurally nonzero entries only. */
+    template <int NP = 1, int P = 0, class RT, class Put>
+    __device__ __forceinline__ static bool jac32(const float (&y)[N], const RT &R, float Tge,
+                                                 float T, float z, const Put &put)
+    {
+        const float mh = 1.67e-24f;
+        float mdensity = 0.0f;
+        (void)Tge; (void)T; (void)z;
+        const float H_1 = y[0];
+        mdensity += H_1;
+        if (H_1 < 0.0f) return false;
+        const float H_2 = y[1];
+        mdensity += H_2;
+        if (H_2 < 0.0f) return false;
+        const float He_1 = y[2];
+        mdensity += He_1;
+        if (He_1 < 0.0f) return false;
+        const float He_2 = y[3];
+        mdensity += He_2;
+        if (He_2 < 0.0f) return false;
+        const float He_3 = y[4];
+        mdensity += He_3;
+        if (He_3 < 0.0f) return false;
+        const float O_1 = y[5];
+        mdensity += O_1;
+        if (O_1 < 0.0f) return false;
+        const float O_2 = y[6];
+        mdensity += O_2;
+        if (O_2 < 0.0f) return false;
+        const float O_3 = y[7];
+        mdensity += O_3;
+        if (O_3 < 0.0f) return false;
+        const float O_4 = y[8];
+        mdensity += O_4;
+        if (O_4 < 0.0f) return false;
+        const float O_5 = y[9];
+        mdensity += O_5;
+        if (O_5 < 0.0f) return false;
+        const float O_6 = y[10];
+        mdensity += O_6;
+        if (O_6 < 0.0f) return false;
+        const float O_7 = y[11];
+        mdensity += O_7;
+        if (O_7 < 0.0f) return false;
+        const float O_8 = y[12];
+        mdensity += O_8;
+        if (O_8 < 0.0f) return false;
+        const float O_9 = y[13];
+        mdensity += O_9;
+        if (O_9 < 0.0f) return false;
+        const float de = y[14];
+        if (de < 0.0f) return false;
+        const float ge = y[15];
+        if (ge < 0.0f) return false;
+        mdensity *= mh;
+        const float H_1_i = R[0];
+        const float H_1_pi = R[1];
+        const float H_2_r = R[2];
+        const float He_1_i = R[3];
+        const float He_1_pi = R[4];
+        const float He_2_i = R[5];
+        const float He_2_pi = R[6];
+        const float He_2_r = R[7];
+        const float He_3_r = R[8];
+        const float O_1_i = R[9];
+        const float O_1_pi = R[10];
+        const float O_2_i = R[11];
+        const float O_2_pi = R[12];
+        const float O_2_r = R[13];
+        const float O_3_i = R[14];
+        const float O_3_pi = R[15];
+        const float O_3_r = R[16];
+        const float O_4_i = R[17];
+        const float O_4_pi = R[18];
+        const float O_4_r = R[19];
+        const float O_5_i = R[20];
+        const float O_5_pi = R[21];
+        const float O_5_r = R[22];
+        const float O_6_i = R[23];
+        const float O_6_pi = R[24];
+        const float O_6_r = R[25];
+        const float O_7_i = R[26];
+        const float O_7_pi = R[27];
+        const float O_7_r = R[28];
+        const float O_8_i = R[29];
+        const float O_8_pi = R[30];
+        const float O_8_r = R[31];
+        const float O_9_r = R[32];
+        const float H_1_c_H_1_c = R[33];
+        const float H_1_ph_H_1_ph = R[34];
+        const float H_2_c_H_2_c = R[35];
+        const float He_1_c_He_1_c = R[36];
+        const float He_1_ph_He_1_ph = R[37];
+        const float He_2_c_He_2_c = R[38];
+        const float He_2_ph_He_2_ph = R[39];
+        const float He_3_c_He_3_c = R[40];
+        const float O_1_c_O_1_c = R[41];
+        const float O_1_ph_O_1_ph = R[42];
+        const float O_2_c_O_2_c = R[43];
+        const float O_2_ph_O_2_ph = R[44];
+        const float O_3_c_O_3_c = R[45];
+        const float O_3_ph_O_3_ph = R[46];
+        const float O_4_c_O_4_c = R[47];
+        const float O_4_ph_O_4_ph = R[48];
+        const float O_5_c_O_5_c = R[49];
+        const float O_5_ph_O_5_ph = R[50];
+        const float O_6_c_O_6_c = R[51];
+        const float O_6_ph_O_6_ph = R[52];
+        const float O_7_c_O_7_c = R[53];
+        const float O_7_ph_O_7_ph = R[54];
+        const float O_8_c_O_8_c = R[55];
+        const float O_8_ph_O_8_ph = R[56];
+        const float O_9_c_O_9_c = R[57];
+        float jv;
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -H_1_i*de - H_1_pi;
+            put(0, 0, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = H_1_i*de + H_1_pi;
+            put(1, 0, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = H_1_i*de + H_1_pi;
+            put(14, 0, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -H_1_c_H_1_c*de + H_1_ph_H_1_ph;
+            jv = jv / mdensity;
+            put(15, 0, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = H_2_r*de;
+            put(0, 1, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -H_2_r*de;
+            put(1, 1, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -H_2_r*de;
+            put(14, 1, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -H_2_c_H_2_c*de;
+            jv = jv / mdensity;
+            put(15, 1, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -He_1_i*de - He_1_pi;
+            put(2, 2, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = He_1_i*de + He_1_pi;
+            put(3, 2, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = He_1_i*de + He_1_pi;
+            put(14, 2, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -He_1_c_He_1_c*de + He_1_ph_He_1_ph;
+            jv = jv / mdensity;
+            put(15, 2, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = He_2_r*de;
+            put(2, 3, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -He_2_i*de - He_2_pi - He_2_r*de;
+            put(3, 3, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = He_2_i*de + He_2_pi;
+            put(4, 3, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = He_2_i*de + He_2_pi - He_2_r*de;
+            put(14, 3, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -He_2_c_He_2_c*de + He_2_ph_He_2_ph;
+            jv = jv / mdensity;
+            put(15, 3, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = He_3_r*de;
+            put(3, 4, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -He_3_r*de;
+            put(4, 4, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -He_3_r*de;
+            put(14, 4, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -He_3_c_He_3_c*de;
+            jv = jv / mdensity;
+            put(15, 4, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -O_1_i*de - O_1_pi;
+            put(5, 5, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = O_1_i*de + O_1_pi;
+            put(6, 5, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_1_i*de + O_1_pi;
+            put(14, 5, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -O_1_c_O_1_c*de + O_1_ph_O_1_ph;
+            jv = jv / mdensity;
+            put(15, 5, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_2_r*de;
+            put(5, 6, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -O_2_i*de - O_2_pi - O_2_r*de;
+            put(6, 6, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_2_i*de + O_2_pi;
+            put(7, 6, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = O_2_i*de + O_2_pi - O_2_r*de;
+            put(14, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -O_2_c_O_2_c*de + O_2_ph_O_2_ph;
+            jv = jv / mdensity;
+            put(15, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = O_3_r*de;
+            put(6, 7, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -O_3_i*de - O_3_pi - O_3_r*de;
+            put(7, 7, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_3_i*de + O_3_pi;
+            put(8, 7, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = O_3_i*de + O_3_pi - O_3_r*de;
+            put(14, 7, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -O_3_c_O_3_c*de + O_3_ph_O_3_ph;
+            jv = jv / mdensity;
+            put(15, 7, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_4_r*de;
+            put(7, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -O_4_i*de - O_4_pi - O_4_r*de;
+            put(8, 8, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_4_i*de + O_4_pi;
+            put(9, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = O_4_i*de + O_4_pi - O_4_r*de;
+            put(14, 8, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -O_4_c_O_4_c*de + O_4_ph_O_4_ph;
+            jv = jv / mdensity;
+            put(15, 8, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = O_5_r*de;
+            put(8, 9, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -O_5_i*de - O_5_pi - O_5_r*de;
+            put(9, 9, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_5_i*de + O_5_pi;
+            put(10, 9, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = O_5_i*de + O_5_pi - O_5_r*de;
+            put(14, 9, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -O_5_c_O_5_c*de + O_5_ph_O_5_ph;
+            jv = jv / mdensity;
+            put(15, 9, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_6_r*de;
+            put(9, 10, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -O_6_i*de - O_6_pi - O_6_r*de;
+            put(10, 10, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_6_i*de + O_6_pi;
+            put(11, 10, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = O_6_i*de + O_6_pi - O_6_r*de;
+            put(14, 10, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -O_6_c_O_6_c*de + O_6_ph_O_6_ph;
+            jv = jv / mdensity;
+            put(15, 10, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = O_7_r*de;
+            put(10, 11, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -O_7_i*de - O_7_pi - O_7_r*de;
+            put(11, 11, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_7_i*de + O_7_pi;
+            put(12, 11, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = O_7_i*de + O_7_pi - O_7_r*de;
+            put(14, 11, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -O_7_c_O_7_c*de + O_7_ph_O_7_ph;
+            jv = jv / mdensity;
+            put(15, 11, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_8_r*de;
+            put(11, 12, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -O_8_i*de - O_8_pi - O_8_r*de;
+            put(12, 12, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = O_8_i*de + O_8_pi;
+            put(13, 12, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = O_8_i*de + O_8_pi - O_8_r*de;
+            put(14, 12, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -O_8_c_O_8_c*de + O_8_ph_O_8_ph;
+            jv = jv / mdensity;
+            put(15, 12, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = O_9_r*de;
+            put(12, 13, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -O_9_r*de;
+            put(13, 13, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -O_9_r*de;
+            put(14, 13, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -O_9_c_O_9_c*de;
+            jv = jv / mdensity;
+            put(15, 13, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -H_1_i*H_1 + H_2_r*H_2;
+            put(0, 14, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = H_1_i*H_1 - H_2_r*H_2;
+            put(1, 14, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -He_1_i*He_1 + He_2_r*He_2;
+            put(2, 14, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = He_1_i*He_1 - He_2_i*He_2 - He_2_r*He_2 + He_3_r*He_3;
+            put(3, 14, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = He_2_i*He_2 - He_3_r*He_3;
+            put(4, 14, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -O_1_i*O_1 + O_2_r*O_2;
+            put(5, 14, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = O_1_i*O_1 - O_2_i*O_2 - O_2_r*O_2 + O_3_r*O_3;
+            put(6, 14, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = O_2_i*O_2 - O_3_i*O_3 - O_3_r*O_3 + O_4_r*O_4;
+            put(7, 14, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = O_3_i*O_3 - O_4_i*O_4 - O_4_r*O_4 + O_5_r*O_5;
+            put(8, 14, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = O_4_i*O_4 - O_5_i*O_5 - O_5_r*O_5 + O_6_r*O_6;
+            put(9, 14, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = O_5_i*O_5 - O_6_i*O_6 - O_6_r*O_6 + O_7_r*O_7;
+            put(10, 14, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = O_6_i*O_6 - O_7_i*O_7 - O_7_r*O_7 + O_8_r*O_8;
+            put(11, 14, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = O_7_i*O_7 - O_8_i*O_8 - O_8_r*O_8 + O_9_r*O_9;
+            put(12, 14, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = O_8_i*O_8 - O_9_r*O_9;
+            put(13, 14, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = H_1_i*H_1 - H_2_r*H_2 + He_1_i*He_1 + He_2_i*He_2 - He_2_r*He_2 - He_3_r*He_3 + O_1_i*O_1 + O_2_i*O_2 - O_2_r*O_2 + O_3_i*O_3 - O_3_r*O_3 + O_4_i*O_4 - O_4_r*O_4 + O_5_i*O_5 - O_5_r*O_5 + O_6_i*O_6 - O_6_r*O_6 + O_7_i*O_7 - O_7_r*O_7 + O_8_i*O_8 - O_8_r*O_8 - O_9_r*O_9;
+            put(14, 14, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -H_1*H_1_c_H_1_c - H_2*H_2_c_H_2_c - He_1*He_1_c_He_1_c - He_2*He_2_c_He_2_c - He_3*He_3_c_He_3_c - O_1*O_1_c_O_1_c - O_2*O_2_c_O_2_c - O_3*O_3_c_O_3_c - O_4*O_4_c_O_4_c - O_5*O_5_c_O_5_c - O_6*O_6_c_O_6_c - O_7*O_7_c_O_7_c - O_8*O_8_c_O_8_c - O_9*O_9_c_O_9_c;
+            jv = jv / mdensity;
+            put(15, 14, jv);
+        }
+        return true;
+    }
 };
 
 using Api = dg::Api<Net>;

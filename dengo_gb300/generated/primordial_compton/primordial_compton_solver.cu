@@ -918,6 +918,317 @@ struct Net {
         }
         return true;
     }
+
+    /* The same Jacobian in FP32 arithmetic (the mixed-precision solve):
+     * y and the rates rounded to FP32 by the caller, put(eq, var, value)
+     * for the structurally nonzero entries only. */
+    template <int NP = 1, int P = 0, class RT, class Put>
+    __device__ __forceinline__ static bool jac32(const float (&y)[N], const RT &R, float Tge,
+                                                 float T, float z, const Put &put)
+    {
+        const float mh = 1.67e-24f;
+        float mdensity = 0.0f;
+        (void)Tge; (void)T; (void)z;
+        const float H2_1 = y[0];
+        mdensity += H2_1;
+        if (H2_1 < 0.0f) return false;
+        const float H2_2 = y[1];
+        mdensity += H2_2;
+        if (H2_2 < 0.0f) return false;
+        const float H_1 = y[2];
+        mdensity += H_1;
+        if (H_1 < 0.0f) return false;
+        const float H_2 = y[3];
+        mdensity += H_2;
+        if (H_2 < 0.0f) return false;
+        const float H_m0 = y[4];
+        mdensity += H_m0;
+        if (H_m0 < 0.0f) return false;
+        const float He_1 = y[5];
+        mdensity += He_1;
+        if (He_1 < 0.0f) return false;
+        const float He_2 = y[6];
+        mdensity += He_2;
+        if (He_2 < 0.0f) return false;
+        const float He_3 = y[7];
+        mdensity += He_3;
+        if (He_3 < 0.0f) return false;
+        const float de = y[8];
+        if (de < 0.0f) return false;
+        const float ge = y[9];
+        if (ge < 0.0f) return false;
+        mdensity *= mh;
+        const float k01 = R[0];
+        const float k02 = R[1];
+        const float k03 = R[2];
+        const float k04 = R[3];
+        const float k05 = R[4];
+        const float k06 = R[5];
+        const float k07 = R[6];
+        const float k08 = R[7];
+        const float k09 = R[8];
+        const float k10 = R[9];
+        const float k11 = R[10];
+        const float k12 = R[11];
+        const float k13 = R[12];
+        const float k14 = R[13];
+        const float k15 = R[14];
+        const float k16 = R[15];
+        const float k17 = R[16];
+        const float k18 = R[17];
+        const float k19 = R[18];
+        const float k21 = R[19];
+        const float k22 = R[20];
+        const float k23 = R[21];
+        const float brem_brem = R[22];
+        const float ceHI_ceHI = R[23];
+        const float ceHeI_ceHeI = R[24];
+        const float ceHeII_ceHeII = R[25];
+        const float ciHI_ciHI = R[26];
+        const float ciHeI_ciHeI = R[27];
+        const float ciHeII_ciHeII = R[28];
+        const float ciHeIS_ciHeIS = R[29];
+        const float compton_comp = R[30];
+        const float gammah_gammah = R[31];
+        const float gloverabel08_gaH2 = R[32];
+        const float gloverabel08_gaHI = R[33];
+        const float gloverabel08_gaHe = R[34];
+        const float gloverabel08_gaHp = R[35];
+        const float gloverabel08_gael = R[36];
+        const float gloverabel08_gphdl = R[37];
+        const float gloverabel08_gpldl = R[38];
+        const float h2formation_h2mcool = R[39];
+        const float h2formation_h2mheat = R[40];
+        const float reHII_reHII = R[41];
+        const float reHeII1_reHeII1 = R[42];
+        const float reHeII2_reHeII2 = R[43];
+        const float reHeIII_reHeIII = R[44];
+        float jv;
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
+            put(0, 0, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k11*H_2;
+            put(1, 0, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
+            put(2, 0, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k11*H_2 + 2*k12*de;
+            put(3, 0, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f);
+            jv = jv / mdensity;
+            put(9, 0, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = k10*H_1 + k19*H_m0;
+            put(0, 1, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k10*H_1 - k18*de - k19*H_m0;
+            put(1, 1, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -k10*H_1 + 2*k18*de + k19*H_m0;
+            put(2, 1, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = k10*H_1;
+            put(3, 1, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k19*H_m0;
+            put(4, 1, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k18*de;
+            put(8, 1, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
+            put(0, 2, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k09*H_2 - k10*H2_2;
+            put(1, 2, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
+            put(2, 2, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k01*de - k09*H_2 + k10*H2_2;
+            put(3, 2, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k07*de - k08*H_m0 - k15*H_m0;
+            put(4, 2, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
+            put(8, 2, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -H2_1*gloverabel08_gaHI*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H2_1*h2formation_h2mcool + 3*dg_ipow<2>(H_1)*h2formation_h2mheat - ceHI_ceHI*de - ciHI_ciHI*de;
+            jv = jv / mdensity;
+            put(9, 2, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k11*H2_1;
+            put(0, 3, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k09*H_1 + k11*H2_1 + k17*H_m0;
+            put(1, 3, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
+            put(2, 3, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
+            put(3, 3, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -k16*H_m0 - k17*H_m0;
+            put(4, 3, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k02*de + k17*H_m0;
+            put(8, 3, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
+            jv = jv / mdensity;
+            put(9, 3, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k08*H_1 + k19*H2_2;
+            put(0, 4, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k17*H_2 - k19*H2_2;
+            put(1, 4, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
+            put(2, 4, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = -k16*H_2 - k17*H_2;
+            put(3, 4, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
+            put(4, 4, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
+            put(8, 4, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k03*de;
+            put(5, 5, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k03*de;
+            put(6, 5, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k03*de;
+            put(8, 5, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
+            jv = jv / mdensity;
+            put(9, 5, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = k04*de;
+            put(5, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -k04*de - k05*de;
+            put(6, 6, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = k05*de;
+            put(7, 6, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k04*de + k05*de;
+            put(8, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
+            jv = jv / mdensity;
+            put(9, 6, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = k06*de;
+            put(6, 7, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -k06*de;
+            put(7, 7, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = -k06*de;
+            put(8, 7, jv);
+        }
+        if (pick(NP, 0, 0, 3) == P) {
+            jv = -4.0f*brem_brem*de - de*reHeIII_reHeIII;
+            jv = jv / mdensity;
+            put(9, 7, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k12*H2_1;
+            put(0, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k18*H2_2;
+            put(1, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = -k01*H_1 + k02*H_2 - k07*H_1 + k14*H_m0 + 2*k18*H2_2;
+            put(2, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
+            put(3, 8, jv);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            jv = k07*H_1 - k14*H_m0;
+            put(4, 8, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            jv = -k03*He_1 + k04*He_2;
+            put(5, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
+            put(6, 8, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            jv = k05*He_2 - k06*He_3;
+            put(7, 8, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
+            put(8, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0f*He_3) - compton_comp*dg_ipow<4>(z + 1.0f)*(T - 2.73f*z - 2.73f);
+            jv = jv / mdensity;
+            put(9, 8, jv);
+        }
+        return true;
+    }
 };
 
 using Api = dg::Api<Net>;
