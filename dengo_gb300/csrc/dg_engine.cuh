@@ -30,6 +30,7 @@
 #include "dg_math.h"
 #include "dg_slots.cuh"
 #include "dg_mixed.cuh"
+#include "dg_xf.h"
 #include "dengo_gb300.h"
 
 namespace dg {
@@ -315,6 +316,33 @@ struct JacPut {
     }
 };
 
+/* The mixed-precision solve's Newton-matrix entry: BE_Resid_Jac's
+ * ((J * inv_q) * scale_v) * -dt, + 1 on the diagonal (as JacPut), in
+ * extended-range FP32 (dg_xf.h) -- each product rounded to FP32's 24-bit
+ * significand, no FP64 instruction -- and stored as the (exact) FP64 value
+ * of the result, which the equilibrated FP32 LU and the FP64 refinement
+ * then use.  Only for cells whose scales are positive finite numbers and
+ * dt > 0 (the FP64 Jacobian serves the others); zero() stores the
+ * structural zero the reference computes there (-0.0, 1.0 on the
+ * diagonal). */
+template <int N, int BLOCK>
+struct JacPutX {
+    Slots<BLOCK> J, INV, SC;
+    double mdt;
+    __device__ __forceinline__ void operator()(int q, int v, XF jv) const
+    {
+        XF a = jv * xf(INV[q]);
+        a = a * xf(SC[v]);
+        a = a * xf(mdt);
+        if (q == v) a = a + 1.0f;
+        J[v * N + q] = xf_to_double(a);
+    }
+    __device__ __forceinline__ void zero(int q, int v) const
+    {
+        J[v * N + q] = (q == v) ? 1.0 : -0.0;
+    }
+};
+
 /* Number-density conversion and electron consistency at the start of a
  * cell (rates_and_rate_tables.C.template:158-170). */
 template <class Net>
@@ -365,11 +393,14 @@ __device__ __forceinline__ bool conserved(const CellIO &io, long long cell,
 }
 
 /* MIXED = false: the reference's FP64 arithmetic throughout (bit-faithful).
- * MIXED = true: the Newton system is solved by MixedSolve (equilibrated FP32
- * LU + FP64 iterative refinement, dg_mixed.cuh), falling back to the FP64
+ * MIXED = true: the Newton matrix is built in extended-range FP32 (jacx,
+ * JacPutX) and solved by MixedSolve (equilibrated FP32 LU + FP64 iterative
+ * refinement, dg_mixed.cuh), falling back to the FP64 Jacobian and
  * elimination for a cell whose matrix holds inf/NaN or whose scales are not
- * all positive and finite; temperature, rates, RHS, Jacobian, residual and
- * the Newton update and its convergence test stay FP64. */
+ * all positive and finite, and re-solving with FP64 linear solves a
+ * converged cell that fails the FP64 conservation check; temperature,
+ * rates, RHS, residual and the Newton update and its convergence test stay
+ * FP64. */
 template <class Net, int BLOCK, bool MIXED>
 __global__ void __launch_bounds__(BLOCK)
 evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
@@ -563,8 +594,12 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 #pragma unroll
                 for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
                 const bool dense_j = dense || !(dt > 0.0);
-                {
-                    JacPut<N, BLOCK> put{J, INV, SC, -dt, dense_j};
+                if (MIXED && !dense_j && !fp64cell) {
+                    /* the Jacobian in extended-range FP32 */
+                    const JacPutX<N, BLOCK> put{J, INV, SC, -dt};
+                    ok = Net::jacx(y, R, Tge, T, ts.z, put);
+                } else {
+                    const JacPut<N, BLOCK> put{J, INV, SC, -dt, dense_j};
                     ok = Net::jac(y, R, Tge, T, ts.z, put);
                 }
                 if (ok) {

@@ -328,12 +328,23 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             double y[N];
             for (int i = 0; i < N; i++) y[i] = Y[i];
             bool ok = true;
-            const JacPut<N, 32> put{J, INV, SC, S[3], F(F_DENSE) != 0};
-            switch (w) {
-            case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
-            case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
-            case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
-            default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
+            if (MIXED && !F(F_DENSE) && !F(F_FP64)) {
+                /* mixed: the Jacobian in extended-range FP32 */
+                const JacPutX<N, 32> put{J, INV, SC, S[3]};
+                switch (w) {
+                case 0: ok = Net::template jacx<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
+                case 1: ok = Net::template jacx<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                case 2: ok = Net::template jacx<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                default: ok = Net::template jacx<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                }
+            } else {
+                const JacPut<N, 32> put{J, INV, SC, S[3], F(F_DENSE) != 0};
+                switch (w) {
+                case 0: ok = Net::template jac<NP, 0>(y, R, S[1], S[0], ts.z, put); break;
+                case 1: ok = Net::template jac<NP, 1 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                case 2: ok = Net::template jac<NP, 2 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                default: ok = Net::template jac<NP, 3 % NP>(y, R, S[1], S[0], ts.z, put); break;
+                }
             }
             if (!ok) atomicAnd(&F(F_OKJ), 0);
         }

@@ -1458,100 +1458,106 @@ struct Net {
         return true;
     }
 
-    /* The same Jacobian in FP32 arithmetic (the mixed-precision solve):
-     * y and the rates rounded to FP32 by the caller, put(eq, var, value)
-     * for the structurally nonzero entries only. */
+    /* The same Jacobian in extended-range FP32 (dg_xf.h), for the
+     * mixed-precision solve: every operation of the same expressions
+     * rounded to FP32's 24-bit significand, the exponent unbounded, so no
+     * FP64 instruction.  Same negative-value test and part split as jac();
+     * put(eq, var, value) receives an XF value for the structurally nonzero
+     * entries, put.zero(eq, var) the others. */
     template <int NP = 1, int P = 0, class RT, class Put>
-    __device__ __forceinline__ static bool jac32(const float (&y)[N], const RT &R, float Tge,
-                                                 float T, float z, const Put &put)
+    __device__ __forceinline__ static bool jacx(const double (&yd)[N], const RT &R, double Tge_d,
+                                                double T_d, double z_d, const Put &put)
     {
-        const float mh = 1.67e-24f;
-        float mdensity = 0.0f;
+        using dg::XF;
+        using dg::xf;
+        const XF mh = xf(1.67e-24);
+        XF mdensity = xf(0.0);
+        const XF Tge = xf(Tge_d), T = xf(T_d), z = xf(z_d);
         (void)Tge; (void)T; (void)z;
-        const float H_1 = y[0];
-        mdensity += H_1;
-        if (H_1 < 0.0f) return false;
-        const float H_2 = y[1];
-        mdensity += H_2;
-        if (H_2 < 0.0f) return false;
-        const float He_1 = y[2];
-        mdensity += He_1;
-        if (He_1 < 0.0f) return false;
-        const float He_2 = y[3];
-        mdensity += He_2;
-        if (He_2 < 0.0f) return false;
-        const float He_3 = y[4];
-        mdensity += He_3;
-        if (He_3 < 0.0f) return false;
-        const float O_1 = y[5];
-        mdensity += O_1;
-        if (O_1 < 0.0f) return false;
-        const float O_2 = y[6];
-        mdensity += O_2;
-        if (O_2 < 0.0f) return false;
-        const float O_3 = y[7];
-        mdensity += O_3;
-        if (O_3 < 0.0f) return false;
-        const float O_4 = y[8];
-        mdensity += O_4;
-        if (O_4 < 0.0f) return false;
-        const float O_5 = y[9];
-        mdensity += O_5;
-        if (O_5 < 0.0f) return false;
-        const float O_6 = y[10];
-        mdensity += O_6;
-        if (O_6 < 0.0f) return false;
-        const float O_7 = y[11];
-        mdensity += O_7;
-        if (O_7 < 0.0f) return false;
-        const float O_8 = y[12];
-        mdensity += O_8;
-        if (O_8 < 0.0f) return false;
-        const float O_9 = y[13];
-        mdensity += O_9;
-        if (O_9 < 0.0f) return false;
-        const float de = y[14];
-        if (de < 0.0f) return false;
-        const float ge = y[15];
-        if (ge < 0.0f) return false;
-        mdensity *= mh;
-        const float H_1_i = R[0];
-        const float H_2_r = R[1];
-        const float He_1_i = R[2];
-        const float He_2_i = R[3];
-        const float He_2_r = R[4];
-        const float He_3_r = R[5];
-        const float O_1_i = R[6];
-        const float O_2_i = R[7];
-        const float O_2_r = R[8];
-        const float O_3_i = R[9];
-        const float O_3_r = R[10];
-        const float O_4_i = R[11];
-        const float O_4_r = R[12];
-        const float O_5_i = R[13];
-        const float O_5_r = R[14];
-        const float O_6_i = R[15];
-        const float O_6_r = R[16];
-        const float O_7_i = R[17];
-        const float O_7_r = R[18];
-        const float O_8_i = R[19];
-        const float O_8_r = R[20];
-        const float O_9_r = R[21];
-        const float H_1_c_H_1_c = R[22];
-        const float H_2_c_H_2_c = R[23];
-        const float He_1_c_He_1_c = R[24];
-        const float He_2_c_He_2_c = R[25];
-        const float He_3_c_He_3_c = R[26];
-        const float O_1_c_O_1_c = R[27];
-        const float O_2_c_O_2_c = R[28];
-        const float O_3_c_O_3_c = R[29];
-        const float O_4_c_O_4_c = R[30];
-        const float O_5_c_O_5_c = R[31];
-        const float O_6_c_O_6_c = R[32];
-        const float O_7_c_O_7_c = R[33];
-        const float O_8_c_O_8_c = R[34];
-        const float O_9_c_O_9_c = R[35];
-        float jv;
+        if (dg_lt0(yd[0])) return false;   /* H_1 < 0.0 */
+        const XF H_1 = xf(yd[0]);
+        mdensity = mdensity + H_1;
+        if (dg_lt0(yd[1])) return false;   /* H_2 < 0.0 */
+        const XF H_2 = xf(yd[1]);
+        mdensity = mdensity + H_2;
+        if (dg_lt0(yd[2])) return false;   /* He_1 < 0.0 */
+        const XF He_1 = xf(yd[2]);
+        mdensity = mdensity + He_1;
+        if (dg_lt0(yd[3])) return false;   /* He_2 < 0.0 */
+        const XF He_2 = xf(yd[3]);
+        mdensity = mdensity + He_2;
+        if (dg_lt0(yd[4])) return false;   /* He_3 < 0.0 */
+        const XF He_3 = xf(yd[4]);
+        mdensity = mdensity + He_3;
+        if (dg_lt0(yd[5])) return false;   /* O_1 < 0.0 */
+        const XF O_1 = xf(yd[5]);
+        mdensity = mdensity + O_1;
+        if (dg_lt0(yd[6])) return false;   /* O_2 < 0.0 */
+        const XF O_2 = xf(yd[6]);
+        mdensity = mdensity + O_2;
+        if (dg_lt0(yd[7])) return false;   /* O_3 < 0.0 */
+        const XF O_3 = xf(yd[7]);
+        mdensity = mdensity + O_3;
+        if (dg_lt0(yd[8])) return false;   /* O_4 < 0.0 */
+        const XF O_4 = xf(yd[8]);
+        mdensity = mdensity + O_4;
+        if (dg_lt0(yd[9])) return false;   /* O_5 < 0.0 */
+        const XF O_5 = xf(yd[9]);
+        mdensity = mdensity + O_5;
+        if (dg_lt0(yd[10])) return false;   /* O_6 < 0.0 */
+        const XF O_6 = xf(yd[10]);
+        mdensity = mdensity + O_6;
+        if (dg_lt0(yd[11])) return false;   /* O_7 < 0.0 */
+        const XF O_7 = xf(yd[11]);
+        mdensity = mdensity + O_7;
+        if (dg_lt0(yd[12])) return false;   /* O_8 < 0.0 */
+        const XF O_8 = xf(yd[12]);
+        mdensity = mdensity + O_8;
+        if (dg_lt0(yd[13])) return false;   /* O_9 < 0.0 */
+        const XF O_9 = xf(yd[13]);
+        mdensity = mdensity + O_9;
+        if (dg_lt0(yd[14])) return false;   /* de < 0.0 */
+        const XF de = xf(yd[14]);
+        if (dg_lt0(yd[15])) return false;   /* ge < 0.0 */
+        const XF ge = xf(yd[15]);
+        mdensity = mdensity * mh;
+        const XF H_1_i = xf(R[0]);
+        const XF H_2_r = xf(R[1]);
+        const XF He_1_i = xf(R[2]);
+        const XF He_2_i = xf(R[3]);
+        const XF He_2_r = xf(R[4]);
+        const XF He_3_r = xf(R[5]);
+        const XF O_1_i = xf(R[6]);
+        const XF O_2_i = xf(R[7]);
+        const XF O_2_r = xf(R[8]);
+        const XF O_3_i = xf(R[9]);
+        const XF O_3_r = xf(R[10]);
+        const XF O_4_i = xf(R[11]);
+        const XF O_4_r = xf(R[12]);
+        const XF O_5_i = xf(R[13]);
+        const XF O_5_r = xf(R[14]);
+        const XF O_6_i = xf(R[15]);
+        const XF O_6_r = xf(R[16]);
+        const XF O_7_i = xf(R[17]);
+        const XF O_7_r = xf(R[18]);
+        const XF O_8_i = xf(R[19]);
+        const XF O_8_r = xf(R[20]);
+        const XF O_9_r = xf(R[21]);
+        const XF H_1_c_H_1_c = xf(R[22]);
+        const XF H_2_c_H_2_c = xf(R[23]);
+        const XF He_1_c_He_1_c = xf(R[24]);
+        const XF He_2_c_He_2_c = xf(R[25]);
+        const XF He_3_c_He_3_c = xf(R[26]);
+        const XF O_1_c_O_1_c = xf(R[27]);
+        const XF O_2_c_O_2_c = xf(R[28]);
+        const XF O_3_c_O_3_c = xf(R[29]);
+        const XF O_4_c_O_4_c = xf(R[30]);
+        const XF O_5_c_O_5_c = xf(R[31]);
+        const XF O_6_c_O_6_c = xf(R[32]);
+        const XF O_7_c_O_7_c = xf(R[33]);
+        const XF O_8_c_O_8_c = xf(R[34]);
+        const XF O_9_c_O_9_c = xf(R[35]);
+        XF jv;
         if (pick(NP, 0, 1, 1) == P) {
             jv = -H_1_i*de;
             put(0, 0, jv);
@@ -1559,6 +1565,42 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             jv = H_1_i*de;
             put(1, 0, jv);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(2, 0);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(3, 0);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(4, 0);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(5, 0);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(6, 0);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(7, 0);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(8, 0);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 0);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(10, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(11, 0);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(12, 0);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(13, 0);
         }
         if (pick(NP, 0, 0, 1) == P) {
             jv = H_1_i*de;
@@ -1577,6 +1619,42 @@ struct Net {
             jv = -H_2_r*de;
             put(1, 1, jv);
         }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(2, 1);
+        }
+        if (pick(NP, 0, 1, 0) == P) {
+            put.zero(3, 1);
+        }
+        if (pick(NP, 0, 0, 1) == P) {
+            put.zero(4, 1);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(5, 1);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(6, 1);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(7, 1);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(8, 1);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(9, 1);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(10, 1);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(11, 1);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(12, 1);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(13, 1);
+        }
         if (pick(NP, 0, 1, 3) == P) {
             jv = -H_2_r*de;
             put(14, 1, jv);
@@ -1586,6 +1664,12 @@ struct Net {
             jv = jv / mdensity;
             put(15, 1, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 2);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 2);
+        }
         if (pick(NP, 0, 1, 2) == P) {
             jv = -He_1_i*de;
             put(2, 2, jv);
@@ -1593,6 +1677,36 @@ struct Net {
         if (pick(NP, 0, 0, 0) == P) {
             jv = He_1_i*de;
             put(3, 2, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 2);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 2);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(6, 2);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(7, 2);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(8, 2);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(9, 2);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(10, 2);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(11, 2);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(12, 2);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(13, 2);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = He_1_i*de;
@@ -1602,6 +1716,12 @@ struct Net {
             jv = -He_1_c_He_1_c*de;
             jv = jv / mdensity;
             put(15, 2, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 3);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 3);
         }
         if (pick(NP, 0, 0, 1) == P) {
             jv = He_2_r*de;
@@ -1615,6 +1735,33 @@ struct Net {
             jv = He_2_i*de;
             put(4, 3, jv);
         }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(5, 3);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(6, 3);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 3);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(8, 3);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 3);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(10, 3);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(11, 3);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(12, 3);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(13, 3);
+        }
         if (pick(NP, 0, 0, 0) == P) {
             jv = He_2_i*de - He_2_r*de;
             put(14, 3, jv);
@@ -1624,6 +1771,15 @@ struct Net {
             jv = jv / mdensity;
             put(15, 3, jv);
         }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 4);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 4);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 4);
+        }
         if (pick(NP, 0, 0, 0) == P) {
             jv = He_3_r*de;
             put(3, 4, jv);
@@ -1631,6 +1787,33 @@ struct Net {
         if (pick(NP, 0, 0, 1) == P) {
             jv = -He_3_r*de;
             put(4, 4, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(5, 4);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(6, 4);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 4);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(8, 4);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 4);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(10, 4);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(11, 4);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(12, 4);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(13, 4);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = -He_3_r*de;
@@ -1642,12 +1825,48 @@ struct Net {
             put(15, 4, jv);
         }
         if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 5);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 5);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(3, 5);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(4, 5);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -O_1_i*de;
             put(5, 5, jv);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = O_1_i*de;
             put(6, 5, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 5);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(8, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 5);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(10, 5);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(11, 5);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(12, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(13, 5);
         }
         if (pick(NP, 0, 0, 1) == P) {
             jv = O_1_i*de;
@@ -1657,6 +1876,21 @@ struct Net {
             jv = -O_1_c_O_1_c*de;
             jv = jv / mdensity;
             put(15, 5, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 6);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 6);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 6);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(3, 6);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(4, 6);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = O_2_r*de;
@@ -1670,6 +1904,24 @@ struct Net {
             jv = O_2_i*de;
             put(7, 6, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(8, 6);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(9, 6);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(10, 6);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(11, 6);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(12, 6);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(13, 6);
+        }
         if (pick(NP, 0, 0, 3) == P) {
             jv = O_2_i*de - O_2_r*de;
             put(14, 6, jv);
@@ -1678,6 +1930,24 @@ struct Net {
             jv = -O_2_c_O_2_c*de;
             jv = jv / mdensity;
             put(15, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(0, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(1, 7);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(2, 7);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(3, 7);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 7);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = O_3_r*de;
@@ -1691,6 +1961,21 @@ struct Net {
             jv = O_3_i*de;
             put(8, 7, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(9, 7);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(10, 7);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(11, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(12, 7);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(13, 7);
+        }
         if (pick(NP, 0, 1, 1) == P) {
             jv = O_3_i*de - O_3_r*de;
             put(14, 7, jv);
@@ -1699,6 +1984,27 @@ struct Net {
             jv = -O_3_c_O_3_c*de;
             jv = jv / mdensity;
             put(15, 7, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(0, 8);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(1, 8);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(2, 8);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(3, 8);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(4, 8);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(5, 8);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(6, 8);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = O_4_r*de;
@@ -1712,6 +2018,18 @@ struct Net {
             jv = O_4_i*de;
             put(9, 8, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(10, 8);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(11, 8);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(12, 8);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(13, 8);
+        }
         if (pick(NP, 0, 0, 2) == P) {
             jv = O_4_i*de - O_4_r*de;
             put(14, 8, jv);
@@ -1720,6 +2038,30 @@ struct Net {
             jv = -O_4_c_O_4_c*de;
             jv = jv / mdensity;
             put(15, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 9);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(2, 9);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(3, 9);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(4, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(5, 9);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 9);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 9);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = O_5_r*de;
@@ -1733,6 +2075,15 @@ struct Net {
             jv = O_5_i*de;
             put(10, 9, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(11, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(12, 9);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(13, 9);
+        }
         if (pick(NP, 0, 1, 0) == P) {
             jv = O_5_i*de - O_5_r*de;
             put(14, 9, jv);
@@ -1741,6 +2092,33 @@ struct Net {
             jv = -O_5_c_O_5_c*de;
             jv = jv / mdensity;
             put(15, 9, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 10);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 10);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 10);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(3, 10);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(4, 10);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(5, 10);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(6, 10);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(7, 10);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(8, 10);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = O_6_r*de;
@@ -1754,6 +2132,12 @@ struct Net {
             jv = O_6_i*de;
             put(11, 10, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(12, 10);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(13, 10);
+        }
         if (pick(NP, 0, 0, 3) == P) {
             jv = O_6_i*de - O_6_r*de;
             put(14, 10, jv);
@@ -1762,6 +2146,36 @@ struct Net {
             jv = -O_6_c_O_6_c*de;
             jv = jv / mdensity;
             put(15, 10, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(0, 11);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(1, 11);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(2, 11);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(3, 11);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 11);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 11);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(6, 11);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(7, 11);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(8, 11);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(9, 11);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = O_7_r*de;
@@ -1775,6 +2189,9 @@ struct Net {
             jv = O_7_i*de;
             put(12, 11, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(13, 11);
+        }
         if (pick(NP, 0, 1, 1) == P) {
             jv = O_7_i*de - O_7_r*de;
             put(14, 11, jv);
@@ -1783,6 +2200,39 @@ struct Net {
             jv = -O_7_c_O_7_c*de;
             jv = jv / mdensity;
             put(15, 11, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(0, 12);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(1, 12);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(2, 12);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(3, 12);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(4, 12);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(5, 12);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(6, 12);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 12);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(8, 12);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 12);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(10, 12);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = O_8_r*de;
@@ -1804,6 +2254,42 @@ struct Net {
             jv = -O_8_c_O_8_c*de;
             jv = jv / mdensity;
             put(15, 12, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 13);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 13);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(2, 13);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(3, 13);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(4, 13);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(5, 13);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 13);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 13);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(8, 13);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(9, 13);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(10, 13);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(11, 13);
         }
         if (pick(NP, 0, 1, 3) == P) {
             jv = O_9_r*de;
@@ -1886,6 +2372,54 @@ struct Net {
             jv = -H_1*H_1_c_H_1_c - H_2*H_2_c_H_2_c - He_1*He_1_c_He_1_c - He_2*He_2_c_He_2_c - He_3*He_3_c_He_3_c - O_1*O_1_c_O_1_c - O_2*O_2_c_O_2_c - O_3*O_3_c_O_3_c - O_4*O_4_c_O_4_c - O_5*O_5_c_O_5_c - O_6*O_6_c_O_6_c - O_7*O_7_c_O_7_c - O_8*O_8_c_O_8_c - O_9*O_9_c_O_9_c;
             jv = jv / mdensity;
             put(15, 14, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 15);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 15);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(2, 15);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(3, 15);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(4, 15);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(5, 15);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 15);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 15);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(8, 15);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(9, 15);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(10, 15);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(11, 15);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(12, 15);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(13, 15);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(14, 15);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(15, 15);
         }
         return true;
     }

@@ -919,91 +919,97 @@ struct Net {
         return true;
     }
 
-    /* The same Jacobian in FP32 arithmetic (the mixed-precision solve):
-     * y and the rates rounded to FP32 by the caller, put(eq, var, value)
-     * for the structurally nonzero entries only. */
+    /* The same Jacobian in extended-range FP32 (dg_xf.h), for the
+     * mixed-precision solve: every operation of the same expressions
+     * rounded to FP32's 24-bit significand, the exponent unbounded, so no
+     * FP64 instruction.  Same negative-value test and part split as jac();
+     * put(eq, var, value) receives an XF value for the structurally nonzero
+     * entries, put.zero(eq, var) the others. */
     template <int NP = 1, int P = 0, class RT, class Put>
-    __device__ __forceinline__ static bool jac32(const float (&y)[N], const RT &R, float Tge,
-                                                 float T, float z, const Put &put)
+    __device__ __forceinline__ static bool jacx(const double (&yd)[N], const RT &R, double Tge_d,
+                                                double T_d, double z_d, const Put &put)
     {
-        const float mh = 1.67e-24f;
-        float mdensity = 0.0f;
+        using dg::XF;
+        using dg::xf;
+        const XF mh = xf(1.67e-24);
+        XF mdensity = xf(0.0);
+        const XF Tge = xf(Tge_d), T = xf(T_d), z = xf(z_d);
         (void)Tge; (void)T; (void)z;
-        const float H2_1 = y[0];
-        mdensity += H2_1;
-        if (H2_1 < 0.0f) return false;
-        const float H2_2 = y[1];
-        mdensity += H2_2;
-        if (H2_2 < 0.0f) return false;
-        const float H_1 = y[2];
-        mdensity += H_1;
-        if (H_1 < 0.0f) return false;
-        const float H_2 = y[3];
-        mdensity += H_2;
-        if (H_2 < 0.0f) return false;
-        const float H_m0 = y[4];
-        mdensity += H_m0;
-        if (H_m0 < 0.0f) return false;
-        const float He_1 = y[5];
-        mdensity += He_1;
-        if (He_1 < 0.0f) return false;
-        const float He_2 = y[6];
-        mdensity += He_2;
-        if (He_2 < 0.0f) return false;
-        const float He_3 = y[7];
-        mdensity += He_3;
-        if (He_3 < 0.0f) return false;
-        const float de = y[8];
-        if (de < 0.0f) return false;
-        const float ge = y[9];
-        if (ge < 0.0f) return false;
-        mdensity *= mh;
-        const float k01 = R[0];
-        const float k02 = R[1];
-        const float k03 = R[2];
-        const float k04 = R[3];
-        const float k05 = R[4];
-        const float k06 = R[5];
-        const float k07 = R[6];
-        const float k08 = R[7];
-        const float k09 = R[8];
-        const float k10 = R[9];
-        const float k11 = R[10];
-        const float k12 = R[11];
-        const float k13 = R[12];
-        const float k14 = R[13];
-        const float k15 = R[14];
-        const float k16 = R[15];
-        const float k17 = R[16];
-        const float k18 = R[17];
-        const float k19 = R[18];
-        const float k21 = R[19];
-        const float k22 = R[20];
-        const float k23 = R[21];
-        const float brem_brem = R[22];
-        const float ceHI_ceHI = R[23];
-        const float ceHeI_ceHeI = R[24];
-        const float ceHeII_ceHeII = R[25];
-        const float ciHI_ciHI = R[26];
-        const float ciHeI_ciHeI = R[27];
-        const float ciHeII_ciHeII = R[28];
-        const float ciHeIS_ciHeIS = R[29];
-        const float compton_comp = R[30];
-        const float gammah_gammah = R[31];
-        const float gloverabel08_gaH2 = R[32];
-        const float gloverabel08_gaHI = R[33];
-        const float gloverabel08_gaHe = R[34];
-        const float gloverabel08_gaHp = R[35];
-        const float gloverabel08_gael = R[36];
-        const float gloverabel08_gphdl = R[37];
-        const float gloverabel08_gpldl = R[38];
-        const float h2formation_h2mcool = R[39];
-        const float h2formation_h2mheat = R[40];
-        const float reHII_reHII = R[41];
-        const float reHeII1_reHeII1 = R[42];
-        const float reHeII2_reHeII2 = R[43];
-        const float reHeIII_reHeIII = R[44];
-        float jv;
+        if (dg_lt0(yd[0])) return false;   /* H2_1 < 0.0 */
+        const XF H2_1 = xf(yd[0]);
+        mdensity = mdensity + H2_1;
+        if (dg_lt0(yd[1])) return false;   /* H2_2 < 0.0 */
+        const XF H2_2 = xf(yd[1]);
+        mdensity = mdensity + H2_2;
+        if (dg_lt0(yd[2])) return false;   /* H_1 < 0.0 */
+        const XF H_1 = xf(yd[2]);
+        mdensity = mdensity + H_1;
+        if (dg_lt0(yd[3])) return false;   /* H_2 < 0.0 */
+        const XF H_2 = xf(yd[3]);
+        mdensity = mdensity + H_2;
+        if (dg_lt0(yd[4])) return false;   /* H_m0 < 0.0 */
+        const XF H_m0 = xf(yd[4]);
+        mdensity = mdensity + H_m0;
+        if (dg_lt0(yd[5])) return false;   /* He_1 < 0.0 */
+        const XF He_1 = xf(yd[5]);
+        mdensity = mdensity + He_1;
+        if (dg_lt0(yd[6])) return false;   /* He_2 < 0.0 */
+        const XF He_2 = xf(yd[6]);
+        mdensity = mdensity + He_2;
+        if (dg_lt0(yd[7])) return false;   /* He_3 < 0.0 */
+        const XF He_3 = xf(yd[7]);
+        mdensity = mdensity + He_3;
+        if (dg_lt0(yd[8])) return false;   /* de < 0.0 */
+        const XF de = xf(yd[8]);
+        if (dg_lt0(yd[9])) return false;   /* ge < 0.0 */
+        const XF ge = xf(yd[9]);
+        mdensity = mdensity * mh;
+        const XF k01 = xf(R[0]);
+        const XF k02 = xf(R[1]);
+        const XF k03 = xf(R[2]);
+        const XF k04 = xf(R[3]);
+        const XF k05 = xf(R[4]);
+        const XF k06 = xf(R[5]);
+        const XF k07 = xf(R[6]);
+        const XF k08 = xf(R[7]);
+        const XF k09 = xf(R[8]);
+        const XF k10 = xf(R[9]);
+        const XF k11 = xf(R[10]);
+        const XF k12 = xf(R[11]);
+        const XF k13 = xf(R[12]);
+        const XF k14 = xf(R[13]);
+        const XF k15 = xf(R[14]);
+        const XF k16 = xf(R[15]);
+        const XF k17 = xf(R[16]);
+        const XF k18 = xf(R[17]);
+        const XF k19 = xf(R[18]);
+        const XF k21 = xf(R[19]);
+        const XF k22 = xf(R[20]);
+        const XF k23 = xf(R[21]);
+        const XF brem_brem = xf(R[22]);
+        const XF ceHI_ceHI = xf(R[23]);
+        const XF ceHeI_ceHeI = xf(R[24]);
+        const XF ceHeII_ceHeII = xf(R[25]);
+        const XF ciHI_ciHI = xf(R[26]);
+        const XF ciHeI_ciHeI = xf(R[27]);
+        const XF ciHeII_ciHeII = xf(R[28]);
+        const XF ciHeIS_ciHeIS = xf(R[29]);
+        const XF compton_comp = xf(R[30]);
+        const XF gammah_gammah = xf(R[31]);
+        const XF gloverabel08_gaH2 = xf(R[32]);
+        const XF gloverabel08_gaHI = xf(R[33]);
+        const XF gloverabel08_gaHe = xf(R[34]);
+        const XF gloverabel08_gaHp = xf(R[35]);
+        const XF gloverabel08_gael = xf(R[36]);
+        const XF gloverabel08_gphdl = xf(R[37]);
+        const XF gloverabel08_gpldl = xf(R[38]);
+        const XF h2formation_h2mcool = xf(R[39]);
+        const XF h2formation_h2mheat = xf(R[40]);
+        const XF reHII_reHII = xf(R[41]);
+        const XF reHeII1_reHeII1 = xf(R[42]);
+        const XF reHeII2_reHeII2 = xf(R[43]);
+        const XF reHeIII_reHeIII = xf(R[44]);
+        XF jv;
         if (pick(NP, 0, 1, 0) == P) {
             jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
             put(0, 0, jv);
@@ -1019,6 +1025,21 @@ struct Net {
         if (pick(NP, 0, 1, 0) == P) {
             jv = -k11*H_2 + 2*k12*de;
             put(3, 0, jv);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(4, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(5, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(6, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(7, 0);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(8, 0);
         }
         if (pick(NP, 0, 1, 1) == P) {
             jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f);
@@ -1045,9 +1066,21 @@ struct Net {
             jv = -k19*H_m0;
             put(4, 1, jv);
         }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(5, 1);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(6, 1);
+        }
+        if (pick(NP, 0, 1, 2) == P) {
+            put.zero(7, 1);
+        }
         if (pick(NP, 0, 1, 0) == P) {
             jv = -k18*de;
             put(8, 1, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 1);
         }
         if (pick(NP, 0, 1, 1) == P) {
             jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
@@ -1068,6 +1101,15 @@ struct Net {
         if (pick(NP, 0, 0, 1) == P) {
             jv = k07*de - k08*H_m0 - k15*H_m0;
             put(4, 2, jv);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 2);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 2);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 2);
         }
         if (pick(NP, 0, 1, 1) == P) {
             jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
@@ -1098,6 +1140,15 @@ struct Net {
             jv = -k16*H_m0 - k17*H_m0;
             put(4, 3, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(5, 3);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(6, 3);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(7, 3);
+        }
         if (pick(NP, 0, 1, 0) == P) {
             jv = -k02*de + k17*H_m0;
             put(8, 3, jv);
@@ -1127,9 +1178,36 @@ struct Net {
             jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
             put(4, 4, jv);
         }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 4);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(6, 4);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(7, 4);
+        }
         if (pick(NP, 0, 0, 3) == P) {
             jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
             put(8, 4, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(9, 4);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(0, 5);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(1, 5);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(2, 5);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(3, 5);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(4, 5);
         }
         if (pick(NP, 0, 1, 2) == P) {
             jv = -k03*de;
@@ -1139,6 +1217,9 @@ struct Net {
             jv = k03*de;
             put(6, 5, jv);
         }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(7, 5);
+        }
         if (pick(NP, 0, 1, 2) == P) {
             jv = k03*de;
             put(8, 5, jv);
@@ -1147,6 +1228,21 @@ struct Net {
             jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
             jv = jv / mdensity;
             put(9, 5, jv);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(0, 6);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(1, 6);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(2, 6);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(3, 6);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(4, 6);
         }
         if (pick(NP, 0, 0, 3) == P) {
             jv = k04*de;
@@ -1168,6 +1264,24 @@ struct Net {
             jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
             jv = jv / mdensity;
             put(9, 6, jv);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(0, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(1, 7);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(2, 7);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(3, 7);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(4, 7);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(5, 7);
         }
         if (pick(NP, 0, 0, 1) == P) {
             jv = k06*de;
@@ -1226,6 +1340,36 @@ struct Net {
             jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0f*He_3) - compton_comp*dg_ipow<4>(z + 1.0f)*(T - 2.73f*z - 2.73f);
             jv = jv / mdensity;
             put(9, 8, jv);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(0, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(1, 9);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(2, 9);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(3, 9);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(4, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(5, 9);
+        }
+        if (pick(NP, 0, 0, 2) == P) {
+            put.zero(6, 9);
+        }
+        if (pick(NP, 0, 1, 3) == P) {
+            put.zero(7, 9);
+        }
+        if (pick(NP, 0, 0, 0) == P) {
+            put.zero(8, 9);
+        }
+        if (pick(NP, 0, 1, 1) == P) {
+            put.zero(9, 9);
         }
         return true;
     }
