@@ -28,6 +28,7 @@ HARNESS = r'''
 #define __host__
 #define __forceinline__ inline
 #include "dg_math.h"
+#include "dg_xf.h"
 #include "%(name)s_solver.h"
 %(net)s
 using Net = dgnet_%(name)s::Net;
@@ -43,13 +44,18 @@ struct Put {
     void operator()(int q, int v, double jv) const { J[v * N + q] = jv; }
     void zero(int q, int v) const { J[v * N + q] = 0.0; }
 };
+struct PutX {
+    double *J;
+    void operator()(int q, int v, dg::XF jv) const { J[v * N + q] = dg::xf_to_double(jv); }
+    void zero(int q, int v) const { J[v * N + q] = 0.0; }
+};
 
 /* Per cell (number densities + ge, AoS): T, the interpolated rates, the
  * RHS and the Jacobian (J[var*N + eq]) as the engines compute them, the
  * interpolation restated from dg_engine.cuh's interpolate(). */
 extern "C" int dgx_eval(const double *input, long long ncells, const double *const *tables,
                         double Tlo, double Thi, double z, double *T_out, double *R_out,
-                        double *f_out, double *J_out, int *ok_out)
+                        double *f_out, double *J_out, int *ok_out, double *Jx_out)
 {
     if (Net::HAS_Z) return -1;
     const int nbins = Net::NT_LEN - 1;
@@ -77,6 +83,10 @@ extern "C" int dgx_eval(const double *input, long long ncells, const double *con
         double *J = J_out + c * N * N;
         for (int i = 0; i < N * N; i++) J[i] = 0.0;
         if (ok) Net::jac(y, Rates{R}, Tge, T, z, Put{J});
+        /* the mixed solve's extended-range FP32 Jacobian */
+        double *Jx = Jx_out + c * N * N;
+        for (int i = 0; i < N * N; i++) Jx[i] = 0.0;
+        if (ok) Net::jacx(y, Rates{R}, Tge, T, z, PutX{Jx});
     }
     return 0;
 }
@@ -111,7 +121,7 @@ def harness(name, tmp_path_factory):
                                str(src), "-o", str(so)])
         lib = C.CDLL(str(so))
         lib.dgx_eval.argtypes = [P_D, C.c_longlong, C.POINTER(P_D), C.c_double, C.c_double,
-                                 C.c_double, P_D, P_D, P_D, P_D, C.POINTER(C.c_int)]
+                                 C.c_double, P_D, P_D, P_D, P_D, C.POINTER(C.c_int), P_D]
         _LIBS[name] = lib
     return _LIBS[name]
 
@@ -156,10 +166,11 @@ def test_device_expressions_match_oracle(name, z, tmp_path_factory):
     f = np.zeros((ncell, N))
     J = np.zeros((ncell, N * N))
     ok = np.zeros(ncell, np.int32)
+    Jx = np.zeros((ncell, N * N))
     Tlo, Thi = float(net.T_bounds[0]), float(net.T_bounds[1])
     assert lib.dgx_eval(y.ctypes.data_as(P_D), ncell, tptr, Tlo, Thi, z, T.ctypes.data_as(P_D),
                         R.ctypes.data_as(P_D), f.ctypes.data_as(P_D), J.ctypes.data_as(P_D),
-                        ok.ctypes.data_as(C.POINTER(C.c_int))) == 0
+                        ok.ctypes.data_as(C.POINTER(C.c_int)), Jx.ctypes.data_as(P_D)) == 0
     assert ok.all()
 
     # the oracle's strip functions (one strip of all cells)
@@ -187,3 +198,17 @@ def test_device_expressions_match_oracle(name, z, tmp_path_factory):
     js = np.abs(J_ref).max(axis=1, keepdims=True)
     assert np.all(np.abs(J - J_ref) <= 1e-13 * js)
     assert np.mean(np.all(J == J_ref, axis=1)) >= 0.9
+    # the extended-range FP32 Jacobian of the mixed solve: FP32 rounding
+    # (2^-24 per operation) but no entry lost to FP32's range -- entries
+    # made of tables far below 1e-38 keep their value; measured against
+    # each entry's own size, floored at 1e-6 of the row's largest entry
+    # (below that cancellation dominates and the entry is negligible in
+    # the scaled Newton matrix anyway)
+    rows = np.abs(J_ref).reshape(ncell, N, N).max(axis=1, keepdims=True)
+    floor = np.maximum(np.abs(J_ref).reshape(ncell, N, N), 1e-6 * rows).reshape(ncell, N * N)
+    err = np.where(J_ref == 0, np.abs(Jx), np.abs(Jx - J_ref)) / np.where(floor > 0, floor, 1.0)
+    assert err.max() <= 1e-4, err.max()
+    # (FP64 subnormals convert to zero by design)
+    tiny = (np.abs(J_ref) > 1e-300) & (np.abs(J_ref) < 1e-38)
+    if tiny.any():
+        assert np.all(Jx[tiny] != 0)
