@@ -44,6 +44,9 @@ PRIMORDIAL_CONFIGS = {
     # ionised gas only (T >= 3e5 K): the stiff cells that run to the substep
     # cap; used to profile the per-cell critical path
     "hot": dict(nH=(1.0, 1e6), T=(3e5, 1e8), unstable=0.0, seed=20245),
+    # the top decade of the tables (T up to just below the last bin, whose
+    # upper neighbour the reference reads past the table's end)
+    "top": dict(nH=(1e-3, 1e12), T=(1e8, 0.999e9), unstable=0.0, seed=20247),
 }
 
 

@@ -68,6 +68,31 @@ def test_gpu_matches_reference_golden(solver, golden, tag):
     # are compared only through the status.
 
 
+@pytest.fixture(scope="module")
+def crlog_oracle():
+    from oracle import Oracle
+    return Oracle("primordial", crlog=True)
+
+
+@pytest.mark.parametrize("config", ["config1", "config2", "config3", "top"])
+def test_gpu_matches_oracle_1024_cells(solver, crlog_oracle, config):
+    """1024 seeded cells of each configuration -- config 3's thermally
+    unstable band (5 % of its cells) and the tables' top decade (T up to
+    0.999e9 K) included -- against the oracle with a correctly rounded
+    log T, as the device's: the same status on every cell; on cells that
+    converge, the state within 1e-10 and the same substep and sweep counts."""
+    from dengo_gb300.workloads import primordial_cells
+    seed = {"config1": 1024, "config2": 2048, "config3": 3072, "top": 4096}[config]
+    state, dtf = primordial_cells(1024, config, seed=seed)
+    out = solver.solve_host(state, dtf, rtol=1e-6, counters=True)
+    ref = crlog_oracle.evolve_cells(solver._tables, state, dtf, nthreads=0)
+    check_cells(out["state"], ref["state"], out["status"], ref["status"], config)
+    ok = ref["status"] == 0
+    assert ok.sum() > 300
+    for k in ("substeps", "sweeps"):
+        assert np.array_equal(out[k][ok], ref[k][ok]), k
+
+
 @pytest.mark.parametrize("config,n", [("config1", 96), ("config3", 96)])
 def test_gpu_matches_oracle(solver, oracle, config, n):
     from dengo_gb300.workloads import primordial_cells
