@@ -43,6 +43,7 @@ class Request:
     # filled in by the loop
     result: np.ndarray = None
     status: np.ndarray = None
+    sweeps: np.ndarray = None      # Newton sweeps of each cell in its last step
     t_admit: float = None
     t_done: float = None
 
@@ -193,10 +194,12 @@ class ServingLoop:
             out.copy_(st, non_blocking=True)
             out_status = torch.empty(g.ncells, dtype=torch.int32, pin_memory=True)
             out_status.copy_(status, non_blocking=True)
+            out_sweeps = torch.empty(g.ncells, dtype=torch.int32, pin_memory=True)
+            out_sweeps.copy_(sweeps, non_blocking=True)
             g.event = torch.cuda.Event()
             g.event.record(slot.stream)
         g.tensors = dict(st=st, at=at, status=status, sweeps=sweeps, dtf=d_dtf, h_state=h_state,
-                         h_dtf=h_dtf, out=out, out_status=out_status)
+                         h_dtf=h_dtf, out=out, out_status=out_status, out_sweeps=out_sweeps)
         self.used += g.nbytes
         slot.group = g
 
@@ -205,9 +208,11 @@ class ServingLoop:
         t = self.now()
         out = g.tensors["out"].numpy()
         ost = g.tensors["out_status"].numpy()
+        osw = g.tensors["out_sweeps"].numpy()
         for r, a, b in zip(g.requests, g.offsets[:-1], g.offsets[1:]):
             r.result = out[a:b].copy()
             r.status = ost[a:b].copy()
+            r.sweeps = osw[a:b].copy()
             r.t_done = t
             self.done.append(r)
         self.used -= g.nbytes
@@ -243,15 +248,23 @@ class ServingLoop:
                 time.sleep(2e-4)
 
     # -- a timed run over an arrival schedule --------------------------------
-    def run(self, requests, timeout=600.0):
+    def run(self, requests, timeout=600.0, admit_until=None):
         """Submit each request at its ``arrival`` time (seconds from now) and
-        serve until all are done.  Returns the latency/throughput summary."""
+        serve until all are done.  With ``admit_until`` (seconds) no request
+        is admitted after that time: requests still pending then are left
+        unserved (the backlog), groups already on the device finish.
+        Returns the latency/throughput summary of the served requests."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         self.t0 = time.perf_counter()
         i = 0
         t_end = self.t0 + timeout
         while i < len(reqs) or self.busy():
             now = self.now()
+            if admit_until is not None and now > admit_until:
+                self.pending.clear()
+                i = len(reqs)
+                if not any(s.group is not None for s in self.slots):
+                    break
             while i < len(reqs) and reqs[i].arrival <= now:
                 self.submit(reqs[i])
                 i += 1
@@ -259,7 +272,11 @@ class ServingLoop:
                 time.sleep(1e-4)
             if time.perf_counter() > t_end:
                 raise TimeoutError("serving run did not finish in %.0f s" % timeout)
-        return summarize(reqs)
+        out = summarize([r for r in reqs if r.t_done is not None])
+        out["offered_requests"] = len(reqs)
+        out["backlog_requests"] = sum(1 for r in reqs if r.t_done is None)
+        out["backlog_cells"] = int(sum(r.ncells for r in reqs if r.t_done is None))
+        return out
 
 
 def summarize(reqs):
@@ -277,13 +294,13 @@ def summarize(reqs):
 _POOLS = {}
 
 
-def _pool(network, ncells, seed):
+def _pool(network, ncells, seed, primordial_config="config1"):
     """Seeded cell states of one network, generated once per process."""
     from .workloads import oxygen_cells, primordial_cells
-    key = (network, ncells, seed)
+    key = (network, ncells, seed, primordial_config)
     if key not in _POOLS:
         if network == "primordial":
-            _POOLS[key] = primordial_cells(ncells, "config1", seed=seed)[0]
+            _POOLS[key] = primordial_cells(ncells, primordial_config, seed=seed)[0]
         else:
             _POOLS[key] = oxygen_cells(ncells, seed=seed)[0]
     return _POOLS[key]
@@ -291,12 +308,13 @@ def _pool(network, ncells, seed):
 
 def poisson_requests(rate, duration, edge_range=(16, 128), mix=(("primordial", 0.7),
                      ("oxygen", 0.3)), dt_range=(1e8, 1e12), seed=5, max_edge=None,
-                     pool_cells=None):
+                     pool_cells=None, primordial_config="config1"):
     """The serving workload: Poisson arrivals at ``rate`` per second for
     ``duration`` seconds; cubic patches with edge ~ logU(edge_range) cells;
     networks drawn by ``mix``; dtf ~ logU(dt_range) s.  Patch contents are
     contiguous slices, at seeded offsets, of one seeded pool of cells per
-    network (primordial config-1 distributions; oxygen ion-by-ion cells)."""
+    network (primordial cells of ``primordial_config``'s distributions;
+    oxygen ion-by-ion cells)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     hi = min(edge_range[1], max_edge) if max_edge else edge_range[1]
     pool_cells = pool_cells or max(hi ** 3, 4096) * 2
@@ -313,7 +331,8 @@ def poisson_requests(rate, duration, edge_range=(16, 128), mix=(("primordial", 0
             edge = min(edge, max_edge)
         n = edge ** 3
         net = names[rng.choice(len(names), p=p)]
-        pool = _pool(net, pool_cells, seed + (0 if net == "primordial" else 1))
+        pool = _pool(net, pool_cells, seed + (0 if net == "primordial" else 1),
+                     primordial_config)
         off = int(rng.integers(0, pool.shape[0] - n + 1))
         dtf = float(np.exp(rng.uniform(np.log(dt_range[0]), np.log(dt_range[1]))))
         out.append(Request(net, pool[off:off + n], dtf, arrival=t, rid=len(out)))
