@@ -37,6 +37,7 @@ static inline double __fma_rn(double a, double b, double c) { return fma(a, b, c
 #include "dg_math.h"
 #include "dg_slots.cuh"
 #include "dg_mixed.cuh"
+#include "dg_xf.h"
 #include "primordial_solver.h"
 '''
 
