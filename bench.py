@@ -55,7 +55,8 @@ METRIC = "cells/s at <=1e-6 rel err vs FP64 oracle (mixed vs plain)"
 # DRAM bytes per cell of one solver launch, from the ncu captures of the
 # split engine on 14 592 cells (read + write; the state and tolerances, the
 # tables stay in L2).
-DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592}
+DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592,
+                       "mixed_xf": 5.14512e6 / 14592}
 # solver kernels per hydro step with a cost hint and a sweep budget: the
 # three order kernels, the first launch, and two resume launches each after
 # two list kernels
@@ -70,7 +71,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cells", type=int, default=32768, help="cells per GPU")
     p.add_argument("--config", default="config2")
-    p.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
+    p.add_argument("--precision", default="both",
+                   choices=["both", "all", "fp64", "mixed", "mixed_xf"],
+                   help="both: fp64 and mixed; all: also mixed_xf (the Newton matrix built "
+                        "in extended-range FP32)")
     p.add_argument("--schedule", type=int, default=3, help="1 per-thread, 2 stride, 3 queue")
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--parity-sample", type=int, default=256)
@@ -244,7 +248,7 @@ class HostArm:
     with pinned host buffers."""
 
     def __init__(self, solver, state0, dtf, args, precision, torch):
-        from dengo_gb300.runtime import CellBatch, DENGO_MIXED, DENGO_FP64
+        from dengo_gb300.runtime import CellBatch, DENGO_MIXED, DENGO_MIXED_XF, DENGO_FP64
         self.solver, self.args, self.torch = solver, args, torch
         n = len(dtf)
         self.n = n
@@ -262,7 +266,8 @@ class HostArm:
         self.hint[:] = np.minimum(temperatures(state0), 2e9).astype(np.int32)
         cfg = solver.default_config()
         cfg.schedule, cfg.block = args.schedule, args.block
-        cfg.precision = DENGO_MIXED if precision == "mixed" else DENGO_FP64
+        cfg.precision = {"fp64": DENGO_FP64, "mixed": DENGO_MIXED,
+                         "mixed_xf": DENGO_MIXED_XF}[precision]
         cfg.warps_per_cell = args.warps_per_cell
         cfg.sweep_budget, cfg.tail_grid = args.sweep_budget, args.tail_grid
         cfg.max_substeps = args.max_substeps
@@ -372,7 +377,8 @@ def run_ours(args):
     solver = Solver("primordial")
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     sample = 0 if args.no_parity else min(args.parity_sample, n)
-    precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    precisions = {"both": ["fp64", "mixed"], "all": ["fp64", "mixed", "mixed_xf"]}.get(
+        args.precision, [args.precision])
 
     clocks = Clocks(dev.index)
     if dist:
@@ -455,12 +461,13 @@ def run_ours(args):
                      "flop_per_sweep": F_SWEEP},
         "e2e": f["e2e"], "parity": f["parity"],
     }
-    if "mixed" in arms and main != "mixed":
-        m = figures("mixed")
-        m["speedup_vs_fp64"] = m["value"] / f["value"] if f["value"] else None
-        m["e2e_speedup_vs_fp64"] = (m["e2e"]["value"] / f["e2e"]["value"]
-                                    if f["e2e"]["value"] else None)
-        line["mixed"] = m
+    for other in ("mixed", "mixed_xf"):
+        if other in arms and main != other:
+            m = figures(other)
+            m["speedup_vs_fp64"] = m["value"] / f["value"] if f["value"] else None
+            m["e2e_speedup_vs_fp64"] = (m["e2e"]["value"] / f["e2e"]["value"]
+                                        if f["e2e"]["value"] else None)
+            line[other] = m
     if not args.no_cpu_baseline:
         base, _ = cpu_baseline(state0, dtf, args.cpu_seconds)
         line["cpu_baseline"] = base

@@ -283,7 +283,7 @@ template <class Net>
 int launch_engine(Gpu *g, const CellIO &io, const TableSet &ts, const KernelCfg &kc,
                   const dengo_solver_config &cfg, cudaStream_t st, unsigned long long *queue)
 {
-    const bool mixed = cfg.precision == DENGO_MIXED;
+    const bool mixed = cfg.precision == DENGO_MIXED || cfg.precision == DENGO_MIXED_XF;
     const int sch = cfg.schedule, gr = cfg.grid;
     if (cfg.warps_per_cell == 2)
         return mixed ? launch_split<Net, 2, true>(g, io, ts, kc, sch, gr, st, queue)
@@ -537,7 +537,8 @@ struct Api {
         dengo_solver_config cfg;
         if (cfg_in) cfg = *cfg_in;
         else dengo_default_config(&cfg);
-        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED) {
+        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED &&
+            cfg.precision != DENGO_MIXED_XF) {
             set_error("%s_solve_cells_device: unknown precision %d", Net::NAME, cfg.precision);
             return -1;
         }
@@ -553,6 +554,7 @@ struct Api {
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         kc.cons_tol = cfg.conservation_tol > 0.0 ? cfg.conservation_tol : 0.0;
+        kc.jac_xf = cfg.precision == DENGO_MIXED_XF;
         if (cfg.sweep_budget <= 0 || b->ncells <= 0)
             return launch_engine<Net>(g, io, ts, kc, cfg, st, g->queue);
         return solve_redistributed(g, io, ts, kc, cfg, st);
@@ -650,7 +652,8 @@ struct Api {
         dengo_solver_config cfg;
         if (cfg_in) cfg = *cfg_in;
         else dengo_default_config(&cfg);
-        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED) {
+        if (cfg.precision != DENGO_FP64 && cfg.precision != DENGO_MIXED &&
+            cfg.precision != DENGO_MIXED_XF) {
             set_error("%s_solve_cells_device_noalloc: unknown precision %d", Net::NAME,
                       cfg.precision);
             return -1;
@@ -669,6 +672,7 @@ struct Api {
         }
         KernelCfg kc{cfg.max_newton_sweeps, cfg.max_substeps, cfg.dt_ratio_floor, cfg.floor_value};
         kc.cons_tol = cfg.conservation_tol > 0.0 ? cfg.conservation_tol : 0.0;
+        kc.jac_xf = cfg.precision == DENGO_MIXED_XF;
         return launch_engine<Net>(g, io, ts, kc, cfg, st, queue);
     }
 
@@ -754,7 +758,8 @@ struct Api {
         dengo_solver_config c;
         if (cfg) c = *cfg;
         else dg_default_config_impl(&c);
-        if (c.precision != DENGO_FP64 && c.precision != DENGO_MIXED) {
+        if (c.precision != DENGO_FP64 && c.precision != DENGO_MIXED &&
+            c.precision != DENGO_MIXED_XF) {
             set_error("%s_set_solver_config: unknown precision %d", Net::NAME, c.precision);
             return -1;
         }

@@ -97,6 +97,9 @@ struct KernelCfg {
      * -- a relative drift of any invariant beyond cons_tol re-solves the
      * cell with FP64 linear solves; 0: no check */
     double cons_tol;
+    /* mixed precision: build the Newton matrix in extended-range FP32
+     * (DENGO_MIXED_XF) instead of from FP64 products */
+    int jac_xf;
 };
 
 /* Suspension record of a cell at a substep boundary: state y, prev, scale,
@@ -393,9 +396,10 @@ __device__ __forceinline__ bool conserved(const CellIO &io, long long cell,
 }
 
 /* MIXED = false: the reference's FP64 arithmetic throughout (bit-faithful).
- * MIXED = true: the Newton matrix is built in extended-range FP32 (jacx,
- * JacPutX) and solved by MixedSolve (equilibrated FP32 LU + FP64 iterative
- * refinement, dg_mixed.cuh), falling back to the FP64 Jacobian and
+ * MIXED = true: the Newton matrix -- formed from FP64 products as the FP64
+ * path forms it or, with cfg.jac_xf, built in extended-range FP32 (jacx,
+ * JacPutX) -- is solved by MixedSolve (equilibrated FP32 LU + FP64
+ * iterative refinement, dg_mixed.cuh), falling back to the FP64 Jacobian and
  * elimination for a cell whose matrix holds inf/NaN or whose scales are not
  * all positive and finite, and re-solving with FP64 linear solves a
  * converged cell that fails the FP64 conservation check; temperature,
@@ -594,7 +598,7 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 #pragma unroll
                 for (int i = 0; i < N; i++) y[i] = u[i] * SC[i];
                 const bool dense_j = dense || !(dt > 0.0);
-                if (MIXED && !dense_j && !fp64cell) {
+                if (MIXED && cfg.jac_xf && !dense_j && !fp64cell) {
                     /* the Jacobian in extended-range FP32 */
                     const JacPutX<N, BLOCK> put{J, INV, SC, -dt};
                     ok = Net::jacx(y, R, Tge, T, ts.z, put);

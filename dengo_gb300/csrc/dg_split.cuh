@@ -328,7 +328,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             double y[N];
             for (int i = 0; i < N; i++) y[i] = Y[i];
             bool ok = true;
-            if (MIXED && !F(F_DENSE) && !F(F_FP64)) {
+            if (MIXED && cfg.jac_xf && !F(F_DENSE) && !F(F_FP64)) {
                 /* mixed: the Jacobian in extended-range FP32 */
                 const JacPutX<N, 32> put{J, INV, SC, S[3]};
                 switch (w) {

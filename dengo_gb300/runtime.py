@@ -19,7 +19,7 @@ P_D = C.POINTER(C.c_double)
 P_I = C.POINTER(C.c_int)
 
 DENGO_OK, DENGO_MAX_SUBSTEPS, DENGO_DT_UNDERFLOW = 0, 1, 2
-DENGO_FP64, DENGO_MIXED = 0, 1
+DENGO_FP64, DENGO_MIXED, DENGO_MIXED_XF = 0, 1, 2
 DENGO_EVOLVE_LOCKSTEP, DENGO_EVOLVE_PER_CELL = 0, 1
 SCHED_AUTO, SCHED_PER_THREAD, SCHED_STRIDE, SCHED_QUEUE = 0, 1, 2, 3
 

@@ -84,7 +84,15 @@ enum dengo_cell_status {
 /* Arithmetic of the Newton step. */
 enum dengo_precision {
     DENGO_FP64 = 0,            /* the reference's FP64 arithmetic, bit-faithful */
-    DENGO_MIXED = 1            /* equilibrated FP32 LU + FP64 iterative refinement of each Newton step */
+    DENGO_MIXED = 1,           /* the Newton matrix formed from FP64 products,
+                                  rounded to FP32 after power-of-two
+                                  equilibration, FP32 LU + FP64 iterative
+                                  refinement of each Newton step, FP64
+                                  conservation check */
+    DENGO_MIXED_XF = 2         /* as DENGO_MIXED, the Newton matrix built in
+                                  extended-range FP32 (FP32 significand,
+                                  integer exponent: no FP64 instruction);
+                                  measured slower than DENGO_MIXED on GB300 */
 };
 
 /* How cells are assigned to lanes. */

@@ -376,7 +376,9 @@ extern "C" int hx_evolve(double *state, double *atol, const double *dtf, long lo
     for (int k = 0; k < NT && k < DG_MAX_TABLES; k++) ts.zvals[k] = zvals[k];
     dg::CellIO io{state, atol, nullptr, rtol_scalar, dtf, 0.0, dt, ttot, status, substeps, sweeps,
                   failures, nullptr, NN, 1, ncells};
-    dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1, cons_tol};
+    /* mixed = 2: the Newton matrix in extended-range FP32 */
+    dg::KernelCfg kc{max_sweeps, 50000, 1e-15, 1e-25, 0, 0, nullptr, nullptr, 1, cons_tol,
+                     mixed == 2 ? 1 : 0};
     unsigned long long queue = 0;
     unsigned long long *q = schedule_queue ? &queue : nullptr;
     if (sweep_budget <= 0) {

@@ -83,17 +83,19 @@ def test_redistribution_is_bit_identical(engines, tables, mixed, budget):
         assert np.array_equal(one[k], three[k]), k
 
 
-@pytest.mark.parametrize("build", ["default", "lenient"])
+@pytest.mark.parametrize("build,mixed", [("default", 1), ("lenient", 1), ("default", 2)])
 @pytest.mark.parametrize("config,seed,n,min_frac", [("config1", 404, 96, 1.0),
                                                      ("config3", 407, 128, 0.97)])
-def test_mixed_engine_within_1e6(engines, tables, crlog_oracle, build, config, seed, n, min_frac):
+def test_mixed_engine_within_1e6(engines, tables, crlog_oracle, build, mixed, config, seed, n,
+                                 min_frac):
     """Every oracle-converged cell converges; floored relative error
     (atol = 1e-6 x input) within 1e-6 on every config-1 cell and >= 97 % of
     config-3 cells -- the GPU test's cells and bar -- for both mixed
-    builds."""
+    builds, and with the Newton matrix built in extended-range FP32
+    (mixed = 2, DENGO_MIXED_XF)."""
     from dengo_gb300.workloads import primordial_cells
     st, dtf = primordial_cells(n, config, seed=seed)
-    h = he.evolve(engines[build], tables, st, dtf, mixed=True)
+    h = he.evolve(engines[build], tables, st, dtf, mixed=mixed)
     ref = crlog_oracle.evolve_cells(tables, st, dtf, nthreads=0)
     conv = ref["status"] == 0
     assert np.all(h["status"][conv] == 0)

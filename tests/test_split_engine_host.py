@@ -44,10 +44,11 @@ def _same(a, b):
         assert np.array_equal(a[k], b[k]), k
 
 
-@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("mixed", [0, 1, 2])
 def test_split_equals_lane(libs, tables, mixed):
     """32 cold cells (a few hundred sweeps each), one launch and with a
-    sweep budget of 100 (cells set aside and resumed twice)."""
+    sweep budget of 100 (cells set aside and resumed twice); FP64, mixed,
+    and mixed with the Newton matrix in extended-range FP32 (2)."""
     from dengo_gb300.workloads import primordial_cells
     st, dtf = primordial_cells(32, "cold", seed=11)
     lane = he.evolve(libs["lane"], tables, st, dtf, mixed=mixed)
