@@ -59,8 +59,13 @@ DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592,
                        "mixed_xf": 5.14512e6 / 14592}
 # solver kernels per hydro step with a cost hint and a sweep budget: the
 # three order kernels, the first launch, and two resume launches each after
-# two list kernels
+# two list kernels (FP64 with the wide tail: each resume launch followed by
+# the wide engine's)
 LAUNCHES_PER_STEP = 3 + 1 + 2 * (2 + 1)
+
+
+def launches_per_step(precision, wide_tail):
+    return LAUNCHES_PER_STEP + (2 if precision == "fp64" and wide_tail else 0)
 
 
 def parse():
@@ -85,6 +90,8 @@ def parse():
                    help="> 0: redistribute cells still running after this many Newton "
                         "sweeps into later, densely packed launches (same results)")
     p.add_argument("--tail-grid", type=int, default=0)
+    p.add_argument("--wide-tail", type=int, default=3,
+                   help="FP64: set-aside cells per SM the wide engine takes (0: off)")
     p.add_argument("--max-substeps", type=int, default=50000,
                    help="the reference's cap; lower only to profile a short launch")
     p.add_argument("--no-parity", action="store_true")
@@ -270,6 +277,7 @@ class HostArm:
                          "mixed_xf": DENGO_MIXED_XF}[precision]
         cfg.warps_per_cell = args.warps_per_cell
         cfg.sweep_budget, cfg.tail_grid = args.sweep_budget, args.tail_grid
+        cfg.wide_tail = args.wide_tail
         cfg.max_substeps = args.max_substeps
         self.cfg = cfg
         a = lambda x: x.ctypes.data
@@ -436,6 +444,7 @@ def run_ours(args):
     achieved = a["sweeps_all"] * F_SWEEP / (a["dev_total_ms"] / 1e3) / 1e12
     engine = {"precision": main, "warps_per_cell": args.warps_per_cell,
               "schedule": args.schedule, "sweep_budget": args.sweep_budget,
+              "wide_tail": args.wide_tail,
               "order": "costliest first (cost hint)" if args.order else "input order",
               "warmup": "%d steps over a 4096-cell copy" % args.warmup}
     line = {
@@ -446,7 +455,8 @@ def run_ours(args):
         "data": "synthetic (seeded)", "config": config_dict(args), "engine": engine,
         "converged_cells_per_s": f["converged_cells_per_s"],
         "frac_within_1e-6": f["frac_within_1e-6"], "step_ms": f["step_ms"],
-        "gpu_launches": LAUNCHES_PER_STEP * args.steps * len(precisions),
+        "gpu_launches": args.steps * sum(launches_per_step(p, args.wide_tail)
+                                         for p in precisions),
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak else None,

@@ -25,6 +25,7 @@
 #include "dg_split.cuh"
 #include "dg_strip.cuh"
 #include "dg_tablefile.h"
+#include "dg_wide.cuh"
 
 extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg);
 
@@ -272,6 +273,24 @@ int launch_split(Gpu *g, const CellIO &io, const TableSet &ts, const KernelCfg &
         }
     }
     kern<<<grid, 32 * NP, smem, st>>>(io, ts, kc, q);
+    DG_CUDA(cudaGetLastError());
+    return 0;
+}
+
+/* The wide engine (dg_wide.cuh) for a resume launch: kc.wide_max CTAs of 4
+ * warps (a multiple of the SM count), CTA b resuming the b-th set-aside
+ * cell; it returns at once unless at most kc.wide_max cells were set aside.
+ * NP and MIXED only fit the launchers' common form (4 warps, FP64). */
+template <class Net, int NP, bool MIXED>
+int launch_wide(Gpu *g, const CellIO &io, const TableSet &ts, const KernelCfg &kc, int schedule,
+                int grid, cudaStream_t st, unsigned long long *queue)
+{
+    static_assert(NP == 4 && !MIXED, "the wide engine is FP64 with 4 warps");
+    (void)g;
+    (void)schedule;
+    (void)grid;
+    if (io.ncells <= 0 || kc.wide_max <= 0) return 0;
+    evolve_wide_kernel<Net><<<kc.wide_max, 128, 0, st>>>(io, ts, kc, queue);
     DG_CUDA(cudaGetLastError());
     return 0;
 }
@@ -568,8 +587,10 @@ struct Api {
      * spread over those CTAs: a few stiff cells then share warps -- free on
      * the FP64 pipe -- instead of competing CTAs sharing each SM's FP64
      * units; launch 3 does the same for the cells launch 2 set aside at 16
-     * times the budget.  Every cell's operations are those of one launch,
-     * so the results are bit-identical to it. */
+     * times the budget.  FP64 (wide_tail): when at most wide_tail cells
+     * per SM were set aside, the wide engine resumes them instead, each on
+     * a CTA of its own.  Every cell's operations are those of one launch, so the
+     * results are bit-identical to it. */
     static int solve_redistributed(Gpu *g, CellIO io, const TableSet &ts, KernelCfg kc,
                                    dengo_solver_config cfg, cudaStream_t st)
     {
@@ -617,11 +638,18 @@ struct Api {
             k2.resume_count = g->resume_count;
             k2.nsm = g->nsm;
             k2.sweep_budget = budgets[r];
+            /* FP64: at most wide_tail set-aside cells per SM go to the
+             * wide engine, whose launch follows (the other launch then
+             * returns at once; the count is known only on the device) */
+            const bool wide = cfg.wide_tail > 0 && cfg.precision == DENGO_FP64;
+            k2.wide_max = wide ? g->nsm * (cfg.wide_tail < 8 ? cfg.wide_tail : 8) : 0;
             dengo_solver_config c2 = cfg;
             if (c2.schedule == DENGO_SCHED_PER_THREAD) c2.schedule = DENGO_SCHED_QUEUE;
             c2.grid = cfg.tail_grid;   /* 0: the persistent default; CTAs past the
                                           rounds the list needs exit */
             if (int e = launch_engine<Net>(g, io2, ts, k2, c2, st, g->queue)) return e;
+            if (wide)
+                if (int e = launch_wide<Net, 4, false>(g, io2, ts, k2, 0, 0, st, g->queue)) return e;
         }
         return 0;
     }
@@ -1288,6 +1316,8 @@ extern "C" inline void dg_default_config_impl(dengo_solver_config *cfg)
     /* mixed precision: FP64 re-solve of a converged cell whose invariants
      * drifted by more than this (relative) */
     cfg->conservation_tol = 1e-9;
+    /* FP64: up to three set-aside cells per SM on the wide engine */
+    cfg->wide_tail = 3;
 }
 
 #endif

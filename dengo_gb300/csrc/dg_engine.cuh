@@ -100,6 +100,11 @@ struct KernelCfg {
     /* mixed precision: build the Newton matrix in extended-range FP32
      * (DENGO_MIXED_XF) instead of from FP64 products */
     int jac_xf;
+    /* FP64 resume launch: when at most wide_max cells were set aside the
+     * wide engine (dg_wide.cuh, one cell per CTA, wide_max CTAs) resumes
+     * them and this engine's launch returns at once; 0: this engine resumes
+     * them */
+    int wide_max;
 };
 
 /* Suspension record of a cell at a substep boundary: state y, prev, scale,
@@ -427,8 +432,10 @@ evolve_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
     if (cfg.resume && cfg.resume_count) {
         /* one lane per set-aside cell: a cell left waiting for a lane would
          * start its remaining ~10^5 sweeps only when another finished */
+        const unsigned int cnt = *cfg.resume_count;
+        if (cfg.wide_max > 0 && cnt <= (unsigned int)cfg.wide_max) return; /* wide engine's */
         const long long per_round = (long long)cfg.nsm * BLOCK;
-        const long long rounds = ((long long)*cfg.resume_count + per_round - 1) / per_round;
+        const long long rounds = ((long long)cnt + per_round - 1) / per_round;
         if (blockIdx.x >= cfg.nsm * (rounds > 0 ? rounds : 1)) return;
     }
     /* the work queue hands each warp 32 consecutive cells to start with (cells

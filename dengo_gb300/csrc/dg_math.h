@@ -191,8 +191,12 @@ DG_HD bool dg_div_ok(double b)
  * fma, RN(q + r rb) = RN(a/b), provided no intermediate leaves the normal
  * range.  The exponent guard keeps |a|, |b| in [2^-873, 2^877] and their
  * ratio within 2^800, which keeps q and r normal; every other operand
- * (zero, subnormal, huge, inf, NaN) takes the plain division.  One reciprocal
- * then serves all quotients by the same divisor at 3 FP64 operations each. */
+ * (zero, subnormal, huge, inf, NaN) takes the plain division -- except a
+ * zero numerator over a nonzero finite b, whose quotient is the zero with
+ * the sign sign(a) xor sign(b) (IEEE 754), formed from the bits: structural
+ * zeros of the Jacobian reach this on every elimination step, and a plain
+ * division costs about nine FP64 operations.  One reciprocal then serves
+ * all quotients by the same divisor at 3 FP64 operations each. */
 DG_HD double dg_div(double a, double b, double rb)
 {
     const int ea = dg_expo(a), eb = dg_expo(b), d = ea - eb;
@@ -201,6 +205,19 @@ DG_HD double dg_div(double a, double b, double rb)
         const double r = dg_fma(-b, q, a);
         return dg_fma(r, rb, q);
     }
+    const uint64_t ba = dg_bits(a), bb = dg_bits(b);
+    if ((ba << 1) == 0 && (bb << 1) != 0 && eb != 0x7FF)
+        return dg_from_bits((ba ^ bb) & 0x8000000000000000ull);
+    return a / b;
+}
+
+/* a / b, correctly rounded, with dg_div's zero-numerator case taken from
+ * the bits: for a quotient whose divisor has no reciprocal at hand. */
+DG_HD double dg_quot(double a, double b)
+{
+    const uint64_t ba = dg_bits(a), bb = dg_bits(b);
+    if ((ba << 1) == 0 && (bb << 1) != 0 && dg_expo(b) != 0x7FF)
+        return dg_from_bits((ba ^ bb) & 0x8000000000000000ull);
     return a / b;
 }
 

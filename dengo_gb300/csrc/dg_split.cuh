@@ -110,8 +110,10 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
     if (cfg.resume && cfg.resume_count) {
         /* one lane per set-aside cell: a cell left waiting for a lane would
          * start its remaining ~10^5 sweeps only when another finished */
+        const unsigned int cnt = *cfg.resume_count;
+        if (cfg.wide_max > 0 && cnt <= (unsigned int)cfg.wide_max) return; /* wide engine's */
         const long long per_round = (long long)cfg.nsm * 32;
-        const long long rounds = ((long long)*cfg.resume_count + per_round - 1) / per_round;
+        const long long rounds = ((long long)cnt + per_round - 1) / per_round;
         if (blockIdx.x >= cfg.nsm * (rounds > 0 ? rounds : 1)) return;
     }
     if (w == 0) {

@@ -1,0 +1,441 @@
+/*
+ * Wide engine: one cell per CTA of 4 warps, for the last few stiff cells of
+ * a hydro step (FP64 path).
+ *
+ * The split engine (dg_split.cuh) gives each lane its own cell, which is
+ * what a full GPU wants; but after the first launches of a step only a few
+ * stiff cells are left, each needing 10^4-10^5 more sequential Newton
+ * sweeps, one per SM at most, and then a lone cell's sweep runs its
+ * elimination one row and one column after another on the 64-cycle FP64
+ * issue of its warps' sub-partitions (measured with an instrumented copy: of
+ * ~124k cycles per sweep, 44k in the LU row updates, 20k in the back
+ * substitution).  Here the cell's lanes share the work instead: the table
+ * interpolation, the residual, the Jacobian's scaling, each elimination
+ * step's multipliers and its (row, column) updates, the x update and the
+ * Newton update run one entry per lane, so each such FP64 warp instruction
+ * does up to 128 of the cell's operations.  The RHS rows and Jacobian
+ * entries are the same four generated parts as in the split engine (lane 0
+ * of warp w computes part w), the pivot search, the back substitution, the
+ * temperature and the substep control run on thread 0.
+ *
+ * Every value is computed with exactly the split engine's operations in the
+ * same order (the scaling of a Jacobian entry, the skip tests of the
+ * elimination, dg_div with the pivot's reciprocal), so the results are
+ * bit-identical to it and to the reference.  The kernel serves the resume
+ * launches of the stiff-cell redistribution when at most cfg.wide_max cells
+ * were set aside (one per SM); otherwise it returns at once and the split
+ * engine's launch does the work.
+ */
+#ifndef DG_WIDE_CUH
+#define DG_WIDE_CUH
+
+#include "dg_engine.cuh"
+
+namespace dg {
+
+/* Jacobian entries as the generated code produces them, before the scaling
+ * of BE_Resid_Jac (applied afterwards, one entry per lane): put() stores the
+ * value, zero() marks a structural zero. */
+template <int N>
+struct RawPut {
+    double *J;
+    int *Z;
+    __device__ __forceinline__ void operator()(int q, int v, double jv) const
+    {
+        J[v * N + q] = jv;
+        Z[v * N + q] = 0;
+    }
+    __device__ __forceinline__ void zero(int q, int v) const { Z[v * N + q] = 1; }
+};
+
+template <class Net>
+__global__ void __launch_bounds__(128)
+evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
+{
+    constexpr int N = Net::N;
+    constexpr int NT = Net::NT;
+    constexpr int NP = 4;
+    static_assert(N <= 32, "the wide engine gives each row of the system a lane of one warp");
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+    if (!cfg.resume || !cfg.resume_count || cfg.wide_max <= 0) return;
+    /* CTA b resumes the b-th set-aside cell: the launch has wide_max CTAs,
+     * at least one per cell, and the first wave spreads them over the SMs */
+    const unsigned int cnt = *cfg.resume_count;
+    if (cnt > (unsigned int)cfg.wide_max || blockIdx.x >= cnt || blockIdx.x >= io.ncells) return;
+    (void)queue;
+
+    /* J: the Newton matrix, J[j * N + i] = row i, column j; PP: the back
+     * substitution's products; MB, PRB: multipliers and row order, double
+     * buffered by step; Z: structural zeros of the Jacobian, then the
+     * back substitution's term flags */
+    __shared__ double J[N * N], PP[N * N], R[NT], Y[N], G[N], U[N], U0[N], SC[N], INV[N], AT[N],
+        RT[N], PREV[N], RPV[N], PV[N], XS[N], MB[2][N], S[6];
+    __shared__ int Z[N * N], FROW[N], PRB[2][N];
+    __shared__ int s_act, s_okr, s_okj, s_bin, s_dense;
+
+    /* thread-0 control state of the CTA's cell */
+    long long cell = 0;
+    double dtf = 0, dt = 0, ttot = 0;
+    int siter = 0, isweep = 0, nsweeps = 0, nfail = 0;
+    bool active = false, dense = false;
+
+    auto substep_begin = [&]() {
+        for (int i = 0; i < N; i++) {
+            const double v = Y[i] * INV[i];
+            U[i] = v;
+            U0[i] = v;
+            AT[i] = AT[i] * INV[i];
+        }
+        isweep = 0;
+    };
+    auto cell_begin = [&]() -> bool {
+        /* a set-aside cell, continued from its suspension record */
+        const double *rc = cfg.rec + cell * rec_len<N>();
+        dense = false;
+        for (int s = 0; s < N; s++) {
+            Y[s] = rc[s];
+            PREV[s] = rc[N + s];
+            SC[s] = rc[2 * N + s];
+            AT[s] = rc[3 * N + s];
+            RT[s] = io.rtol ? io.rtol[cell * io.cs + s * io.ss] : io.rtol_scalar;
+            INV[s] = 1.0 / SC[s];
+            dense = dense || !(SC[s] > 0.0 && dg_finite(SC[s]));
+        }
+        dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+        dt = rc[4 * N];
+        ttot = rc[4 * N + 1];
+        siter = (int)rc[4 * N + 2];
+        nsweeps = (int)rc[4 * N + 3];
+        nfail = (int)rc[4 * N + 4];
+        if (!(ttot < dtf)) return false;
+        substep_begin();
+        return true;
+    };
+    auto cell_end = [&](int status) {
+        for (int s = 0; s < N; s++) {
+            double v = Y[s], a = AT[s];
+            if (!Net::INPUT_IS_NUMBER && s != Net::IGE) {
+                v = v * Net::unit(s);
+                a = a * Net::unit(s);
+            }
+            const long long off = cell * io.cs + s * io.ss;
+            io.state[off] = v;
+            io.atol[off] = a;
+        }
+        if (io.dt) io.dt[cell] = dt;
+        if (io.ttot) io.ttot[cell] = ttot;
+        if (io.status) io.status[cell] = status;
+        if (io.substeps) io.substeps[cell] = siter;
+        if (io.sweeps) io.sweeps[cell] = nsweeps;
+        if (io.failures) io.failures[cell] = nfail;
+    };
+    auto suspend = [&]() {
+        double *rc = cfg.rec + cell * rec_len<N>();
+        for (int s = 0; s < N; s++) {
+            rc[s] = Y[s];
+            rc[N + s] = PREV[s];
+            rc[2 * N + s] = SC[s];
+            rc[3 * N + s] = AT[s];
+        }
+        rc[4 * N] = dt;
+        rc[4 * N + 1] = ttot;
+        rc[4 * N + 2] = siter;
+        rc[4 * N + 3] = nsweeps;
+        rc[4 * N + 4] = nfail;
+        rc[4 * N + 5] = 0.0;   /* the FP64 path: no conservation re-solve */
+        io.status[cell] = ST_SUSPENDED;
+    };
+    if (tid == 0) {
+        cell = (long long)io.order[blockIdx.x];
+        active = cell >= 0 && cell_begin();
+        if (cell >= 0 && !active) cell_end(ST_OK);
+        s_act = active;
+    }
+    __syncthreads();
+    while (s_act) {
+        /* ---- P0 (thread 0): unscale, temperature, bin ---- */
+        if (tid == 0) {
+            double y[N];
+            for (int i = 0; i < N; i++) {
+                y[i] = U[i] * SC[i];
+                Y[i] = y[i];
+            }
+            double T, Tge;
+            Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+            const double logT = dg_log(T);
+            const int bin = (int)(ts.idbin * (logT - ts.lb));
+            const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+            const double t1 = (ts.lb + (bin) * ts.dbin);
+            const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+            S[0] = T;
+            S[1] = Tge;
+            S[2] = (logT - t1) / (t2 - t1);
+            S[3] = -dt;
+            s_bin = bc;
+            s_dense = dense || !(dt > 0.0);
+            s_okr = 1;
+            s_okj = 1;
+        }
+        __syncthreads();
+        /* ---- P1: interpolation, one table per lane ---- */
+        for (int k = tid; k < NT; k += 128) {
+            if (Net::zdep(k)) {
+                R[k] = ts.zvals[k];
+            } else {
+                const double2 pr = __ldg(ts.pairs + (size_t)s_bin * NT + k);
+                R[k] = pr.x + S[2] * pr.y;
+            }
+        }
+        __syncthreads();
+        /* ---- P2: RHS rows of part w (lane 0 of warp w) ---- */
+        if (l == 0) {
+            double y[N], f[N];
+            for (int i = 0; i < N; i++) y[i] = Y[i];
+            const Slots<1> Rs{R};
+            bool ok = true;
+            switch (w) {
+            case 0: ok = Net::template rhs<NP, 0>(y, Rs, S[0], ts.z, f); break;
+            case 1: ok = Net::template rhs<NP, 1>(y, Rs, S[0], ts.z, f); break;
+            case 2: ok = Net::template rhs<NP, 2>(y, Rs, S[0], ts.z, f); break;
+            default: ok = Net::template rhs<NP, 3>(y, Rs, S[0], ts.z, f); break;
+            }
+            if (ok) {
+                for (int i = 0; i < N; i++)
+                    if (Net::rhs_row_part(NP, i) == w) G[i] = f[i];
+            } else {
+                atomicAnd(&s_okr, 0);
+            }
+        }
+        __syncthreads();
+        /* ---- P3: residual g = u - u0 - dt f (scaled), one row per lane ---- */
+        if (s_okr) for (int i = tid; i < N; i += 128) {
+            const double dtv = -S[3];
+            const double u = Y[i] * INV[i];
+            double g = G[i] * INV[i];
+            g = u - U0[i] - dtv * g;
+            G[i] = g;
+            U[i] = u;
+            Y[i] = u * SC[i];
+        }
+        __syncthreads();
+        /* ---- P4: Jacobian entries of part w (lane 0 of warp w), raw ---- */
+        const bool do_j = s_okr != 0;
+        if (do_j && l == 0) {
+            double y[N];
+            for (int i = 0; i < N; i++) y[i] = Y[i];
+            const Slots<1> Rs{R};
+            const RawPut<N> put{J, Z};
+            bool ok = true;
+            switch (w) {
+            case 0: ok = Net::template jac<NP, 0>(y, Rs, S[1], S[0], ts.z, put); break;
+            case 1: ok = Net::template jac<NP, 1>(y, Rs, S[1], S[0], ts.z, put); break;
+            case 2: ok = Net::template jac<NP, 2>(y, Rs, S[1], S[0], ts.z, put); break;
+            default: ok = Net::template jac<NP, 3>(y, Rs, S[1], S[0], ts.z, put); break;
+            }
+            if (!ok) atomicAnd(&s_okj, 0);
+        }
+        __syncthreads();
+        const bool do_lu = do_j && s_okj;
+        /* ---- P4b: BE_Resid_Jac's scaling, one entry per lane (JacPut's
+         *      operations), u = y / scale, the identity row order ---- */
+        if (do_lu) {
+            const double mdt = S[3];
+            for (int e = tid; e < N * N; e += 128) {
+                const int v = e / N, q = e - v * N;
+                if (Z[e] && !s_dense) {
+                    J[e] = (q == v) ? 1.0 : -0.0;
+                } else {
+                    double a = (Z[e] ? 0.0 : J[e]) * INV[q];
+                    a = a * SC[v];
+                    a = mdt * a;
+                    if (q == v) a = a + 1.0;
+                    J[e] = a;
+                }
+            }
+            for (int i = tid; i < N; i += 128) {
+                U[i] = Y[i] * INV[i];
+                PRB[0][i] = i;
+            }
+        }
+        /* ---- P5: Gauss_Elim with one barrier per elimination step.
+         * Column j belongs to warp j mod 4 throughout.  Step k: the owner of
+         * column k finds the pivot (a warp reduction that picks the first
+         * row of largest magnitude, as the serial scan), records the row
+         * interchange in the row order (the rows stay in place: logical row
+         * i is J row PR[i]) and forms the multipliers a_ik / pivot, one row
+         * per lane; after the barrier every warp updates its own columns,
+         * one (row, column) entry per lane, one warp the right-hand side,
+         * another the pivot's reciprocal for the back substitution.  The
+         * owner of column k+1 has just updated that column itself and goes
+         * on to step k+1 at once; the row order and the multipliers are
+         * double-buffered for the warps still in step k. ---- */
+        for (int k = 0; k < N - 1; k++) {
+            const int *PRo = PRB[k & 1];
+            int *PRn = PRB[(k + 1) & 1];
+            double *M = MB[k & 1];
+            if (do_lu && w == (k & 3)) {
+                const int i = l;
+                const bool cand = i >= k && i < N;
+                const int pri = i < N ? PRo[i] : 0;
+                const double a = cand ? J[k * N + pri] : 0.0;
+                const unsigned long long key = dg_bits(a) << 1;
+                const bool valid = cand && key <= DG_INF2;
+                const double ak = __shfl_sync(0xffffffffu, a, k);
+                const int prk = __shfl_sync(0xffffffffu, pri, k);
+                int p = k;
+                if ((dg_bits(ak) << 1) <= DG_INF2) {
+                    /* largest |a| among the finite candidates, first row on a tie */
+                    const unsigned int hi = valid ? (unsigned int)(key >> 32) : 0u;
+                    const unsigned int mhi = __reduce_max_sync(0xffffffffu, hi);
+                    const bool c1 = valid && hi == mhi;
+                    const unsigned int lo = c1 ? (unsigned int)key : 0u;
+                    const unsigned int mlo = __reduce_max_sync(0xffffffffu, lo);
+                    p = __ffs(__ballot_sync(0xffffffffu, c1 && (unsigned int)key == mlo)) - 1;
+                }
+                const double piv = __shfl_sync(0xffffffffu, a, p);
+                const int prp = __shfl_sync(0xffffffffu, pri, p);
+                /* logical row p now holds the old row k (and its a_kk) */
+                const int r = i == k ? prp : (i == p ? prk : pri);
+                if (i < N) PRn[i] = r;
+                if (i > k && i < N) {
+                    const double m = dg_quot(i == p ? ak : a, piv);
+                    J[k * N + r] = m;
+                    M[i] = m;
+                }
+                if (l == 0) PV[k] = piv;
+                __syncwarp();
+            }
+            __syncthreads();
+            if (do_lu) {
+                const int pk = PRn[k];
+                /* row k's entries right of the pivot all finite? */
+                bool fin = true;
+                for (int j = k + 1 + l; j < N; j += 32) fin = fin && dg_finite(J[j * N + pk]);
+                const bool rowfin = __all_sync(0xffffffffu, fin);
+                const int rows = N - 1 - k;
+                const int j0 = k + 1 + ((w - (k + 1)) & 3);
+                const int ncol = j0 < N ? (N - 1 - j0) / 4 + 1 : 0;
+                for (int e = l; e < ncol * rows; e += 32) {
+                    const int c = e / rows, i = k + 1 + (e - c * rows), j = j0 + 4 * c;
+                    const double m = M[i];
+                    if (dg_nonzero(m) || !rowfin) {
+                        const double akj = J[j * N + pk];
+                        if (dg_nonzero(akj) || !dg_finite(m)) {
+                            const int r = PRn[i];
+                            J[j * N + r] = J[j * N + r] - m * akj;
+                        }
+                    }
+                }
+                if (w == ((k + 2) & 3)) {
+                    const double xk = G[pk];
+                    for (int i = k + 1 + l; i < N; i += 32) {
+                        const double m = M[i];
+                        if (dg_nonzero(m) || !dg_finite(xk)) G[PRn[i]] = G[PRn[i]] - m * xk;
+                    }
+                }
+                if (w == ((k + 3) & 3) && l == 0) RPV[k] = 1.0 / PV[k];
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        /* ---- back substitution (warp 0, lane i = row i): x_j is formed by
+         * lane j from its row's products in increasing column order, then
+         * every row above forms its product with x_j at once ---- */
+        if (do_lu && w == 0) {
+            const int *PRf = PRB[(N - 1) & 1];
+            const int rl = l < N ? PRf[l] : 0;
+#pragma unroll
+            for (int j = N - 1; j >= 0; j--) {
+                if (l == j) {
+                    double acc = G[rl];
+#pragma unroll
+                    for (int t = j + 1; t < N; t++)
+                        if (Z[t * N + j]) acc = acc - PP[t * N + j];
+                    const double u = J[j * N + rl];
+                    XS[j] = j == N - 1 ? dg_quot(acc, u) : dg_div(acc, u, RPV[j]);
+                }
+                __syncwarp();
+                if (l < j) {
+                    const double xj = XS[j];
+                    const double a = J[j * N + rl];
+                    Z[j * N + l] = dg_nonzero(a) || !dg_finite(xj);
+                    PP[j * N + l] = a * xj;
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        /* ---- P6a: Newton update and each row's max-norm / NaN test ---- */
+        if (s_okr && s_okj) for (int i = tid; i < N; i += 128) {
+            const double u = U[i] - 1.0 * XS[i];
+            U[i] = u;
+            FROW[i] = dg_abs_gt_val(XS[i], AT[i] + RT[i] * fabs(u)) ? 1 : (dg_isnan(u) ? 2 : 0);
+        }
+        __syncthreads();
+        /* ---- P6b (thread 0): the first row that fails decides, as in the
+         *      reference's row loop; substep control ---- */
+        if (tid == 0) {
+            bool ok = s_okr && s_okj, unsolved = false, nan = false;
+            if (ok) {
+                for (int i = 0; i < N; i++) {
+                    const int r = FROW[i];
+                    if (r) {
+                        unsolved = r == 1;
+                        nan = r == 2;
+                        break;
+                    }
+                }
+            }
+            isweep++;
+            nsweeps++;
+            int rv = -1;
+            if (!ok || nan) rv = 1;
+            else if (!unsolved) rv = 0;
+            else if (isweep >= cfg.max_sweeps) rv = 1;
+            if (rv >= 0) {
+                double y[N];
+                for (int i = 0; i < N; i++) {
+                    y[i] = U[i] * SC[i];
+                    AT[i] = AT[i] * SC[i];
+                }
+                if (rv == 0)
+                    for (int i = 0; i < N; i++)
+                        if (dg_lt0(y[i])) rv = 1;
+                int done = -1;
+                if (rv == 0) {
+                    if (siter == cfg.max_substeps) {
+                        done = ST_MAX_SUBSTEPS;
+                    } else {
+                        siter++;
+                        ttot += dt;
+                        const double grown = dt * 1.1, rest = dtf - ttot;
+                        dt = grown < rest ? grown : rest;
+                        for (int i = 0; i < N; i++) {
+                            PREV[i] = y[i];
+                            if (dg_lt_pos(y[i], cfg.floor_value)) y[i] = cfg.floor_value;
+                        }
+                        if (!(ttot < dtf)) done = ST_OK;
+                    }
+                } else {
+                    nfail++;
+                    dt /= 2.0;
+                    for (int i = 0; i < N; i++) y[i] = PREV[i];
+                    if (dt / dtf < cfg.dt_ratio_floor) done = ST_DT_UNDERFLOW;
+                }
+                for (int i = 0; i < N; i++) Y[i] = y[i];
+                if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
+                    substep_begin();
+                } else {
+                    if (done < 0) suspend();
+                    else cell_end(done);
+                    active = false;
+                }
+            }
+            s_act = active;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dg
+#endif

@@ -32,7 +32,7 @@ class SolverConfig(C.Structure):
                 ("block", C.c_int), ("grid", C.c_int), ("warps_per_cell", C.c_int),
                 ("sweep_budget", C.c_int), ("tail_grid", C.c_int),
                 ("evolve_mode", C.c_int), ("write_intermediate", C.c_int),
-                ("conservation_tol", C.c_double)]
+                ("conservation_tol", C.c_double), ("wide_tail", C.c_int)]
 
 
 class CellBatch(C.Structure):
@@ -164,6 +164,7 @@ class Solver:
         cfg.sweep_budget, cfg.tail_grid = 2000, 0
         cfg.evolve_mode, cfg.write_intermediate = DENGO_EVOLVE_LOCKSTEP, -1
         cfg.conservation_tol = 1e-9
+        cfg.wide_tail = 3
         return cfg
 
     def set_config(self, config=None):

@@ -21,11 +21,14 @@ resume list built on the host.
 The split engine (dg_split.cuh, evolve_split_kernel: 32 cells per CTA, each
 cell's sweep shared by NP warps that meet at __syncthreads) is built the
 same way with ``engine="split"``, but its 32 x NP lanes run as that many host
-threads: ``__syncthreads`` is a barrier across them, ``__syncthreads_or``,
-``__ballot_sync`` and ``__shfl_sync`` (warp 0 only) reductions between
-barriers, and the atomics take a lock.  One CTA runs the whole batch from
-the work queue.  A build that hangs is cut off by the caller's timeout
-(``evolve_in_subprocess``).
+threads: ``__syncthreads`` is a barrier across them, ``__syncthreads_or`` a
+reduction between barriers, the warp collectives (``__shfl_sync``,
+``__ballot_sync``, ``__all_sync``, ``__reduce_max_sync``, ``__syncwarp``)
+barriers across the warp's 32 threads around a value each posts, and the
+atomics take a lock.  One CTA runs the whole batch from the work queue.  A build that hangs is cut off by the caller's timeout
+(``evolve_in_subprocess``).  ``engine="wide"`` adds the wide engine
+(dg_wide.cuh, one CTA of 128 threads per cell) and hands it every cell of
+the FP64 path's resume launches.
 """
 import ctypes as C
 import os
@@ -129,8 +132,21 @@ struct hx_barrier {
     std::atomic<int> left;
     std::atomic<unsigned> gen;
 };
-static hx_barrier *hx_cta;    /* all lanes of the CTA */
-static hx_barrier *hx_warp0;  /* the 32 lanes of warp 0 */
+static hx_barrier *hx_cta;      /* all lanes of the CTA */
+static hx_barrier *hx_warp[32];  /* the 32 lanes of each warp */
+/* A CTA of `threads` lanes (a multiple of 32): its barrier and one per warp. */
+static void hx_setup(int threads)
+{
+    static std::vector<hx_barrier *> keep;
+    for (hx_barrier *b : keep) delete b;
+    keep.clear();
+    hx_cta = new hx_barrier(threads);
+    keep.push_back(hx_cta);
+    for (int w = 0; w < (threads + 31) / 32; w++) {
+        hx_warp[w] = new hx_barrier(32);
+        keep.push_back(hx_warp[w]);
+    }
+}
 static inline void __syncthreads() { hx_cta->arrive_and_wait(); }
 static std::atomic<int> hx_or;
 static inline int __syncthreads_or(int p)
@@ -142,26 +158,45 @@ static inline int __syncthreads_or(int p)
     hx_cta->arrive_and_wait();
     return hx_or.load();
 }
-static std::atomic<unsigned> hx_ballot;
+/* Warp collectives, called by all 32 lanes of a warp: each lane posts its
+ * value, the warp meets, each reads what it needs, the warp meets again. */
+static unsigned long long hx_wbuf[32][32];
+static inline void __syncwarp(unsigned = 0xffffffffu) { hx_warp[threadIdx.x >> 5]->arrive_and_wait(); }
+static inline unsigned long long *hx_post(unsigned long long b)
+{
+    const int w = threadIdx.x >> 5;
+    hx_wbuf[w][threadIdx.x & 31] = b;
+    hx_warp[w]->arrive_and_wait();
+    return hx_wbuf[w];
+}
+template <class T> static inline T __shfl_sync(unsigned, T v, int src)
+{
+    unsigned long long b = 0;
+    memcpy(&b, &v, sizeof(T));
+    const unsigned long long r = hx_post(b)[src & 31];
+    __syncwarp();
+    T o;
+    memcpy(&o, &r, sizeof(T));
+    return o;
+}
 static inline unsigned __ballot_sync(unsigned, int p)
 {
-    hx_warp0->arrive_and_wait();
-    if (threadIdx.x == 0) hx_ballot = 0;
-    hx_warp0->arrive_and_wait();
-    if (p) hx_ballot |= 1u << (threadIdx.x & 31);
-    hx_warp0->arrive_and_wait();
-    return hx_ballot.load();
+    const unsigned long long *v = hx_post(p != 0);
+    unsigned m = 0;
+    for (int i = 0; i < 32; i++) m |= (unsigned)(v[i] != 0) << i;
+    __syncwarp();
+    return m;
 }
-static unsigned long long hx_shfl;
-static inline unsigned long long __shfl_sync(unsigned, unsigned long long v, int)
+static inline int __all_sync(unsigned, int p) { return __ballot_sync(~0u, p) == 0xffffffffu; }
+static inline unsigned __reduce_max_sync(unsigned, unsigned x)
 {
-    hx_warp0->arrive_and_wait();
-    if (threadIdx.x == 0) hx_shfl = v;
-    hx_warp0->arrive_and_wait();
-    const unsigned long long r = hx_shfl;
-    hx_warp0->arrive_and_wait();
-    return r;
+    const unsigned long long *v = hx_post(x);
+    unsigned m = 0;
+    for (int i = 0; i < 32; i++) m = (unsigned)v[i] > m ? (unsigned)v[i] : m;
+    __syncwarp();
+    return m;
 }
+static inline int __ffs(int x) { return __builtin_ffs(x); }
 template <class T> static inline T __ldg(const T *p) { return *p; }
 #define __launch_bounds__(...)
 #ifndef __noinline__
@@ -180,9 +215,7 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
     blockIdx.x = 0;
     gridDim.x = 1;
     blockDim.x = 32 * NP;
-    hx_barrier cta(32 * NP), warp0(32);
-    hx_cta = &cta;
-    hx_warp0 = &warp0;
+    hx_setup(32 * NP);
     std::vector<std::thread> lanes;
     for (unsigned t = 0; t < 32 * NP; t++)
         lanes.emplace_back([=]() {
@@ -190,6 +223,35 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
             dg::evolve_split_kernel<Net, NP, MIXED>(io, ts, cfg, queue);
         });
     for (auto &th : lanes) th.join();
+}
+'''
+
+DRIVER_WIDE_LAUNCH = DRIVER_SPLIT_LAUNCH.replace("static void launch(", "static void launch_split(") + r'''
+/* The split engine, and for the FP64 path's resume launches the wide engine
+ * (dg_wide.cuh, one CTA of 4 warps per cell) with every set-aside cell:
+ * the split engine's launch then returns at once. */
+template <bool MIXED>
+static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned long long *queue)
+{
+    const bool wide = !MIXED && cfg.resume;
+    if (wide) cfg.wide_max = 1 << 30;
+    launch_split<MIXED>(io, ts, cfg, queue);
+    if (!wide) return;
+    /* one CTA per set-aside cell, one after another */
+    const unsigned int count = *cfg.resume_count;
+    for (unsigned int b = 0; b < count; b++) {
+        blockIdx.x = b;
+        gridDim.x = count;
+        blockDim.x = 128;
+        hx_setup(128);
+        std::vector<std::thread> lanes;
+        for (unsigned t = 0; t < 128; t++)
+            lanes.emplace_back([=]() {
+                threadIdx.x = t;
+                dg::evolve_wide_kernel<Net>(io, ts, cfg, queue);
+            });
+        for (auto &th : lanes) th.join();
+    }
 }
 '''
 
@@ -245,9 +307,7 @@ extern "C" int hx_run_strip(double *input, const double *rtol, double *atol, int
     blockIdx.x = 0;
     gridDim.x = 1;
     blockDim.x = threads;
-    hx_barrier cta(threads), warp0(32);
-    hx_cta = &cta;
-    hx_warp0 = &warp0;
+    hx_setup(threads);
     std::vector<std::thread> lanes;
     for (int t = 0; t < threads; t++)
         lanes.emplace_back([=]() {
@@ -293,9 +353,7 @@ extern "C" int hx_evolve_lockstep(double *input, const double *rtol, double *ato
         blockIdx.x = 0;
         gridDim.x = 1;
         blockDim.x = threads;
-        hx_barrier cta(threads), warp0(32);
-        hx_cta = &cta;
-        hx_warp0 = &warp0;
+        hx_setup(threads);
         std::vector<std::thread> lanes;
         for (int t = 0; t < threads; t++)
             lanes.emplace_back([=]() {
@@ -430,7 +488,7 @@ def _cut_net(name):
 
 
 def build(name, out_dir, strict=True, engine="lane"):
-    """Compile the host engine (``engine`` "lane" or "split") for network
+    """Compile the host engine (``engine`` "lane", "split" or "wide") for network
     ``name`` into ``out_dir``; returns the ctypes library."""
     lib = C.CDLL(compile_engine(name, out_dir, strict, engine))
     return _bind(lib)
@@ -440,15 +498,20 @@ def compile_engine(name, out_dir, strict=True, engine="lane"):
     from dengo_gb300.build import network_dir
     tag = "%s_%s%s" % (name, engine, "" if strict else "_lenient")
     src = os.path.join(str(out_dir), "hx_%s.cpp" % tag)
-    if engine in ("split", "strip"):
-        # The kernel's block-shared scalars (``__shared__ int s_any;``) become
-        # statics: one CTA runs at a time, and its lanes are threads that
-        # must see one copy.  (The dynamic array is dg::dg_smem above.)
-        with open(os.path.join(CSRC, "dg_%s.cuh" % engine)) as f:
-            kernel_source = re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
+    if engine in ("split", "strip", "wide"):
+        # The kernel's block-shared scalars and arrays (``__shared__ int
+        # s_any;``) become statics: one CTA runs at a time, and its lanes are
+        # threads that must see one copy.  (The dynamic array is dg::dg_smem
+        # above.)  The wide engine comes with the split engine, which makes
+        # the first launch.
+        kernel_source = ""
+        for part in (["split", "wide"] if engine == "wide" else [engine]):
+            with open(os.path.join(CSRC, "dg_%s.cuh" % part)) as f:
+                kernel_source += re.sub(r"(?<!extern )__shared__ ", "static ", f.read())
         prelude = PRELUDE_SPLIT.replace("%(kernel_source)s", kernel_source)
+        launch = DRIVER_WIDE_LAUNCH if engine == "wide" else DRIVER_SPLIT_LAUNCH
         driver = (DRIVER_STRIP % dict(name=name) if engine == "strip" else
-                  DRIVER % dict(name=name, launch=DRIVER_SPLIT_LAUNCH, z_values=_cut_z_values()))
+                  DRIVER % dict(name=name, launch=launch, z_values=_cut_z_values()))
     else:
         prelude, driver = PRELUDE, DRIVER % dict(name=name, launch=DRIVER_LANE_LAUNCH,
                                                  z_values=_cut_z_values())

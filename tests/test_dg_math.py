@@ -22,10 +22,12 @@ extern "C" double h_pow2(double x) { return dg_ipow<2>(x); }
 extern "C" double h_pow3(double x) { return dg_ipow<3>(x); }
 extern "C" double h_pow4(double x) { return dg_ipow<4>(x); }
 extern "C" double h_glibc_log(double x) { return log(x); }
-/* dg_div(a, b, 1/b) against a / b on random bit patterns: a and b with
+/* dg_div(a, b, 1/b) and dg_quot(a, b) against a / b on random bit patterns: a and b with
  * uniformly random sign, exponent field and mantissa (every class of value),
- * and on pairs whose exponents straddle the guarded range's edges.  Returns
- * the number of results whose bits differ (NaNs compare equal). */
+ * on pairs whose exponents straddle the guarded range's edges, and on signed
+ * zero numerators over every class of b (zero, subnormal, normal, inf,
+ * NaN).  Returns the number of results whose bits differ (NaNs compare
+ * equal). */
 extern "C" long long h_div_mismatch(long long n, unsigned long long seed) {
     long long bad = 0;
     for (long long i = 0; i < n; i++) {
@@ -39,15 +41,24 @@ extern "C" long long h_div_mismatch(long long n, unsigned long long seed) {
             const int ka = (int)((seed >> 3) % 9), kb = (int)((seed >> 9) % 9);
             ba = (ba & 0x800fffffffffffffull) | ((unsigned long long)ea[ka] << 52);
             bb = (bb & 0x800fffffffffffffull) | ((unsigned long long)eb[kb] << 52);
+        } else if ((i & 3) == 2) {   /* +-0 over b of every class */
+            static const int eb[] = {0, 0, 1, 150, 1023, 2046, 2047, 2047};
+            const int kb = (int)((seed >> 5) % 8);
+            ba &= 0x8000000000000000ull;
+            bb = (bb & 0x800fffffffffffffull) | ((unsigned long long)eb[kb] << 52);
+            if (kb == 0) bb &= 0x8000000000000000ull;            /* b = +-0 */
+            if (kb == 6) bb &= 0x8000000000000000ull | (0x7ffull << 52);   /* b = +-inf */
         }
         double a, b;
         memcpy(&a, &ba, 8);
         memcpy(&b, &bb, 8);
-        const double q = dg_div(a, b, 1.0 / b), r = a / b;
-        uint64_t bq, br;
+        const double q = dg_div(a, b, 1.0 / b), r = a / b, q2 = dg_quot(a, b);
+        uint64_t bq, br, bq2;
         memcpy(&bq, &q, 8);
         memcpy(&br, &r, 8);
+        memcpy(&bq2, &q2, 8);
         bad += !(bq == br || (q != q && r != r));
+        bad += !(bq2 == br || (q2 != q2 && r != r));
     }
     return bad;
 }

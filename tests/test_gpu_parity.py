@@ -337,6 +337,37 @@ def test_temperature_from_mass_density(solver, golden):
     assert np.all(T >= 1.0) and np.all(np.isfinite(T))
 
 
+@pytest.mark.parametrize("config,n", [("config2", 128), ("top", 96), ("config3", 160),
+                                      ("config2", 640)])
+def test_wide_tail_is_bit_identical(solver, crlog_oracle, config, n):
+    """FP64 resume launches with at most one (wide_tail 1) or three (3, the
+    default) set-aside cells per SM run on the wide engine (one CTA of 4
+    warps per cell); the results equal those of the split engine
+    (wide_tail 0) bit for bit, and the oracle's within the FP64 bar.  The
+    640-cell case sets aside more cells than SMs: wide_tail 1 leaves them to
+    the split engine, the default puts up to three on each SM."""
+    from dengo_gb300.runtime import Solver
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(n, config, seed=31)
+    outs = []
+    for wide in (0, 1, 3):
+        cfg = Solver.default_config()
+        cfg.wide_tail = wide
+        outs.append(solver.solve_host(state, dtf, rtol=1e-6, config=cfg, counters=True))
+    stiff = int(np.sum(outs[0]["sweeps"] > cfg.sweep_budget))
+    assert 0 < stiff <= 3 * 152, stiff
+    for o in outs[1:]:
+        for k in ("state", "atol", "dt", "ttot", "status", "substeps", "sweeps", "failures"):
+            assert np.array_equal(o[k].view(np.uint8), outs[0][k].view(np.uint8)), k
+    print("%s: %d set-aside cells, split %.1f ms, wide (1/SM) %.1f ms, wide (3/SM) %.1f ms" %
+          (config, stiff, outs[0]["solve_ms"], outs[1]["solve_ms"], outs[2]["solve_ms"]))
+    ref = crlog_oracle.evolve_cells(solver._tables, state, dtf, nthreads=0)
+    check_cells(outs[1]["state"], ref["state"], outs[1]["status"], ref["status"], config)
+    ok = ref["status"] == 0
+    for k in ("substeps", "sweeps"):
+        assert np.array_equal(outs[1][k][ok], ref[k][ok]), k
+
+
 @pytest.mark.parametrize("wpc,precision", [(4, 0), (1, 0), (4, 1)])
 def test_sweep_budget_redistribution_is_bit_identical(solver, golden, wpc, precision):
     """Stiff-cell redistribution (cells set aside at a sweep budget, resumed
