@@ -78,6 +78,9 @@ class NetworkSpec:
     # conserve (left null space of the stoichiometry), one list of N
     # coefficients per invariant (0 for ge)
     conservation: list = field(default_factory=list)
+    # T(ge) in lane-parallel parts (temperature_lanes), or None when the
+    # printed expressions are not of that form
+    t_lanes: object = None
 
     @property
     def N(self):
@@ -114,6 +117,46 @@ _GAMMA_DIV = re.compile(r"\b([A-Za-z_][A-Za-z0-9_]*)/\(gamma - 1\.0\)")
 def gamma_div(text):
     """Rewrite ``x/(gamma - 1.0)`` as ``dg_div(x, gm1, rgm1)`` (same value)."""
     return _GAMMA_DIV.sub(r"dg_div(\1, gm1, rgm1)", text)
+
+
+_DTERM = re.compile(r"^(?:(\d+\.\d*(?:e[+-]?\d+)?)\*)?([A-Za-z_][A-Za-z0-9_]*)$")
+
+
+def temperature_lanes(species, mass_density, T_div, Tge_div):
+    """The temperature as lane-parallel parts: ``{"density": [(species
+    index, weight literal), ...], "quot": [species index, ...]}`` when the
+    printed expressions are ``density = w_0*y_a + w_1*y_b + ...`` and
+    ``T = density*ge*mh/(kb*(dg_div(y_c, gm1, rgm1) + ...))`` (``Tge`` the
+    same without ``*ge``), each sum in the order listed; else None.  Every
+    term is one product or one quotient and the sums run left to right, so
+    terms formed on separate lanes and summed in that order give the
+    printed expressions' values bit for bit."""
+    index = {sp.name: sp.index for sp in species}
+    dens = []
+    for term in mass_density.split(" + "):
+        m = _DTERM.match(term.strip())
+        if not m or m.group(2) not in index:
+            return None
+        dens.append((index[m.group(2)], m.group(1) or "1.0"))
+    quot = []
+    inner = None
+    for pre in ("density*ge*mh/(kb*(", "density*mh/(kb*("):
+        text = T_div if "ge*" in pre else Tge_div
+        if not (text.startswith(pre) and text.endswith("))")):
+            return None
+        body = text[len(pre):-2]
+        if inner is None:
+            inner = body
+        elif body != inner:
+            return None
+    for term in inner.split(" + "):
+        m = re.match(r"^dg_div\(([A-Za-z_][A-Za-z0-9_]*), gm1, rgm1\)$", term.strip())
+        if not m or m.group(1) not in index:
+            return None
+        quot.append(index[m.group(1)])
+    if not dens or not quot or len(dens) > 32 or len(quot) > 32:
+        return None
+    return {"density": dens, "quot": quot}
 
 
 def balance(costs, nparts):
@@ -226,6 +269,8 @@ def network_spec(net, name):
         T_ref=ccode_ref(T), T_dev=ccode_device(T),
         Tge_ref=ccode_ref(Tg), Tge_dev=ccode_device(Tg),
         T_dev_div=gamma_div(ccode_device(T)), Tge_dev_div=gamma_div(ccode_device(Tg)),
+        t_lanes=temperature_lanes(species, ccode_device(md), gamma_div(ccode_device(T)),
+                                  gamma_div(ccode_device(Tg))),
         rhs_ref=rhs_ref, rhs_dev=rhs_dev,
         jac_ref=jac_ref, jac_dev=jac_dev, jac_dev32=jac_dev32, jac_nonzero=jac_nz,
         rhs_part=rhs_part, jac_part=jac_part)

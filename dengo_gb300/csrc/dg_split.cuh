@@ -11,9 +11,13 @@
  * instruction still serves 32 cells.
  *
  * Work split of one sweep (barriers between phases):
- *   warp 0        substep bookkeeping, T(ge), log T, bin; pivot search and
- *                 row swap; back substitution; the convergence decision;
- *                 cell refill (work queue)
+ *   warp 0        substep bookkeeping; the convergence decision; cell refill
+ *                 (work queue)
+ *   warp 1 % NP   T(ge), log T, bin
+ *   warp 2 % NP   pivot search and row swap (FP64 elimination); mixed: the
+ *                 FP32 factorisation and first solve
+ *   warp 3 % NP   back substitution (FP64 elimination); mixed: the
+ *                 refinement's FP32 corrections
  *   all warps     table interpolation (tables k = w mod NP), RHS rows and
  *                 Jacobian entries of part w (generated partition balanced by
  *                 operation count); for rows i = w mod NP: the residual, the
@@ -87,6 +91,13 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
     constexpr int N = Net::N;
     extern __shared__ double dg_smem[];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    /* The per-cell serial phases go to different warps -- each warp of a
+     * CTA runs on its own SM sub-partition, so with several CTAs per SM no
+     * sub-partition's FP64 unit carries all of them: the control (warp 0),
+     * T(ge) and log T (W_T), the pivot search or the mixed path's FP32
+     * factorisation (W_PIV), the back substitution or the refinement's
+     * corrections (W_BS). */
+    constexpr int W_T = 1 % NP, W_PIV = 2 % NP, W_BS = 3 % NP;
     double *cellbase = dg_smem + l;
     const Slots<32> J{cellbase + L::J * 32}, R{cellbase + L::R * 32}, Y{cellbase + L::Y * 32},
         G{cellbase + L::G * 32}, U{cellbase + L::U * 32}, U0{cellbase + L::U0 * 32},
@@ -245,33 +256,37 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
         fetch();
         F(F_ACT) = active;
     }
+    __syncthreads();   /* the first cells' state, read by warp W_T */
     for (;;) {
-        /* ---- P0 (warp 0): unscale, temperature, bin ---- */
+        /* ---- P0: the control warp publishes -dt; warp W_T unscales the
+         *      state and forms T(ge), log T and the bin ---- */
         if (w == 0) {
             const unsigned anyact = __ballot_sync(0xffffffffu, active);
             if (l == 0) s_any = anyact != 0;
             if (active) {
-                double y[N];
-                for (int i = 0; i < N; i++) {
-                    y[i] = U[i] * SC[i];
-                    Y[i] = y[i];
-                }
-                double T, Tge;
-                Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
-                const double logT = dg_log(T);
-                const int bin = (int)(ts.idbin * (logT - ts.lb));
-                const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
-                const double t1 = (ts.lb + (bin) * ts.dbin);
-                const double t2 = (ts.lb + (bin + 1) * ts.dbin);
-                S[0] = T;
-                S[1] = Tge;
-                S[2] = (logT - t1) / (t2 - t1);
                 S[3] = -dt;
-                F(F_BIN) = bc;
                 F(F_DENSE) = dense || !(dt > 0.0);
             }
             F(F_OKR) = 1;
             F(F_OKJ) = 1;
+        }
+        if (w == W_T && F(F_ACT)) {
+            double y[N];
+            for (int i = 0; i < N; i++) {
+                y[i] = U[i] * SC[i];
+                Y[i] = y[i];
+            }
+            double T, Tge;
+            Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+            const double logT = dg_log(T);
+            const int bin = (int)(ts.idbin * (logT - ts.lb));
+            const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+            const double t1 = (ts.lb + (bin) * ts.dbin);
+            const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+            S[0] = T;
+            S[1] = Tge;
+            S[2] = (logT - t1) / (t2 - t1);
+            F(F_BIN) = bc;
         }
         __syncthreads();
         if (!s_any) break;
@@ -407,9 +422,9 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                 }
             }
             __syncthreads();
-            /* M3 (warp 0): FP32 factorisation and first solve; the FP64
-             * elimination for a dense or non-finite system */
-            if (w == 0 && do_lu) {
+            /* M3 (warp W_PIV): FP32 factorisation and first solve; the
+             * FP64 elimination for a dense or non-finite system */
+            if (w == W_PIV && do_lu) {
                 double g[N], x[N];
                 int sx[N], tx[N], px[N];
                 bool ok = eq;
@@ -450,7 +465,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                         if (i % NP == w) Y[i] = ms.residual_row(i, G[i], X);
                 }
                 __syncthreads();
-                if (w == 0 && refining) {
+                if (w == W_BS && refining) {
                     double r[N], x[N];
                     int sx[N], tx[N], px[N];
                     for (int i = 0; i < N; i++) {
@@ -476,17 +491,17 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
             }
 #if DG_MIXED_STRICT
             /* refinement stopped short of 2^-40 (3) or ran out of steps (1) */
-            if (w == 0 && do_lu && (F(F_MIX) == 1 || F(F_MIX) == 3)) {
+            if (w == W_BS && do_lu && (F(F_MIX) == 1 || F(F_MIX) == 3)) {
                 fp64_fallback<N>(J, G);
                 F(F_MIX) = 0;
             }
 #endif
-            if (w == 0 && do_lu && F(F_MIX) != 0)
+            if (w == W_BS && do_lu && F(F_MIX) != 0)
                 for (int i = 0; i < N; i++) G[i] = X[i];
         } else {
             for (int k = 0; k < N - 1; k++) {
                 __syncthreads();
-                if (w == 0 && do_lu) {
+                if (w == W_PIV && do_lu) {
                     int p = k;
                     double best = J[k * N + k];
                     for (int i = k + 1; i < N; i++) {
@@ -534,7 +549,7 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
                 }
             }
             __syncthreads();
-            if (w == 0 && do_lu) {
+            if (w == W_BS && do_lu) {
                 /* back substitution; the pivots are the final diagonal and
                  * their reciprocals were formed during the elimination */
                 RPV[N - 1] = 1.0 / J[(N - 1) * N + (N - 1)];

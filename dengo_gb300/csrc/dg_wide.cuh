@@ -69,7 +69,7 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
      * buffered by step; Z: structural zeros of the Jacobian, then the
      * back substitution's term flags */
     __shared__ double J[N * N], PP[N * N], R[NT], Y[N], G[N], U[N], U0[N], SC[N], INV[N], AT[N],
-        RT[N], PREV[N], RPV[N], PV[N], XS[N], MB[2][N], S[6];
+        RT[N], PREV[N], RPV[N], PV[N], XS[N], MB[2][N], S[6], TD[Net::T_ND], TQ[Net::T_NQ], TS[2];
     __shared__ int Z[N * N], FROW[N], PRB[2][N];
     __shared__ int s_act, s_okr, s_okj, s_bin, s_dense;
 
@@ -153,30 +153,78 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
     }
     __syncthreads();
     while (s_act) {
-        /* ---- P0 (thread 0): unscale, temperature, bin ---- */
-        if (tid == 0) {
-            double y[N];
-            for (int i = 0; i < N; i++) {
-                y[i] = U[i] * SC[i];
-                Y[i] = y[i];
+        if (Net::T_LANES) {
+            /* ---- P0a: the unscaled state (warp 0) and the temperature's
+             *      terms, products on warp 0, quotients on warp 1 ---- */
+            if (w == 0) {
+                for (int i = l; i < N; i += 32) Y[i] = U[i] * SC[i];
+                if (l < Net::T_ND) {
+                    const int sp = Net::t_dsp(l);
+                    TD[l] = Net::t_dw(l) * (U[sp] * SC[sp]);
+                }
+                if (l == 0) {
+                    S[3] = -dt;
+                    s_dense = dense || !(dt > 0.0);
+                    s_okr = 1;
+                    s_okj = 1;
+                }
+            } else if (w == 1 && l < Net::T_NQ) {
+                const int sp = Net::t_qsp(l);
+                TQ[l] = Net::t_quot(U[sp] * SC[sp]);
             }
-            double T, Tge;
-            Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
-            const double logT = dg_log(T);
-            const int bin = (int)(ts.idbin * (logT - ts.lb));
-            const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
-            const double t1 = (ts.lb + (bin) * ts.dbin);
-            const double t2 = (ts.lb + (bin + 1) * ts.dbin);
-            S[0] = T;
-            S[1] = Tge;
-            S[2] = (logT - t1) / (t2 - t1);
-            S[3] = -dt;
-            s_bin = bc;
-            s_dense = dense || !(dt > 0.0);
-            s_okr = 1;
-            s_okj = 1;
+            __syncthreads();
+            /* ---- P0b: the two sums, in the printed order ---- */
+            if (tid == 0) {
+                double d = TD[0];
+                for (int k = 1; k < Net::T_ND; k++) d = d + TD[k];
+                TS[0] = d;
+            } else if (tid == 32) {
+                double q = TQ[0];
+                for (int k = 1; k < Net::T_NQ; k++) q = q + TQ[k];
+                TS[1] = q;
+            }
+            __syncthreads();
+            /* ---- P0c: T, log T, bin (thread 0); Tge (warp 1) ---- */
+            if (tid == 0) {
+                const double T = Net::t_finish(TS[0], TS[1], Y[Net::IGE], ts.Tlo, ts.Thi);
+                const double logT = dg_log(T);
+                const int bin = (int)(ts.idbin * (logT - ts.lb));
+                const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+                const double t1 = (ts.lb + (bin) * ts.dbin);
+                const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+                S[0] = T;
+                S[2] = (logT - t1) / (t2 - t1);
+                s_bin = bc;
+            } else if (tid == 32) {
+                S[1] = Net::tge_finish(TS[0], TS[1]);
+            }
+            __syncthreads();
+        } else {
+            /* ---- P0 (thread 0): unscale, temperature, bin ---- */
+            if (tid == 0) {
+                double y[N];
+                for (int i = 0; i < N; i++) {
+                    y[i] = U[i] * SC[i];
+                    Y[i] = y[i];
+                }
+                double T, Tge;
+                Net::temperature(y, ts.Tlo, ts.Thi, T, Tge);
+                const double logT = dg_log(T);
+                const int bin = (int)(ts.idbin * (logT - ts.lb));
+                const int bc = bin <= 0 ? 0 : (bin >= ts.nbins ? ts.nbins - 1 : bin);
+                const double t1 = (ts.lb + (bin) * ts.dbin);
+                const double t2 = (ts.lb + (bin + 1) * ts.dbin);
+                S[0] = T;
+                S[1] = Tge;
+                S[2] = (logT - t1) / (t2 - t1);
+                S[3] = -dt;
+                s_bin = bc;
+                s_dense = dense || !(dt > 0.0);
+                s_okr = 1;
+                s_okj = 1;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         /* ---- P1: interpolation, one table per lane ---- */
         for (int k = tid; k < NT; k += 128) {
             if (Net::zdep(k)) {

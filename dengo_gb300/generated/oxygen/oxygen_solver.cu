@@ -262,6 +262,52 @@ struct Net {
         Tge = density*mh/(kb*(dg_div(H_1, gm1, rgm1) + dg_div(H_2, gm1, rgm1) + dg_div(He_1, gm1, rgm1) + dg_div(He_2, gm1, rgm1) + dg_div(He_3, gm1, rgm1) + dg_div(O_1, gm1, rgm1) + dg_div(O_2, gm1, rgm1) + dg_div(O_3, gm1, rgm1) + dg_div(O_4, gm1, rgm1) + dg_div(O_5, gm1, rgm1) + dg_div(O_6, gm1, rgm1) + dg_div(O_7, gm1, rgm1) + dg_div(O_8, gm1, rgm1) + dg_div(O_9, gm1, rgm1) + dg_div(de, gm1, rgm1)));
     }
 
+    /* temperature() in lane-parallel parts (the wide engine): density term
+     * k is t_dw(k) * y[t_dsp(k)], quotient term k is t_quot(y[t_qsp(k)]);
+     * the sums taken in k order, t_finish and tge_finish give temperature()'s
+     * T and Tge bit for bit (the same products, quotients and left-to-right
+     * sums).  T_LANES false: the printed expressions have another form. */
+    static constexpr bool T_LANES = true;
+    static constexpr int T_ND = 14, T_NQ = 15;
+    __host__ __device__ static constexpr int t_dsp(int k)
+    {
+        return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 4 : k == 5 ? 5 : k == 6 ? 6 : k == 7 ? 7 : k == 8 ? 8 : k == 9 ? 9 : k == 10 ? 10 : k == 11 ? 11 : k == 12 ? 12 : k == 13 ? 13 : 0;
+    }
+    __host__ __device__ static constexpr double t_dw(int k)
+    {
+        return k == 0 ? 1.0079400000000001 : k == 1 ? 1.0079400000000001 : k == 2 ? 4.0026020000000004 : k == 3 ? 4.0026020000000004 : k == 4 ? 4.0026020000000004 : k == 5 ? 15.9994 : k == 6 ? 15.9994 : k == 7 ? 15.9994 : k == 8 ? 15.9994 : k == 9 ? 15.9994 : k == 10 ? 15.9994 : k == 11 ? 15.9994 : k == 12 ? 15.9994 : k == 13 ? 15.9994 : 0.0;
+    }
+    __host__ __device__ static constexpr int t_qsp(int k)
+    {
+        return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 4 : k == 5 ? 5 : k == 6 ? 6 : k == 7 ? 7 : k == 8 ? 8 : k == 9 ? 9 : k == 10 ? 10 : k == 11 ? 11 : k == 12 ? 12 : k == 13 ? 13 : k == 14 ? 14 : 0;
+    }
+    __device__ __forceinline__ static double t_quot(double x)
+    {
+        const double gamma = 5.e0/3.e0;
+        const double gm1 = gamma - 1.0;
+        const double rgm1 = 1.0 / gm1;
+        return dg_div(x, gm1, rgm1);
+    }
+    __device__ __forceinline__ static double t_finish(double density, double den, double ge,
+                                                      double Tlo, double Thi)
+    {
+        const double kb = 1.3806504e-16;
+        const double mh = 1.67e-24;
+        double Tv = density*ge*mh/(kb*den);
+        if (Tv < Tlo) {
+            Tv = Tlo;
+        } else if (Tv > Thi) {
+            Tv = Thi;
+        }
+        return Tv;
+    }
+    __device__ __forceinline__ static double tge_finish(double density, double den)
+    {
+        const double kb = 1.3806504e-16;
+        const double mh = 1.67e-24;
+        return density*mh/(kb*den);
+    }
+
     /* rates_and_rate_tables.C.template:635-668 */
     __device__ __forceinline__ static double temperature_from_mass_density(const double (&yin)[N])
     {
