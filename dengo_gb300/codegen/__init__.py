@@ -36,11 +36,10 @@ def _env():
 
 
 # The engine kernels one network library holds, one translation unit each in
-# the package build: (launcher, BLOCK or warps per cell, mixed precision);
-# the wide engine (one cell per CTA of 4 warps) is FP64 only.
+# the package build: (launcher, BLOCK or warps per cell, mixed precision).
 ENGINE_VARIANTS = [("launch_lane", b, m) for b in (32, 64, 128) for m in ("false", "true")] + \
                   [("launch_split", w, m) for w in (2, 4) for m in ("false", "true")] + \
-                  [("launch_wide", 4, "false")]
+                  [("launch_wide", 4, m) for m in ("false", "true")]
 
 
 def render_solver(net, name, output_dir, family="rates_and_rate_tables"):

@@ -280,17 +280,17 @@ int launch_split(Gpu *g, const CellIO &io, const TableSet &ts, const KernelCfg &
 /* The wide engine (dg_wide.cuh) for a resume launch: kc.wide_max CTAs of 4
  * warps (a multiple of the SM count), CTA b resuming the b-th set-aside
  * cell; it returns at once unless at most kc.wide_max cells were set aside.
- * NP and MIXED only fit the launchers' common form (4 warps, FP64). */
+ * NP only fits the launchers' common form (4 warps). */
 template <class Net, int NP, bool MIXED>
 int launch_wide(Gpu *g, const CellIO &io, const TableSet &ts, const KernelCfg &kc, int schedule,
                 int grid, cudaStream_t st, unsigned long long *queue)
 {
-    static_assert(NP == 4 && !MIXED, "the wide engine is FP64 with 4 warps");
+    static_assert(NP == 4, "the wide engine has 4 warps");
     (void)g;
     (void)schedule;
     (void)grid;
     if (io.ncells <= 0 || kc.wide_max <= 0) return 0;
-    evolve_wide_kernel<Net><<<kc.wide_max, 128, 0, st>>>(io, ts, kc, queue);
+    evolve_wide_kernel<Net, MIXED><<<kc.wide_max, 128, 0, st>>>(io, ts, kc, queue);
     DG_CUDA(cudaGetLastError());
     return 0;
 }
@@ -587,9 +587,9 @@ struct Api {
      * spread over those CTAs: a few stiff cells then share warps -- free on
      * the FP64 pipe -- instead of competing CTAs sharing each SM's FP64
      * units; launch 3 does the same for the cells launch 2 set aside at 16
-     * times the budget.  FP64 (wide_tail): when at most wide_tail cells
-     * per SM were set aside, the wide engine resumes them instead, each on
-     * a CTA of its own.  Every cell's operations are those of one launch, so the
+     * times the budget.  wide_tail: when at most wide_tail cells per SM
+     * were set aside, the wide engine resumes them instead, each on a CTA
+     * of its own.  Every cell's operations are those of one launch, so the
      * results are bit-identical to it. */
     static int solve_redistributed(Gpu *g, CellIO io, const TableSet &ts, KernelCfg kc,
                                    dengo_solver_config cfg, cudaStream_t st)
@@ -638,18 +638,23 @@ struct Api {
             k2.resume_count = g->resume_count;
             k2.nsm = g->nsm;
             k2.sweep_budget = budgets[r];
-            /* FP64: at most wide_tail set-aside cells per SM go to the
-             * wide engine, whose launch follows (the other launch then
-             * returns at once; the count is known only on the device) */
-            const bool wide = cfg.wide_tail > 0 && cfg.precision == DENGO_FP64;
+            /* at most wide_tail set-aside cells per SM go to the wide
+             * engine, whose launch follows (the other launch then returns at
+             * once; the count is known only on the device); not for the
+             * Newton matrix in extended-range FP32 */
+            const bool wide = cfg.wide_tail > 0 && cfg.precision != DENGO_MIXED_XF;
             k2.wide_max = wide ? g->nsm * (cfg.wide_tail < 8 ? cfg.wide_tail : 8) : 0;
             dengo_solver_config c2 = cfg;
             if (c2.schedule == DENGO_SCHED_PER_THREAD) c2.schedule = DENGO_SCHED_QUEUE;
             c2.grid = cfg.tail_grid;   /* 0: the persistent default; CTAs past the
                                           rounds the list needs exit */
             if (int e = launch_engine<Net>(g, io2, ts, k2, c2, st, g->queue)) return e;
-            if (wide)
-                if (int e = launch_wide<Net, 4, false>(g, io2, ts, k2, 0, 0, st, g->queue)) return e;
+            if (wide) {
+                const int e = cfg.precision == DENGO_MIXED
+                                  ? launch_wide<Net, 4, true>(g, io2, ts, k2, 0, 0, st, g->queue)
+                                  : launch_wide<Net, 4, false>(g, io2, ts, k2, 0, 0, st, g->queue);
+                if (e) return e;
+            }
         }
         return 0;
     }

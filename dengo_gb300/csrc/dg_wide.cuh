@@ -1,6 +1,6 @@
 /*
  * Wide engine: one cell per CTA of 4 warps, for the last few stiff cells of
- * a hydro step (FP64 path).
+ * a hydro step (FP64 and mixed precision).
  *
  * The split engine (dg_split.cuh) gives each lane its own cell, which is
  * what a full GPU wants; but after the first launches of a step only a few
@@ -18,10 +18,19 @@
  * of warp w computes part w), the pivot search, the back substitution, the
  * temperature and the substep control run on thread 0.
  *
+ * Mixed precision (the Newton matrix formed from FP64 products): the
+ * equilibration exponents, the FP32 rounding and MixedSolve::factor's
+ * elimination run one row, column or entry per lane of warp 0, the FP32
+ * solves and the refinement steps on its lane 0, the FP64 refinement
+ * residual one row per lane; the FP64 elimination above serves the systems
+ * the split engine hands to it, and a converged cell that fails the
+ * conservation check is re-solved from its input with FP64 solves.
+ *
  * Every value is computed with exactly the split engine's operations in the
  * same order (the scaling of a Jacobian entry, the skip tests of the
- * elimination, dg_div with the pivot's reciprocal), so the results are
- * bit-identical to it and to the reference.  The kernel serves the resume
+ * elimination, dg_div with the pivot's reciprocal, the FP32 pivots and
+ * fused multiply-adds), so the results are bit-identical to it and, on the
+ * FP64 path, to the reference.  The kernel serves the resume
  * launches of the stiff-cell redistribution when at most cfg.wide_max cells
  * were set aside (one per SM); otherwise it returns at once and the split
  * engine's launch does the work.
@@ -48,8 +57,8 @@ struct RawPut {
     __device__ __forceinline__ void zero(int q, int v) const { Z[v * N + q] = 1; }
 };
 
-template <class Net>
-__global__ void __launch_bounds__(128)
+template <class Net, bool MIXED>
+__global__ void __launch_bounds__(128, 3)
 evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *queue)
 {
     constexpr int N = Net::N;
@@ -57,27 +66,40 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
     constexpr int NP = 4;
     static_assert(N <= 32, "the wide engine gives each row of the system a lane of one warp");
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-    if (!cfg.resume || !cfg.resume_count || cfg.wide_max <= 0) return;
+    /* the mixed path with the Newton matrix in extended-range FP32 stays on
+     * the split engine */
+    if (!cfg.resume || !cfg.resume_count || cfg.wide_max <= 0 || (MIXED && cfg.jac_xf)) return;
     /* CTA b resumes the b-th set-aside cell: the launch has wide_max CTAs,
      * at least one per cell, and the first wave spreads them over the SMs */
     const unsigned int cnt = *cfg.resume_count;
     if (cnt > (unsigned int)cfg.wide_max || blockIdx.x >= cnt || blockIdx.x >= io.ncells) return;
     (void)queue;
 
-    /* J: the Newton matrix, J[j * N + i] = row i, column j; PP: the back
-     * substitution's products; MB, PRB: multipliers and row order, double
-     * buffered by step; Z: structural zeros of the Jacobian, then the
-     * back substitution's term flags */
-    __shared__ double J[N * N], PP[N * N], R[NT], Y[N], G[N], U[N], U0[N], SC[N], INV[N], AT[N],
+    /* J: the Newton matrix, J[j * N + i] = row i, column j; MB, PRB:
+     * multipliers and row order, double buffered by step; Z: structural
+     * zeros of the Jacobian */
+    __shared__ double J[N * N], R[NT], Y[N], G[N], U[N], U0[N], SC[N], INV[N], AT[N],
         RT[N], PREV[N], RPV[N], PV[N], XS[N], MB[2][N], S[6], TD[Net::T_ND], TQ[Net::T_NQ], TS[2];
     __shared__ int Z[N * N], FROW[N], PRB[2][N];
     __shared__ int s_act, s_okr, s_okj, s_bin, s_dense;
+    /* mixed: FP32 factors, row and column scale exponents, FP32 pivot rows,
+     * the refined solution and residual; s_mix 0 FP64 elimination, 1
+     * refining, 2 refined, 3 stopped short; s_fp64: the cell is re-solved
+     * with FP64 linear solves (it failed the conservation check) */
+    __shared__ float JF[MIXED ? N * N : 1];
+    __shared__ int SI[N], TJ[N], PXP[N];
+    __shared__ double X[N], RR[N];
+    __shared__ int s_mix, s_eprev, s_fp64;
+    /* the solve's state after refinement step it is s_mixb[it & 1]: thread 0
+     * writes the next step's slot while slower threads may still read this
+     * step's */
+    __shared__ int s_mixb[2];
 
     /* thread-0 control state of the CTA's cell */
     long long cell = 0;
     double dtf = 0, dt = 0, ttot = 0;
     int siter = 0, isweep = 0, nsweeps = 0, nfail = 0;
-    bool active = false, dense = false;
+    bool active = false, dense = false, fp64cell = false;
 
     auto substep_begin = [&]() {
         for (int i = 0; i < N; i++) {
@@ -88,8 +110,37 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         }
         isweep = 0;
     };
-    auto cell_begin = [&]() -> bool {
-        /* a set-aside cell, continued from its suspension record */
+    /* from_record: a set-aside cell, continued from its suspension record;
+     * else (the mixed path's conservation re-solve) from the caller's input */
+    auto cell_begin = [&](bool from_record) -> bool {
+        if (!from_record) {
+            double y[N], at[N];
+            for (int s = 0; s < N; s++) {
+                const long long off = cell * io.cs + s * io.ss;
+                y[s] = io.state[off];
+                at[s] = io.atol[off];
+                RT[s] = io.rtol ? io.rtol[off] : io.rtol_scalar;
+            }
+            to_number_density<Net>(y, at);
+            Net::electrons(y);
+            dtf = io.dtf ? io.dtf[cell] : io.dtf_scalar;
+            dt = io.dt ? io.dt[cell] : -1.0;
+            if (dt < 0) dt = dtf / 1e5;
+            ttot = 0;
+            siter = nsweeps = nfail = 0;
+            dense = false;
+            for (int s = 0; s < N; s++) {
+                AT[s] = at[s];
+                Y[s] = y[s];
+                SC[s] = y[s];
+                PREV[s] = y[s];
+                INV[s] = 1.0 / y[s];
+                dense = dense || !(y[s] > 0.0 && dg_finite(y[s]));
+            }
+            if (!(ttot < dtf)) return false;
+            substep_begin();
+            return true;
+        }
         const double *rc = cfg.rec + cell * rec_len<N>();
         dense = false;
         for (int s = 0; s < N; s++) {
@@ -107,6 +158,7 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         siter = (int)rc[4 * N + 2];
         nsweeps = (int)rc[4 * N + 3];
         nfail = (int)rc[4 * N + 4];
+        fp64cell = MIXED && rc[4 * N + 5] != 0.0;
         if (!(ttot < dtf)) return false;
         substep_begin();
         return true;
@@ -142,12 +194,12 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         rc[4 * N + 2] = siter;
         rc[4 * N + 3] = nsweeps;
         rc[4 * N + 4] = nfail;
-        rc[4 * N + 5] = 0.0;   /* the FP64 path: no conservation re-solve */
+        rc[4 * N + 5] = fp64cell ? 1.0 : 0.0;
         io.status[cell] = ST_SUSPENDED;
     };
     if (tid == 0) {
         cell = (long long)io.order[blockIdx.x];
-        active = cell >= 0 && cell_begin();
+        active = cell >= 0 && cell_begin(true);
         if (cell >= 0 && !active) cell_end(ST_OK);
         s_act = active;
     }
@@ -167,6 +219,9 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                     s_dense = dense || !(dt > 0.0);
                     s_okr = 1;
                     s_okj = 1;
+                    s_mix = 0;
+                    s_mixb[0] = 0;
+                    s_fp64 = fp64cell;
                 }
             } else if (w == 1 && l < Net::T_NQ) {
                 const int sp = Net::t_qsp(l);
@@ -222,6 +277,9 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 s_dense = dense || !(dt > 0.0);
                 s_okr = 1;
                 s_okj = 1;
+                s_mix = 0;
+                s_mixb[0] = 0;
+                s_fp64 = fp64cell;
             }
             __syncthreads();
         }
@@ -305,6 +363,147 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 PRB[0][i] = i;
             }
         }
+        __syncthreads();   /* the whole matrix, for the first pivot column's owner or the
+                              mixed solve's warp */
+        /* ---- P5 (mixed): the equilibrated FP32 factorisation on warp 0
+         *      (one row, column or entry per lane, MixedSolve's operations),
+         *      its solves and the FP64 refinement on lane 0 of warp 0, the
+         *      refinement residual one row per lane; the FP64 elimination
+         *      below for a dense or non-finite system, a cell that is being
+         *      re-solved in FP64, or a refinement that stopped short ---- */
+        bool lu64 = do_lu;
+        if constexpr (MIXED) {
+            using MS = MixedSolve<Net, 1>;
+            const MS ms{Slots<1>{J}, SlotsF<1>{JF}};
+            const bool eq = do_lu && !s_dense && !s_fp64;
+            if (eq && w == 0) {
+                /* row scale exponents and the finiteness of A and g */
+                bool fin = true;
+                if (l < N) {
+                    int m = 0;
+                    fin = dg_expo(G[l]) != 0x7ff;
+                    for (int j = 0; j < N; j++) {
+                        const int e = dg_expo(J[j * N + l]);
+                        fin = fin && e != 0x7ff;
+                        m = e > m ? e : m;
+                    }
+                    SI[l] = m ? 1022 - m : 0;
+                }
+                const bool allfin = __all_sync(0xffffffffu, fin);
+                __syncwarp();
+                /* column scale exponents */
+                if (l < N) {
+                    int cm = MS::NONE;
+                    for (int i = 0; i < N; i++) {
+                        if (!Net::jnz(i, l)) continue;
+                        const int e = dg_expo(J[l * N + i]);
+                        if (e != 0 && e + SI[i] > cm) cm = e + SI[i];
+                    }
+                    TJ[l] = cm == MS::NONE ? 0 : 1022 - cm;
+                }
+                __syncwarp();
+                if (allfin) {
+                    /* R A C rounded to FP32 */
+                    for (int e = l; e < N * N; e += 32) {
+                        const int j = e / N, i = e - j * N;
+                        JF[e] = Net::jnz(i, j) ? dg_f32_scaled(J[e], SI[i] + TJ[j]) : 0.0f;
+                    }
+                    __syncwarp();
+                    /* MixedSolve::factor, one row / entry per lane */
+                    for (int k = 0; k < N - 1; k++) {
+                        const bool cand = l >= k && l < N;
+                        const unsigned int key = cand ? __float_as_uint(fabsf(JF[k * N + l])) : 0u;
+                        const unsigned int kk = __shfl_sync(0xffffffffu, key, k);
+                        int p = k;
+                        if (kk <= 0x7f800000u) {
+                            /* the first row of largest |a| among the non-NaN ones */
+                            const bool valid = cand && key <= 0x7f800000u;
+                            const unsigned int mx = __reduce_max_sync(0xffffffffu, valid ? key : 0u);
+                            p = __ffs(__ballot_sync(0xffffffffu, valid && key == mx)) - 1;
+                        }
+                        if (p != k && l >= k && l < N) {
+                            const float t = JF[l * N + k];
+                            JF[l * N + k] = JF[l * N + p];
+                            JF[l * N + p] = t;
+                        }
+                        if (l == 0) PXP[k] = p;
+                        __syncwarp();
+                        const float rp = 1.0f / JF[k * N + k];
+                        const float mi = l > k && l < N ? JF[k * N + l] * rp : 0.0f;
+                        __syncwarp();
+                        if (l > k && l < N) JF[k * N + l] = mi;
+                        if (l == 0) JF[k * N + k] = rp;
+                        __syncwarp();
+                        const int rows = N - 1 - k;
+                        for (int e = l; e < rows * rows; e += 32) {
+                            const int j = k + 1 + e / rows, i = k + 1 + e % rows;
+                            JF[j * N + i] = fmaf(-JF[k * N + i], JF[j * N + k], JF[j * N + i]);
+                        }
+                        __syncwarp();
+                    }
+                    if (l == 0) {
+                        PXP[N - 1] = N - 1;
+                        JF[(N - 1) * N + (N - 1)] = 1.0f / JF[(N - 1) * N + (N - 1)];
+                        /* the first solve */
+                        double g[N], x[N];
+                        int sx[N], tx[N], px[N];
+                        for (int i = 0; i < N; i++) {
+                            g[i] = G[i];
+                            sx[i] = SI[i];
+                            tx[i] = TJ[i];
+                            px[i] = PXP[i];
+                        }
+                        int ed;
+                        if (ms.apply(px, sx, tx, g, x, ed)) {
+                            for (int i = 0; i < N; i++) X[i] = x[i];
+                            s_mixb[0] = 1;
+                            s_eprev = 0x7ff;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            int it = 0;
+            for (; it < MS::MAX_REFINE; it++) {
+                if (!(eq && s_mixb[it & 1] == 1)) break;
+                if (w == 0) {
+                    if (l < N) RR[l] = ms.residual_row(l, G[l], X);
+                    __syncwarp();
+                    if (l == 0) {
+                        double r[N], x[N];
+                        int sx[N], tx[N], px[N];
+                        for (int i = 0; i < N; i++) {
+                            r[i] = RR[i];
+                            x[i] = X[i];
+                            sx[i] = SI[i];
+                            tx[i] = TJ[i];
+                            px[i] = PXP[i];
+                        }
+                        int eprev = s_eprev, next = 0;
+                        bool more;
+                        if (ms.refine(px, sx, tx, r, x, eprev, more)) {
+                            for (int i = 0; i < N; i++) X[i] = x[i];
+                            s_eprev = eprev;
+                            next = more ? 1 : 2;
+                            if (DG_MIXED_STRICT && !more && !MS::refined(x, eprev)) next = 3;
+                        }
+                        s_mixb[(it + 1) & 1] = next;
+                    }
+                }
+                __syncthreads();
+            }
+            /* a refinement that ran out of steps or stopped short of 2^-40
+             * goes to the FP64 elimination */
+            if (tid == 0) {
+                int m = eq ? s_mixb[it & 1] : 0;
+                if (DG_MIXED_STRICT && (m == 1 || m == 3)) m = 0;
+                s_mix = m;
+            }
+            __syncthreads();
+            if (eq && s_mix != 0)
+                for (int i = tid; i < N; i += 128) XS[i] = X[i];
+            lu64 = do_lu && s_mix == 0;
+        }
         /* ---- P5: Gauss_Elim with one barrier per elimination step.
          * Column j belongs to warp j mod 4 throughout.  Step k: the owner of
          * column k finds the pivot (a warp reduction that picks the first
@@ -321,7 +520,7 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
             const int *PRo = PRB[k & 1];
             int *PRn = PRB[(k + 1) & 1];
             double *M = MB[k & 1];
-            if (do_lu && w == (k & 3)) {
+            if (lu64 && w == (k & 3)) {
                 const int i = l;
                 const bool cand = i >= k && i < N;
                 const int pri = i < N ? PRo[i] : 0;
@@ -354,7 +553,7 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 __syncwarp();
             }
             __syncthreads();
-            if (do_lu) {
+            if (lu64) {
                 const int pk = PRn[k];
                 /* row k's entries right of the pivot all finite? */
                 bool fin = true;
@@ -386,30 +585,37 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
             }
         }
         __syncthreads();
-        /* ---- back substitution (warp 0, lane i = row i): x_j is formed by
-         * lane j from its row's products in increasing column order, then
-         * every row above forms its product with x_j at once ---- */
-        if (do_lu && w == 0) {
+        /* ---- back substitution (warp 0, lane i = row i, in registers):
+         * lane j forms x_j from its row's products in increasing column
+         * order, a shuffle hands x_j to the warp, and every row above forms
+         * its product with x_j at once ---- */
+        if (lu64 && w == 0) {
             const int *PRf = PRB[(N - 1) & 1];
             const int rl = l < N ? PRf[l] : 0;
+            double a[N], p[N];
+#pragma unroll
+            for (int t = 0; t < N; t++) {
+                a[t] = l < N ? J[t * N + rl] : 0.0;
+                p[t] = 0.0;
+            }
+            const double g0 = l < N ? G[rl] : 0.0;
+            unsigned int f = 0;   /* bit t: row l subtracts its product with x_t */
+            double xv = 0.0;
 #pragma unroll
             for (int j = N - 1; j >= 0; j--) {
                 if (l == j) {
-                    double acc = G[rl];
+                    double acc = g0;
 #pragma unroll
                     for (int t = j + 1; t < N; t++)
-                        if (Z[t * N + j]) acc = acc - PP[t * N + j];
-                    const double u = J[j * N + rl];
-                    XS[j] = j == N - 1 ? dg_quot(acc, u) : dg_div(acc, u, RPV[j]);
+                        if (f & (1u << t)) acc = acc - p[t];
+                    xv = j == N - 1 ? dg_quot(acc, a[j]) : dg_div(acc, a[j], RPV[j]);
+                    XS[j] = xv;
                 }
-                __syncwarp();
+                const double xj = __shfl_sync(0xffffffffu, xv, j);
                 if (l < j) {
-                    const double xj = XS[j];
-                    const double a = J[j * N + rl];
-                    Z[j * N + l] = dg_nonzero(a) || !dg_finite(xj);
-                    PP[j * N + l] = a * xj;
+                    p[j] = a[j] * xj;
+                    if (dg_nonzero(a[j]) || !dg_finite(xj)) f |= 1u << j;
                 }
-                __syncwarp();
             }
         }
         __syncthreads();
@@ -473,6 +679,14 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
                 for (int i = 0; i < N; i++) Y[i] = y[i];
                 if (done < 0 && !(cfg.sweep_budget > 0 && nsweeps >= cfg.sweep_budget)) {
                     substep_begin();
+                } else if (MIXED && done == ST_OK && cfg.cons_tol != 0.0 && !fp64cell &&
+                           !conserved<Net>(io, cell, y, cfg.cons_tol)) {
+                    /* start the cell again from its input, FP64 linear solves */
+                    fp64cell = true;
+                    if (!cell_begin(false)) {
+                        cell_end(ST_OK);
+                        active = false;
+                    }
                 } else {
                     if (done < 0) suspend();
                     else cell_end(done);

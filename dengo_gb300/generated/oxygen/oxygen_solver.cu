@@ -2512,6 +2512,9 @@ template int dg::launch_split<dgnet_oxygen::Net, 4, true>(DG_LAUNCH_ARGS);
 #if DG_KERNEL_PART == 10
 template int dg::launch_wide<dgnet_oxygen::Net, 4, false>(DG_LAUNCH_ARGS);
 #endif
+#if DG_KERNEL_PART == 11
+template int dg::launch_wide<dgnet_oxygen::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
 #else
 #if defined(DG_SPLIT_KERNELS)
 extern template int dg::launch_lane<dgnet_oxygen::Net, 32, false>(DG_LAUNCH_ARGS);
@@ -2525,6 +2528,7 @@ extern template int dg::launch_split<dgnet_oxygen::Net, 2, true>(DG_LAUNCH_ARGS)
 extern template int dg::launch_split<dgnet_oxygen::Net, 4, false>(DG_LAUNCH_ARGS);
 extern template int dg::launch_split<dgnet_oxygen::Net, 4, true>(DG_LAUNCH_ARGS);
 extern template int dg::launch_wide<dgnet_oxygen::Net, 4, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_wide<dgnet_oxygen::Net, 4, true>(DG_LAUNCH_ARGS);
 #endif
 
 extern "C" {

@@ -2644,6 +2644,9 @@ template int dg::launch_split<dgnet_oxygen_uvb::Net, 4, true>(DG_LAUNCH_ARGS);
 #if DG_KERNEL_PART == 10
 template int dg::launch_wide<dgnet_oxygen_uvb::Net, 4, false>(DG_LAUNCH_ARGS);
 #endif
+#if DG_KERNEL_PART == 11
+template int dg::launch_wide<dgnet_oxygen_uvb::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
 #else
 #if defined(DG_SPLIT_KERNELS)
 extern template int dg::launch_lane<dgnet_oxygen_uvb::Net, 32, false>(DG_LAUNCH_ARGS);
@@ -2657,6 +2660,7 @@ extern template int dg::launch_split<dgnet_oxygen_uvb::Net, 2, true>(DG_LAUNCH_A
 extern template int dg::launch_split<dgnet_oxygen_uvb::Net, 4, false>(DG_LAUNCH_ARGS);
 extern template int dg::launch_split<dgnet_oxygen_uvb::Net, 4, true>(DG_LAUNCH_ARGS);
 extern template int dg::launch_wide<dgnet_oxygen_uvb::Net, 4, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_wide<dgnet_oxygen_uvb::Net, 4, true>(DG_LAUNCH_ARGS);
 #endif
 
 extern "C" {

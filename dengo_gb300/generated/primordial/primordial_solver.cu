@@ -1456,6 +1456,9 @@ template int dg::launch_split<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
 #if DG_KERNEL_PART == 10
 template int dg::launch_wide<dgnet_primordial::Net, 4, false>(DG_LAUNCH_ARGS);
 #endif
+#if DG_KERNEL_PART == 11
+template int dg::launch_wide<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
 #else
 #if defined(DG_SPLIT_KERNELS)
 extern template int dg::launch_lane<dgnet_primordial::Net, 32, false>(DG_LAUNCH_ARGS);
@@ -1469,6 +1472,7 @@ extern template int dg::launch_split<dgnet_primordial::Net, 2, true>(DG_LAUNCH_A
 extern template int dg::launch_split<dgnet_primordial::Net, 4, false>(DG_LAUNCH_ARGS);
 extern template int dg::launch_split<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
 extern template int dg::launch_wide<dgnet_primordial::Net, 4, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_wide<dgnet_primordial::Net, 4, true>(DG_LAUNCH_ARGS);
 #endif
 
 extern "C" {

@@ -1462,6 +1462,9 @@ template int dg::launch_split<dgnet_primordial_compton::Net, 4, true>(DG_LAUNCH_
 #if DG_KERNEL_PART == 10
 template int dg::launch_wide<dgnet_primordial_compton::Net, 4, false>(DG_LAUNCH_ARGS);
 #endif
+#if DG_KERNEL_PART == 11
+template int dg::launch_wide<dgnet_primordial_compton::Net, 4, true>(DG_LAUNCH_ARGS);
+#endif
 #else
 #if defined(DG_SPLIT_KERNELS)
 extern template int dg::launch_lane<dgnet_primordial_compton::Net, 32, false>(DG_LAUNCH_ARGS);
@@ -1475,6 +1478,7 @@ extern template int dg::launch_split<dgnet_primordial_compton::Net, 2, true>(DG_
 extern template int dg::launch_split<dgnet_primordial_compton::Net, 4, false>(DG_LAUNCH_ARGS);
 extern template int dg::launch_split<dgnet_primordial_compton::Net, 4, true>(DG_LAUNCH_ARGS);
 extern template int dg::launch_wide<dgnet_primordial_compton::Net, 4, false>(DG_LAUNCH_ARGS);
+extern template int dg::launch_wide<dgnet_primordial_compton::Net, 4, true>(DG_LAUNCH_ARGS);
 #endif
 
 extern "C" {

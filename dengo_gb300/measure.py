@@ -19,6 +19,13 @@
         measured time of one sweep of a lone cell -- the latency no schedule
         can beat, since a cell's sweeps run one after another.
 
+    python -m dengo_gb300.measure tail [--per-sm 1 2 3 6 --budget 50 --precision fp64]
+        The last launches of a hydro step: one stiff primordial cell (the
+        config-2 "hot" seeded set) copied k times per SM, set aside after
+        --budget sweeps and resumed, once by the split engine (wide_tail 0)
+        and once by the wide engine (wide_tail k); microseconds per Newton
+        sweep of each, the time a step's stiffest cells take per sweep.
+
 Each prints one JSON line.
 """
 import json
@@ -161,6 +168,34 @@ def config5(rate=50.0, duration=60.0, edge_range=(16, 128), budget_gb=40.0, slot
                                        "requests": int(len(floors))}}
 
 
+def tail(per_sm=(1, 2, 3, 6), budget=50, kind="hot", cell=0, seed=20245, split=True,
+         precision=DENGO_FP64):
+    """Microseconds per Newton sweep of k copies per SM of one stiff cell
+    resumed after ``budget`` sweeps: split engine vs wide engine."""
+    import torch
+    from .workloads import primordial_cells
+    torch.cuda.set_device(0)
+    solver = Solver("primordial")
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    state, dtf = primordial_cells(64, kind, seed=seed)
+    rows = []
+    for k in per_sm:
+        n = nsm * k
+        st = np.repeat(state[cell:cell + 1], n, axis=0)
+        d = np.repeat(np.asarray(dtf)[cell:cell + 1], n)
+        for wide in ((0, k) if split else (k,)):
+            cfg = Solver.default_config()
+            cfg.sweep_budget, cfg.wide_tail, cfg.precision = budget, wide, precision
+            r = solver.solve_host(st, d, config=cfg, counters=True)
+            sw = int(r["sweeps"].max())
+            rows.append({"cells": n, "per_sm": k, "engine": "wide" if wide else "split",
+                         "sweeps": sw, "ms": r["solve_ms"],
+                         "us_per_sweep": r["solve_ms"] * 1e3 / max(sw - budget, 1)})
+    return {"cell": {"kind": kind, "seed": seed, "index": cell}, "budget": budget,
+            "precision": "mixed" if precision == DENGO_MIXED else "fp64", "sms": nsm,
+            "rows": rows}
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
@@ -179,10 +214,20 @@ def main(argv=None):
     a5.add_argument("--admit-until", type=float, default=None,
                     help="stop admitting requests after this many seconds (the rest is "
                          "reported as backlog)")
+    at = sub.add_parser("tail")
+    at.add_argument("--per-sm", type=int, nargs="+", default=[1, 2, 3, 6])
+    at.add_argument("--budget", type=int, default=50)
+    at.add_argument("--kind", default="hot")
+    at.add_argument("--cell", type=int, default=0)
+    at.add_argument("--wide-only", action="store_true")
+    at.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     a = ap.parse_args(argv)
     t0 = time.perf_counter()
     if a.what == "config4":
         out = config4(a.cells, a.sample)
+    elif a.what == "tail":
+        out = tail(a.per_sm, a.budget, a.kind, a.cell, split=not a.wide_only,
+                   precision=DENGO_MIXED if a.precision == "mixed" else DENGO_FP64)
     else:
         out = config5(a.rate, a.duration, (a.edge_min, a.edge_max), a.budget_gb, a.slots,
                       DENGO_MIXED if a.precision == "mixed" else DENGO_FP64, a.admit_until)

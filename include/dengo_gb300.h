@@ -169,11 +169,11 @@ typedef struct dengo_solver_config {
                                   linear solves.  <= 0: no check; default
                                   1e-9 (the FP64 path's own drift stays near
                                   1e-12) */
-    int wide_tail;             /* DENGO_FP64 with sweep_budget > 0: a resume
-                                  launch with at most wide_tail set-aside
-                                  cells per SM (1 to 8) gives each cell a
-                                  block of four warps that share its
-                                  elimination entry by entry (the wide
+    int wide_tail;             /* sweep_budget > 0, DENGO_FP64 or
+                                  DENGO_MIXED: a resume launch with at most
+                                  wide_tail set-aside cells per SM (1 to 8)
+                                  gives each cell a block of four warps that
+                                  share its sweep entry by entry (the wide
                                   engine); results are unchanged.  0 = off;
                                   default 3 */
 } dengo_solver_config;

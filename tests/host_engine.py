@@ -28,7 +28,7 @@ barriers across the warp's 32 threads around a value each posts, and the
 atomics take a lock.  One CTA runs the whole batch from the work queue.  A build that hangs is cut off by the caller's timeout
 (``evolve_in_subprocess``).  ``engine="wide"`` adds the wide engine
 (dg_wide.cuh, one CTA of 128 threads per cell) and hands it every cell of
-the FP64 path's resume launches.
+the resume launches.
 """
 import ctypes as C
 import os
@@ -114,8 +114,11 @@ static inline int atomicMin(int *p, int v)
     if (v < o) *p = v;
     return o;
 }
-/* A reusable barrier whose waiters yield the core (the lanes far outnumber
- * the host's cores, so sleeping and waking them costs more). */
+/* A reusable barrier.  Waiters yield the core for a while (the lanes far
+ * outnumber the host's cores, and most barriers are met quickly), then
+ * sleep on the generation counter, so that threads parked at one barrier
+ * (the other warps, while one warp runs a long stretch of warp-level steps)
+ * do not crowd out the threads that are working. */
 struct hx_barrier {
     explicit hx_barrier(int n) : count(n), left(n), gen(0) {}
     void arrive_and_wait()
@@ -124,8 +127,13 @@ struct hx_barrier {
         if (left.fetch_sub(1, std::memory_order_acq_rel) == 1) {
             left.store(count, std::memory_order_relaxed);
             gen.store(g + 1, std::memory_order_release);
+            gen.notify_all();
         } else {
-            while (gen.load(std::memory_order_acquire) == g) std::this_thread::yield();
+            for (int spin = 0; spin < 64; spin++) {
+                if (gen.load(std::memory_order_acquire) != g) return;
+                std::this_thread::yield();
+            }
+            while (gen.load(std::memory_order_acquire) == g) gen.wait(g, std::memory_order_acquire);
         }
     }
     const int count;
@@ -227,13 +235,14 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
 '''
 
 DRIVER_WIDE_LAUNCH = DRIVER_SPLIT_LAUNCH.replace("static void launch(", "static void launch_split(") + r'''
-/* The split engine, and for the FP64 path's resume launches the wide engine
+/* The split engine, and for the resume launches the wide engine
  * (dg_wide.cuh, one CTA of 4 warps per cell) with every set-aside cell:
- * the split engine's launch then returns at once. */
+ * the split engine's launch then returns at once (not for the Newton matrix
+ * in extended-range FP32). */
 template <bool MIXED>
 static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned long long *queue)
 {
-    const bool wide = !MIXED && cfg.resume;
+    const bool wide = cfg.resume && !cfg.jac_xf;
     if (wide) cfg.wide_max = 1 << 30;
     launch_split<MIXED>(io, ts, cfg, queue);
     if (!wide) return;
@@ -248,7 +257,7 @@ static void launch(dg::CellIO io, dg::TableSet ts, dg::KernelCfg cfg, unsigned l
         for (unsigned t = 0; t < 128; t++)
             lanes.emplace_back([=]() {
                 threadIdx.x = t;
-                dg::evolve_wide_kernel<Net>(io, ts, cfg, queue);
+                dg::evolve_wide_kernel<Net, MIXED>(io, ts, cfg, queue);
             });
         for (auto &th : lanes) th.join();
     }

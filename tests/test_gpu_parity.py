@@ -368,6 +368,25 @@ def test_wide_tail_is_bit_identical(solver, crlog_oracle, config, n):
         assert np.array_equal(outs[1][k][ok], ref[k][ok]), k
 
 
+@pytest.mark.parametrize("config,n", [("config2", 128), ("config3", 512)])
+def test_wide_tail_mixed_is_bit_identical(solver, config, n):
+    """Mixed precision: resume launches on the wide engine (wide_tail 3, the
+    default) give the split engine's results (wide_tail 0) bit for bit."""
+    from dengo_gb300.runtime import Solver, DENGO_MIXED
+    from dengo_gb300.workloads import primordial_cells
+    state, dtf = primordial_cells(n, config, seed=37)
+    outs = []
+    for wide in (0, 3):
+        cfg = Solver.default_config()
+        cfg.precision, cfg.wide_tail = DENGO_MIXED, wide
+        outs.append(solver.solve_host(state, dtf, rtol=1e-6, config=cfg, counters=True))
+    assert int(np.sum(outs[0]["sweeps"] > cfg.sweep_budget)) > 0
+    for k in ("state", "atol", "dt", "ttot", "status", "substeps", "sweeps", "failures"):
+        assert np.array_equal(outs[1][k].view(np.uint8), outs[0][k].view(np.uint8)), k
+    print("mixed %s: split %.1f ms, wide %.1f ms" % (config, outs[0]["solve_ms"],
+                                                   outs[1]["solve_ms"]))
+
+
 @pytest.mark.parametrize("wpc,precision", [(4, 0), (1, 0), (4, 1)])
 def test_sweep_budget_redistribution_is_bit_identical(solver, golden, wpc, precision):
     """Stiff-cell redistribution (cells set aside at a sweep budget, resumed

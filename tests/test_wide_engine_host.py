@@ -1,10 +1,11 @@
-"""The wide engine (dg_wide.cuh: one cell per CTA of 4 warps, the FP64
-path's engine for the last few set-aside cells of a solve) compiled for the
-host with its 128 lanes as threads (tests/host_engine.py), against the split
-engine compiled the same way: a solve whose resume launches all run on the
-wide engine must equal, bit for bit, the same solve on the split engine
-alone -- and hence the single-lane engine and the reference.  Each solve
-runs in a child process with a time limit."""
+"""The wide engine (dg_wide.cuh: one cell per CTA of 4 warps, the engine for
+the last few set-aside cells of a solve) compiled for the host with its 128
+lanes as threads (tests/host_engine.py), against the split engine compiled
+the same way: a solve whose resume launches all run on the wide engine must
+equal, bit for bit, the same solve on the split engine alone -- and hence
+the single-lane engine and, on the FP64 path, the reference.  FP64 and mixed
+precision (its FP64 fallbacks and conservation re-solves included).  Each
+solve runs in a child process with a time limit."""
 import json
 import os
 
@@ -30,7 +31,9 @@ def tables():
 def libs(tmp_path_factory):
     d = tmp_path_factory.mktemp("wide_engine")
     return {"split": he.compile_engine("primordial", d, engine="split"),
-            "wide": he.compile_engine("primordial", d, engine="wide")}
+            "wide": he.compile_engine("primordial", d, engine="wide"),
+            "split_lenient": he.compile_engine("primordial", d, strict=False, engine="split"),
+            "wide_lenient": he.compile_engine("primordial", d, strict=False, engine="wide")}
 
 
 def _same(a, b):
@@ -47,20 +50,54 @@ CASES = [("cold", 24, 23, None, 60),
          ("top", 64, 23, [11, 14, 47], 40)]
 
 
+@pytest.mark.parametrize("mixed", [0, 1])
 @pytest.mark.parametrize("kind,n,seed,pick,budget", CASES, ids=[c[0] for c in CASES])
-def test_wide_resume_equals_split(libs, tables, kind, n, seed, pick, budget):
+def test_wide_resume_equals_split(libs, tables, kind, n, seed, pick, budget, mixed):
     """Cells set aside after a small sweep budget and resumed twice (at 16x
     the budget, then to the end): the wide engine's resumed cells equal the
-    split engine's."""
+    split engine's, FP64 and mixed precision."""
     from dengo_gb300.workloads import primordial_cells
     st, dtf = primordial_cells(n, kind, seed=seed)
     if pick is not None:
         st, dtf = st[pick], np.broadcast_to(np.asarray(dtf, np.float64), (n,))[pick]
     split = he.evolve_in_subprocess(libs["split"], tables, st, dtf, timeout=900,
-                                    sweep_budget=budget)
+                                    sweep_budget=budget, mixed=mixed)
     wide = he.evolve_in_subprocess(libs["wide"], tables, st, dtf, timeout=900,
-                                   sweep_budget=budget)
+                                   sweep_budget=budget, mixed=mixed)
     assert wide["resumed"] > 0 and wide["resumed"] == split["resumed"]
+    _same(wide, split)
+
+
+@pytest.mark.parametrize("build", ["", "_lenient"])
+def test_wide_mixed_fallback_equals_split(libs, tables, build):
+    """Three config-3 cells whose mixed refinement sometimes stops short of
+    2^-40, resumed on the wide engine: it hands those systems to the FP64
+    elimination (shipped build) or keeps them (lenient build) exactly as the
+    split engine does."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(256, "config3", seed=78)
+    pick = [8, 174, 218]
+    st, dtf = st[pick], np.asarray(dtf)[pick]
+    split = he.evolve_in_subprocess(libs["split" + build], tables, st, dtf, timeout=900,
+                                    mixed=True, sweep_budget=30)
+    wide = he.evolve_in_subprocess(libs["wide" + build], tables, st, dtf, timeout=900,
+                                   mixed=True, sweep_budget=30)
+    assert wide["resumed"] > 0
+    _same(wide, split)
+
+
+def test_wide_conservation_resolve_equals_split(libs, tables):
+    """A conservation tolerance below zero fails every converged mixed cell,
+    which is re-solved from its input with FP64 linear solves: set aside and
+    resumed on the wide engine, both the first solve and the re-solve equal
+    the split engine's."""
+    from dengo_gb300.workloads import primordial_cells
+    st, dtf = primordial_cells(8, "cold", seed=41)
+    split = he.evolve_in_subprocess(libs["split"], tables, st, dtf, timeout=900, mixed=True,
+                                    sweep_budget=40, cons_tol=-1.0)
+    wide = he.evolve_in_subprocess(libs["wide"], tables, st, dtf, timeout=900, mixed=True,
+                                   sweep_budget=40, cons_tol=-1.0)
+    assert wide["resumed"] > 0
     _same(wide, split)
 
 
