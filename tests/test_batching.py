@@ -27,8 +27,12 @@ def test_graph_replay_equals_eager_steps(solver):
     cfg.warps_per_cell = 4
     dev = torch.device("cuda")
     d_dtf = torch.tensor(dtf, device=dev)
-    eager = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg)
-    graph = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg).capture()
+    # both share the solver's context (its scratch), so they share a stream:
+    # calls on one context must not overlap on the GPU
+    stream = torch.cuda.Stream(device=dev)
+    eager = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg, stream=stream)
+    graph = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg,
+                      stream=stream).capture()
     for _ in range(3):
         eager.eager()
         graph.replay()
@@ -68,8 +72,12 @@ def test_graph_replay_with_sweep_budget_equals_eager_steps(solver):
     cfg.warps_per_cell, cfg.sweep_budget, cfg.max_substeps = 4, 30, 2000
     dev = torch.device("cuda")
     d_dtf = torch.tensor(dtf, device=dev)
-    eager = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg)
-    graph = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg).capture()
+    # both share the solver's context (its scratch), so they share a stream:
+    # calls on one context must not overlap on the GPU
+    stream = torch.cuda.Stream(device=dev)
+    eager = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg, stream=stream)
+    graph = StepGraph(solver, torch.tensor(state, device=dev), d_dtf, cfg,
+                      stream=stream).capture()
     for _ in range(2):
         eager.eager()
         graph.replay()
