@@ -59,13 +59,13 @@ DRAM_BYTES_PER_CELL = {"fp64": 2.876928e6 / 14592, "mixed": 5.14512e6 / 14592,
                        "mixed_xf": 5.14512e6 / 14592}
 # solver kernels per hydro step with a cost hint and a sweep budget: the
 # three order kernels, the first launch, and two resume launches each after
-# two list kernels (FP64 with the wide tail: each resume launch followed by
-# the wide engine's)
+# two list kernels (with the wide tail, FP64 and mixed: each resume launch
+# followed by the wide engine's)
 LAUNCHES_PER_STEP = 3 + 1 + 2 * (2 + 1)
 
 
 def launches_per_step(precision, wide_tail):
-    return LAUNCHES_PER_STEP + (2 if precision == "fp64" and wide_tail else 0)
+    return LAUNCHES_PER_STEP + (2 if precision in ("fp64", "mixed") and wide_tail else 0)
 
 
 def parse():

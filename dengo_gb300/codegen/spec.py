@@ -81,6 +81,9 @@ class NetworkSpec:
     # T(ge) in lane-parallel parts (temperature_lanes), or None when the
     # printed expressions are not of that form
     t_lanes: object = None
+    # the RHS rows and Jacobian entries that are flat sums of signed
+    # products, as term tables for lane-parallel evaluation (sop_tables)
+    sop: object = None
 
     @property
     def N(self):
@@ -157,6 +160,153 @@ def temperature_lanes(species, mass_density, T_div, Tge_div):
     if not dens or not quot or len(dens) > 32 or len(quot) > 32:
         return None
     return {"density": dens, "quot": quot}
+
+
+_SOP_TOK = re.compile(r"\s*(?:(dg_ipow<(\d+)>\(([A-Za-z_][A-Za-z0-9_]*)\))|"
+                      r"(\d+\.\d*(?:e[+-]?\d+)?|\d+(?:e[+-]?\d+)?)|([A-Za-z_][A-Za-z0-9_]*)|([-+*]))")
+
+
+def sop_parse(expr, names):
+    """``[(sign, [factor, ...]), ...]`` when the C expression ``expr`` is a
+    flat sum of signed products of atoms -- ``[-]a*b*c +|- d*e ...`` with
+    atoms numeric literals, names in ``names`` (rates, species) and
+    ``dg_ipow<n>(species)`` -- else None.  C evaluates such an expression as
+    ((t0 + t1) - t2) ..., each term as ((a*b)*c)...; a leading unary minus
+    binds to the first factor, which negates the term exactly.  Factors:
+    ``("lit", text)``, ``("name", name)``, ``("pow", n, name)``."""
+    toks, pos, e = [], 0, expr.strip()
+    while pos < len(e):
+        m = _SOP_TOK.match(e, pos)
+        if not m or m.end() == pos:
+            return None
+        pos = m.end()
+        if m.group(1):
+            if m.group(3) not in names or not 2 <= int(m.group(2)) <= 6:
+                return None
+            toks.append(("pow", int(m.group(2)), m.group(3)))
+        elif m.group(4):
+            toks.append(("lit", m.group(4)))
+        elif m.group(5):
+            if m.group(5) not in names:
+                return None
+            toks.append(("name", m.group(5)))
+        else:
+            toks.append(m.group(6))
+    terms, i, sign = [], 0, 1
+    if toks and toks[0] == "-":
+        sign, i = -1, 1
+    while True:
+        facs = []
+        while True:
+            if i >= len(toks) or isinstance(toks[i], str):
+                return None
+            facs.append(toks[i])
+            i += 1
+            if i < len(toks) and toks[i] == "*":
+                i += 1
+                continue
+            break
+        terms.append((sign, facs))
+        if i == len(toks):
+            return terms
+        if toks[i] not in ("+", "-"):
+            return None
+        sign = 1 if toks[i] == "+" else -1
+        i += 1
+
+
+def sop_tables(species, tables, rhs_dev, jac_dev, jac_nz):
+    """Operand and term tables of the RHS rows and Jacobian entries that
+    sop_parse accepts, for lane-parallel evaluation (the wide engine), and
+    the lists of the others.  Operands: the rates, the species, the powers
+    dg_ipow<n>(species) that occur, the literals, and 1.0 (which pads a
+    term's factors: x * 1.0 is x).  A term is a sign and FMAX operand
+    indices; an entry is a term range and a final operation (RHS ge row:
+    / mdensity; Jacobian: dg_div by mdensity for the ge row, * Tge for the ge
+    column).  None when nothing parses."""
+    sp_index = {sp.name: sp.index for sp in species}
+    ge = [sp.index for sp in species if sp.is_ge][0]
+    names = set(sp_index) | {t.name for t in tables}
+    t_index = {t.name: t.index for t in tables}
+    NT, N = len(tables), len(species)
+
+    def body(stmt, lhs):
+        m = re.match(r"^\s*%s = (.*);\s*$" % re.escape(lhs), stmt, re.S)
+        return m.group(1) if m else None
+
+    rhs, jac = {}, {}
+    for i in range(N):
+        b = body(rhs_dev[i], "f[%d]" % i)
+        t = sop_parse(b, names) if b is not None else None
+        if t is not None:
+            rhs[i] = t
+    for v in range(N):
+        for q in range(N):
+            if not jac_nz[v][q]:
+                continue
+            b = body(jac_dev[v][q], "jv")
+            t = sop_parse(b, names) if b is not None else None
+            if t is not None:
+                jac[(q, v)] = t
+    if not rhs and not jac:
+        return None
+    pows = sorted({(f[1], sp_index[f[2]]) for ts in list(rhs.values()) + list(jac.values())
+                   for _, fs in ts for f in fs if f[0] == "pow"})
+    lits = []
+    for ts in list(rhs.values()) + list(jac.values()):
+        for _, fs in ts:
+            for f in fs:
+                if f[0] == "lit" and f[1] not in lits:
+                    lits.append(f[1])
+    op_pow = {p: NT + N + k for k, p in enumerate(pows)}
+    op_lit = {l: NT + N + len(pows) + k for k, l in enumerate(lits)}
+    one = NT + N + len(pows) + len(lits)
+    fmax = max(len(fs) for ts in list(rhs.values()) + list(jac.values()) for _, fs in ts)
+
+    def operand(f):
+        if f[0] == "lit":
+            return op_lit[f[1]]
+        if f[0] == "pow":
+            return op_pow[(f[1], sp_index[f[2]])]
+        return t_index[f[1]] if f[1] in t_index else NT + sp_index[f[1]]
+
+    def flatten(entries):
+        terms, ranges = [], []
+        for key, ts in entries:
+            t0 = len(terms)
+            for sign, fs in ts:
+                ops = [operand(f) for f in fs]
+                terms.append((sign, ops + [one] * (fmax - len(ops))))
+            ranges.append((key, t0, len(terms)))
+        return terms, ranges
+
+    rhs_terms, rhs_ranges = flatten(sorted(rhs.items()))
+    jac_terms, jac_ranges = flatten(sorted(jac.items(), key=lambda kv: (kv[0][1], kv[0][0])))
+
+    def lit_value(text):
+        return text if ("." in text or "e" in text) else text + ".0"
+
+    rhs_rest = [i for i in range(N) if i not in rhs]
+    jac_rest = [(q, v) for v in range(N) for q in range(N) if jac_nz[v][q] and (q, v) not in jac]
+    # the other rows / entries as scalar code on up to three warps, balanced
+    # by the length of their printed expressions
+    rk, jk = min(3, len(rhs_rest)), min(3, len(jac_rest))
+    rpart = dict(zip(rhs_rest, balance([float(len(rhs_dev[i])) for i in rhs_rest], rk))) \
+        if rk else {}
+    jpart = dict(zip(jac_rest, balance([float(len(jac_dev[v][q])) for q, v in jac_rest], jk))) \
+        if jk else {}
+    enc = lambda terms: [(ops[0] | (0x8000 if sign < 0 else 0), *ops[1:]) for sign, ops in terms]
+    return {"nops": one + 1, "one": one, "fmax": fmax, "pows": pows,
+            "rk": rk, "jk": jk, "rhs_rest_part": rpart, "jac_rest_part": jpart,
+            "rhs_enc": enc(rhs_terms), "jac_enc": enc(jac_terms),
+            "lits": [lit_value(l) for l in lits], "lit0": NT + N + len(pows),
+            "rhs_terms": rhs_terms,
+            "rhs_entries": [(i, t0, t1, 1 if i == ge else 0) for i, t0, t1 in rhs_ranges],
+            "rhs_rest": rhs_rest,
+            "jac_terms": jac_terms,
+            "jac_entries": [(q, v, t0, t1, (1 if q == ge else 0) | (2 if v == ge else 0))
+                            for (q, v), t0, t1 in jac_ranges],
+            "jac_rest": jac_rest}
 
 
 def balance(costs, nparts):
@@ -271,6 +421,7 @@ def network_spec(net, name):
         T_dev_div=gamma_div(ccode_device(T)), Tge_dev_div=gamma_div(ccode_device(Tg)),
         t_lanes=temperature_lanes(species, ccode_device(md), gamma_div(ccode_device(T)),
                                   gamma_div(ccode_device(Tg))),
+        sop=sop_tables(species, tables, rhs_dev, jac_dev, jac_nz),
         rhs_ref=rhs_ref, rhs_dev=rhs_dev,
         jac_ref=jac_ref, jac_dev=jac_dev, jac_dev32=jac_dev32, jac_nonzero=jac_nz,
         rhs_part=rhs_part, jac_part=jac_part)

@@ -42,6 +42,17 @@
 
 namespace dg {
 
+/* A barrier among the first n threads of warps [from, ...): the CTA's
+ * named barrier id (bar.sync id, n); the host build supplies its own. */
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ void dg_named_sync(int id, int n)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+#elif !defined(DG_HOST_NAMED_SYNC)
+__host__ __device__ inline void dg_named_sync(int, int) {}
+#endif
+
 /* Jacobian entries as the generated code produces them, before the scaling
  * of BE_Resid_Jac (applied afterwards, one entry per lane): put() stores the
  * value, zero() marks a structural zero. */
@@ -82,6 +93,13 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         RT[N], PREV[N], RPV[N], PV[N], XS[N], MB[2][N], S[6], TD[Net::T_ND], TQ[Net::T_NQ], TS[2];
     __shared__ int Z[N * N], FROW[N], PRB[2][N];
     __shared__ int s_act, s_okr, s_okj, s_bin, s_dense;
+    /* sums of products (Net::SOP): the operands (rates first, so the
+     * interpolation writes them there), the term values, and mdensity,
+     * 1/mdensity and the ge row's and column's structural zeros */
+    constexpr int NTV = Net::SOP_RT > Net::SOP_JT ? Net::SOP_RT : Net::SOP_JT;
+    __shared__ double OPS[Net::SOP ? (Net::SOP_NOPS > NT ? Net::SOP_NOPS : NT) : 1],
+        TV[Net::SOP ? NTV : 1], SMD[5];
+    double *const Rp = Net::SOP ? OPS : R;
     /* mixed: FP32 factors, row and column scale exponents, FP32 pivot rows,
      * the refined solution and residual; s_mix 0 FP64 elimination, 1
      * refining, 2 refined, 3 stopped short; s_fp64: the cell is re-solved
@@ -94,6 +112,27 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
      * writes the next step's slot while slower threads may still read this
      * step's */
     __shared__ int s_mixb[2];
+
+    /* the species and their powers as operands (lanes), and the RHS's or
+     * Jacobian's test for negative values (flag cleared on one) */
+    auto sop_operands = [&](const double *y, int &okflag) {
+        for (int i = tid; i < N; i += 128) {
+            OPS[NT + i] = y[i];
+            if (dg_lt0(y[i])) atomicAnd(&okflag, 0);
+        }
+        for (int k = tid; k < Net::SOP_NPOW; k += 128) {
+            const double x = y[Net::sop_pow_sp(k)];
+            double p;
+            switch (Net::sop_pow_n(k)) {
+            case 2: p = ::dg_ipow<2>(x); break;
+            case 3: p = ::dg_ipow<3>(x); break;
+            case 4: p = ::dg_ipow<4>(x); break;
+            case 5: p = ::dg_ipow<5>(x); break;
+            default: p = ::dg_ipow<6>(x); break;
+            }
+            OPS[NT + N + k] = p;
+        }
+    };
 
     /* thread-0 control state of the CTA's cell */
     long long cell = 0;
@@ -197,6 +236,16 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         rc[4 * N + 5] = fp64cell ? 1.0 : 0.0;
         io.status[cell] = ST_SUSPENDED;
     };
+    if constexpr (Net::SOP) {
+        /* the constant operands, and the Jacobian's structural zeros off
+         * the ge row and column (the tabled and scalar entries leave them) */
+        for (int k = tid; k < Net::SOP_NLIT; k += 128) OPS[Net::SOP_LIT0 + k] = Net::sop_lit(k);
+        if (tid == 0) OPS[Net::SOP_ONE] = 1.0;
+        for (int e = tid; e < N * N; e += 128) {
+            const int v = e / N, q = e - v * N;
+            Z[e] = !Net::jraw(q, v) && q != Net::IGE && v != Net::IGE;
+        }
+    }
     if (tid == 0) {
         cell = (long long)io.order[blockIdx.x];
         active = cell >= 0 && cell_begin(true);
@@ -286,18 +335,65 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
         /* ---- P1: interpolation, one table per lane ---- */
         for (int k = tid; k < NT; k += 128) {
             if (Net::zdep(k)) {
-                R[k] = ts.zvals[k];
+                Rp[k] = ts.zvals[k];
             } else {
                 const double2 pr = __ldg(ts.pairs + (size_t)s_bin * NT + k);
-                R[k] = pr.x + S[2] * pr.y;
+                Rp[k] = pr.x + S[2] * pr.y;
             }
         }
         __syncthreads();
-        /* ---- P2: RHS rows of part w (lane 0 of warp w) ---- */
-        if (l == 0) {
+        if constexpr (Net::SOP) {
+            /* ---- P2a: the species and their powers as operands; any
+             *      negative value fails the RHS ---- */
+            sop_operands(Y, s_okr);
+            if (Net::SOP_RE && tid == 96) SMD[0] = Net::mdensity_of(Y);
+            __syncthreads();
+            /* ---- P2b: warps [0, SOP_RK) the scalar rows, lane 0 each;
+             *      the other warps every term, one per lane, then every
+             *      tabled row's sum, one per lane ---- */
+            if (w < Net::SOP_RK) {
+                if (l == 0) {
+                    double y[N], f[N];
+                    for (int i = 0; i < N; i++) y[i] = Y[i];
+                    const Slots<1> Rs{Rp};
+                    bool ok = true;
+                    switch (w) {
+                    case 0: ok = Net::template rhs_rest<0>(y, Rs, S[0], ts.z, f); break;
+                    case 1: ok = Net::template rhs_rest<1>(y, Rs, S[0], ts.z, f); break;
+                    default: ok = Net::template rhs_rest<2>(y, Rs, S[0], ts.z, f); break;
+                    }
+                    if (ok) {
+                        for (int i = 0; i < N; i++)
+                            if (Net::sop_rpart(i) == w) G[i] = f[i];
+                    } else {
+                        atomicAnd(&s_okr, 0);
+                    }
+                }
+            } else {
+                constexpr int NW = 4 - Net::SOP_RK;
+                const int sl = tid - 32 * Net::SOP_RK;
+                for (int t = sl; t < Net::SOP_RT; t += 32 * NW) {
+                    const int o0 = Net::sop_rterm(t, 0);
+                    double v = OPS[o0 & 0x7fff];
+                    for (int f = 1; f < Net::SOP_FMAX; f++) v = v * OPS[Net::sop_rterm(t, f)];
+                    TV[t] = (o0 & 0x8000) ? -v : v;
+                }
+                if (NW == 1) __syncwarp();
+                else dg_named_sync(1, 32 * NW);
+                for (int e = sl; e < Net::SOP_RE; e += 32 * NW) {
+                    int row, t0, t1, post;
+                    Net::sop_rentry(e, row, t0, t1, post);
+                    double acc = TV[t0];
+                    for (int t = t0 + 1; t < t1; t++) acc = acc + TV[t];
+                    if (post & 1) acc = acc / SMD[0];
+                    G[row] = acc;
+                }
+            }
+        } else if (l == 0) {
+            /* ---- P2: RHS rows of part w (lane 0 of warp w) ---- */
             double y[N], f[N];
             for (int i = 0; i < N; i++) y[i] = Y[i];
-            const Slots<1> Rs{R};
+            const Slots<1> Rs{Rp};
             bool ok = true;
             switch (w) {
             case 0: ok = Net::template rhs<NP, 0>(y, Rs, S[0], ts.z, f); break;
@@ -324,12 +420,73 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
             Y[i] = u * SC[i];
         }
         __syncthreads();
-        /* ---- P4: Jacobian entries of part w (lane 0 of warp w), raw ---- */
         const bool do_j = s_okr != 0;
-        if (do_j && l == 0) {
+        if constexpr (Net::SOP) {
+            /* ---- P4a: operands from the Jacobian's state; mdensity and
+             *      what the ge row and column need ---- */
+            if (do_j) {
+                sop_operands(Y, s_okj);
+                if (tid == 96) {
+                    const double md = Net::mdensity_of(Y);
+                    SMD[1] = md;
+                    SMD[2] = 1.0 / md;
+                    SMD[3] = dg_quot(0.0, md);
+                    SMD[4] = 0.0 * S[1];
+                }
+            }
+            __syncthreads();
+            /* ---- P4b: scalar entries on warps [0, SOP_JK), terms and
+             *      sums on the others, the ge zeros ---- */
+            if (do_j) {
+                if (w < Net::SOP_JK) {
+                    if (l == 0) {
+                        double y[N];
+                        for (int i = 0; i < N; i++) y[i] = Y[i];
+                        const Slots<1> Rs{Rp};
+                        const RawPut<N> put{J, Z};
+                        bool ok = true;
+                        switch (w) {
+                        case 0: ok = Net::template jac_rest<0>(y, Rs, S[1], S[0], ts.z, put); break;
+                        case 1: ok = Net::template jac_rest<1>(y, Rs, S[1], S[0], ts.z, put); break;
+                        default: ok = Net::template jac_rest<2>(y, Rs, S[1], S[0], ts.z, put); break;
+                        }
+                        if (!ok) atomicAnd(&s_okj, 0);
+                    }
+                } else {
+                    constexpr int NW = 4 - Net::SOP_JK;
+                    const int sl = tid - 32 * Net::SOP_JK;
+                    for (int t = sl; t < Net::SOP_JT; t += 32 * NW) {
+                        const int o0 = Net::sop_jterm(t, 0);
+                        double v = OPS[o0 & 0x7fff];
+                        for (int f = 1; f < Net::SOP_FMAX; f++) v = v * OPS[Net::sop_jterm(t, f)];
+                        TV[t] = (o0 & 0x8000) ? -v : v;
+                    }
+                    if (NW == 1) __syncwarp();
+                    else dg_named_sync(2, 32 * NW);
+                    const double md = SMD[1], rmd = SMD[2], Tge = S[1];
+                    for (int e = sl; e < Net::SOP_JE; e += 32 * NW) {
+                        int q, v, t0, t1, post;
+                        Net::sop_jentry(e, q, v, t0, t1, post);
+                        double acc = TV[t0];
+                        for (int t = t0 + 1; t < t1; t++) acc = acc + TV[t];
+                        if (post & 1) acc = dg_div(acc, md, rmd);
+                        if (post & 2) acc = acc * Tge;
+                        J[v * N + q] = acc;
+                    }
+                    /* the ge row's and column's structural zeros: 0/mdensity,
+                     * 0*Tge, and their product on the diagonal */
+                    for (int i = sl; i < N; i += 32 * NW) {
+                        if (!Net::jraw(Net::IGE, i))
+                            J[i * N + Net::IGE] = i == Net::IGE ? SMD[3] * Tge : SMD[3];
+                        if (i != Net::IGE && !Net::jraw(i, Net::IGE)) J[Net::IGE * N + i] = SMD[4];
+                    }
+                }
+            }
+        } else if (do_j && l == 0) {
+            /* ---- P4: Jacobian entries of part w (lane 0 of warp w), raw ---- */
             double y[N];
             for (int i = 0; i < N; i++) y[i] = Y[i];
-            const Slots<1> Rs{R};
+            const Slots<1> Rs{Rp};
             const RawPut<N> put{J, Z};
             bool ok = true;
             switch (w) {

@@ -65,6 +65,8 @@ struct Net {
         return v == 0 ? 0xc003ull : v == 1 ? 0xc003ull : v == 2 ? 0xc00cull : v == 3 ? 0xc01cull : v == 4 ? 0xc018ull : v == 5 ? 0xc060ull : v == 6 ? 0xc0e0ull : v == 7 ? 0xc1c0ull : v == 8 ? 0xc380ull : v == 9 ? 0xc700ull : v == 10 ? 0xce00ull : v == 11 ? 0xdc00ull : v == 12 ? 0xf800ull : v == 13 ? 0xf000ull : v == 14 ? 0xffffull : v == 15 ? 0x0ull : 0ull;
     }
     __host__ __device__ static constexpr bool jnz(int q, int v) { return q == v || ((jnz_col(v) >> q) & 1ull) != 0; }
+    /* structural nonzeros of J itself (d rhs_q / d y_v) */
+    __host__ __device__ static constexpr bool jraw(int q, int v) { return ((jnz_col(v) >> q) & 1ull) != 0; }
 
     static const char *species_name(int i)
     {
@@ -1502,6 +1504,363 @@ struct Net {
             put(15, 15, zero_both);
         }
         return true;
+    }
+
+    /* The RHS rows and Jacobian entries that are flat sums of signed
+     * products, as tables for lane-parallel evaluation (the wide engine).
+     * Operands (a per-cell array): [0, NT) the rates, [NT, NT+N) the
+     * species, then the powers dg_ipow<n>(species) that occur (sop_pow_n,
+     * sop_pow_sp), the literals (sop_lit) and 1.0 (SOP_ONE).  A term is
+     * SOP_FMAX operand indices, multiplied left to right, the first with
+     * bit 15 set when the term is negated; an entry sums its terms
+     * [t0, t1) left to right and applies post (RHS: 1 = / mdensity;
+     * Jacobian: 1 = dg_div by mdensity, 2 = * Tge, after the division) --
+     * the printed expressions' own operations, so the values are theirs bit
+     * for bit.  The other rows and entries (rhs_rest, jac_rest) are the
+     * generated scalar code, in SOP_RK / SOP_JK parts. */
+    static constexpr bool SOP = true;
+    static constexpr int SOP_NOPS = 53, SOP_ONE = 52, SOP_FMAX = 3;
+    static constexpr int SOP_NPOW = 0, SOP_LIT0 = 52, SOP_NLIT = 0;
+    static constexpr int SOP_RT = 80, SOP_RE = 16, SOP_RK = 0;
+    static constexpr int SOP_JT = 160, SOP_JE = 80, SOP_JK = 0;
+    /* the scalar part of RHS row i, -1 for a tabled row */
+    __host__ __device__ static constexpr int sop_rpart(int i)
+    {
+        return -1;
+    }
+    __host__ __device__ static int sop_pow_n(int k)
+    {
+        static const unsigned char T[] = { 0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_pow_sp(int k)
+    {
+        static const unsigned char T[] = { 0 };
+        return T[k];
+    }
+    __host__ __device__ static double sop_lit(int k)
+    {
+        static const double T[] = { 0.0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_rterm(int t, int f)
+    {
+        static const unsigned short T[] = { 32768, 36, 50, 1, 37, 50, 0, 36, 50, 32769, 37, 50, 32770, 38, 50, 4, 39, 50, 2, 38, 50, 32771, 39, 50, 32772, 39, 50, 5, 40, 50, 3, 39, 50, 32773, 40, 50, 32774, 41, 50, 8, 42, 50, 6, 41, 50, 32775, 42, 50, 32776, 42, 50, 10, 43, 50, 7, 42, 50, 32777, 43, 50, 32778, 43, 50, 12, 44, 50, 9, 43, 50, 32779, 44, 50, 32780, 44, 50, 14, 45, 50, 11, 44, 50, 32781, 45, 50, 32782, 45, 50, 16, 46, 50, 13, 45, 50, 32783, 46, 50, 32784, 46, 50, 18, 47, 50, 15, 46, 50, 32785, 47, 50, 32786, 47, 50, 20, 48, 50, 17, 47, 50, 32787, 48, 50, 32788, 48, 50, 21, 49, 50, 19, 48, 50, 32789, 49, 50, 0, 36, 50, 32769, 37, 50, 2, 38, 50, 3, 39, 50, 32772, 39, 50, 32773, 40, 50, 6, 41, 50, 7, 42, 50, 32776, 42, 50, 9, 43, 50, 32778, 43, 50, 11, 44, 50, 32780, 44, 50, 13, 45, 50, 32782, 45, 50, 15, 46, 50, 32784, 46, 50, 17, 47, 50, 32786, 47, 50, 19, 48, 50, 32788, 48, 50, 32789, 49, 50, 32804, 22, 50, 32805, 23, 50, 32806, 24, 50, 32807, 25, 50, 32808, 26, 50, 32809, 27, 50, 32810, 28, 50, 32811, 29, 50, 32812, 30, 50, 32813, 31, 50, 32814, 32, 50, 32815, 33, 50, 32816, 34, 50, 32817, 35, 50, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    __host__ __device__ static int sop_jterm(int t, int f)
+    {
+        static const unsigned short T[] = { 32768, 50, 52, 0, 50, 52, 0, 50, 52, 32790, 50, 52, 1, 50, 52, 32769, 50, 52, 32769, 50, 52, 32791, 50, 52, 32770, 50, 52, 2, 50, 52, 2, 50, 52, 32792, 50, 52, 4, 50, 52, 32771, 50, 52, 32772, 50, 52, 3, 50, 52, 3, 50, 52, 32772, 50, 52, 32793, 50, 52, 5, 50, 52, 32773, 50, 52, 32773, 50, 52, 32794, 50, 52, 32774, 50, 52, 6, 50, 52, 6, 50, 52, 32795, 50, 52, 8, 50, 52, 32775, 50, 52, 32776, 50, 52, 7, 50, 52, 7, 50, 52, 32776, 50, 52, 32796, 50, 52, 10, 50, 52, 32777, 50, 52, 32778, 50, 52, 9, 50, 52, 9, 50, 52, 32778, 50, 52, 32797, 50, 52, 12, 50, 52, 32779, 50, 52, 32780, 50, 52, 11, 50, 52, 11, 50, 52, 32780, 50, 52, 32798, 50, 52, 14, 50, 52, 32781, 50, 52, 32782, 50, 52, 13, 50, 52, 13, 50, 52, 32782, 50, 52, 32799, 50, 52, 16, 50, 52, 32783, 50, 52, 32784, 50, 52, 15, 50, 52, 15, 50, 52, 32784, 50, 52, 32800, 50, 52, 18, 50, 52, 32785, 50, 52, 32786, 50, 52, 17, 50, 52, 17, 50, 52, 32786, 50, 52, 32801, 50, 52, 20, 50, 52, 32787, 50, 52, 32788, 50, 52, 19, 50, 52, 19, 50, 52, 32788, 50, 52, 32802, 50, 52, 21, 50, 52, 32789, 50, 52, 32789, 50, 52, 32803, 50, 52, 32768, 36, 52, 1, 37, 52, 0, 36, 52, 32769, 37, 52, 32770, 38, 52, 4, 39, 52, 2, 38, 52, 32771, 39, 52, 32772, 39, 52, 5, 40, 52, 3, 39, 52, 32773, 40, 52, 32774, 41, 52, 8, 42, 52, 6, 41, 52, 32775, 42, 52, 32776, 42, 52, 10, 43, 52, 7, 42, 52, 32777, 43, 52, 32778, 43, 52, 12, 44, 52, 9, 43, 52, 32779, 44, 52, 32780, 44, 52, 14, 45, 52, 11, 44, 52, 32781, 45, 52, 32782, 45, 52, 16, 46, 52, 13, 45, 52, 32783, 46, 52, 32784, 46, 52, 18, 47, 52, 15, 46, 52, 32785, 47, 52, 32786, 47, 52, 20, 48, 52, 17, 47, 52, 32787, 48, 52, 32788, 48, 52, 21, 49, 52, 19, 48, 52, 32789, 49, 52, 0, 36, 52, 32769, 37, 52, 2, 38, 52, 3, 39, 52, 32772, 39, 52, 32773, 40, 52, 6, 41, 52, 7, 42, 52, 32776, 42, 52, 9, 43, 52, 32778, 43, 52, 11, 44, 52, 32780, 44, 52, 13, 45, 52, 32782, 45, 52, 15, 46, 52, 32784, 46, 52, 17, 47, 52, 32786, 47, 52, 19, 48, 52, 32788, 48, 52, 32789, 49, 52, 32804, 22, 52, 32805, 23, 52, 32806, 24, 52, 32807, 25, 52, 32808, 26, 52, 32809, 27, 52, 32810, 28, 52, 32811, 29, 52, 32812, 30, 52, 32813, 31, 52, 32814, 32, 52, 32815, 33, 52, 32816, 34, 52, 32817, 35, 52, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    /* RHS entry e: row, t0, t1, post */
+    __host__ __device__ static void sop_rentry(int e, int &row, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 2, 0, 1, 2, 4, 0, 2, 4, 6, 0, 3, 6, 10, 0, 4, 10, 12, 0, 5, 12, 14, 0, 6, 14, 18, 0, 7, 18, 22, 0, 8, 22, 26, 0, 9, 26, 30, 0, 10, 30, 34, 0, 11, 34, 38, 0, 12, 38, 42, 0, 13, 42, 44, 0, 14, 44, 66, 0, 15, 66, 80, 1, 0 };
+        row = T[4 * e];
+        t0 = T[4 * e + 1];
+        t1 = T[4 * e + 2];
+        post = T[4 * e + 3];
+    }
+    /* Jacobian entry e: equation q, variable v, t0, t1, post */
+    __host__ __device__ static void sop_jentry(int e, int &q, int &v, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 0, 1, 0, 1, 0, 1, 2, 0, 14, 0, 2, 3, 0, 15, 0, 3, 4, 1, 0, 1, 4, 5, 0, 1, 1, 5, 6, 0, 14, 1, 6, 7, 0, 15, 1, 7, 8, 1, 2, 2, 8, 9, 0, 3, 2, 9, 10, 0, 14, 2, 10, 11, 0, 15, 2, 11, 12, 1, 2, 3, 12, 13, 0, 3, 3, 13, 15, 0, 4, 3, 15, 16, 0, 14, 3, 16, 18, 0, 15, 3, 18, 19, 1, 3, 4, 19, 20, 0, 4, 4, 20, 21, 0, 14, 4, 21, 22, 0, 15, 4, 22, 23, 1, 5, 5, 23, 24, 0, 6, 5, 24, 25, 0, 14, 5, 25, 26, 0, 15, 5, 26, 27, 1, 5, 6, 27, 28, 0, 6, 6, 28, 30, 0, 7, 6, 30, 31, 0, 14, 6, 31, 33, 0, 15, 6, 33, 34, 1, 6, 7, 34, 35, 0, 7, 7, 35, 37, 0, 8, 7, 37, 38, 0, 14, 7, 38, 40, 0, 15, 7, 40, 41, 1, 7, 8, 41, 42, 0, 8, 8, 42, 44, 0, 9, 8, 44, 45, 0, 14, 8, 45, 47, 0, 15, 8, 47, 48, 1, 8, 9, 48, 49, 0, 9, 9, 49, 51, 0, 10, 9, 51, 52, 0, 14, 9, 52, 54, 0, 15, 9, 54, 55, 1, 9, 10, 55, 56, 0, 10, 10, 56, 58, 0, 11, 10, 58, 59, 0, 14, 10, 59, 61, 0, 15, 10, 61, 62, 1, 10, 11, 62, 63, 0, 11, 11, 63, 65, 0, 12, 11, 65, 66, 0, 14, 11, 66, 68, 0, 15, 11, 68, 69, 1, 11, 12, 69, 70, 0, 12, 12, 70, 72, 0, 13, 12, 72, 73, 0, 14, 12, 73, 75, 0, 15, 12, 75, 76, 1, 12, 13, 76, 77, 0, 13, 13, 77, 78, 0, 14, 13, 78, 79, 0, 15, 13, 79, 80, 1, 0, 14, 80, 82, 0, 1, 14, 82, 84, 0, 2, 14, 84, 86, 0, 3, 14, 86, 90, 0, 4, 14, 90, 92, 0, 5, 14, 92, 94, 0, 6, 14, 94, 98, 0, 7, 14, 98, 102, 0, 8, 14, 102, 106, 0, 9, 14, 106, 110, 0, 10, 14, 110, 114, 0, 11, 14, 114, 118, 0, 12, 14, 118, 122, 0, 13, 14, 122, 124, 0, 14, 14, 124, 146, 0, 15, 14, 146, 160, 1, 0 };
+        q = T[5 * e];
+        v = T[5 * e + 1];
+        t0 = T[5 * e + 2];
+        t1 = T[5 * e + 3];
+        post = T[5 * e + 4];
+    }
+
+    /* The RHS rows sop_tables leaves to scalar code, part P of SOP_RK. */
+    template <int P, class RT>
+    __device__ __forceinline__ static bool rhs_rest(const double (&y)[N], const RT &R, double T, double z,
+                                                    double (&f)[N])
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)f;
+        const double H_1 = y[0];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[1];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double He_1 = y[2];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[3];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[4];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double O_1 = y[5];
+        mdensity += O_1;
+        if (dg_lt0(O_1)) return false;   /* O_1 < 0.0 */
+        const double O_2 = y[6];
+        mdensity += O_2;
+        if (dg_lt0(O_2)) return false;   /* O_2 < 0.0 */
+        const double O_3 = y[7];
+        mdensity += O_3;
+        if (dg_lt0(O_3)) return false;   /* O_3 < 0.0 */
+        const double O_4 = y[8];
+        mdensity += O_4;
+        if (dg_lt0(O_4)) return false;   /* O_4 < 0.0 */
+        const double O_5 = y[9];
+        mdensity += O_5;
+        if (dg_lt0(O_5)) return false;   /* O_5 < 0.0 */
+        const double O_6 = y[10];
+        mdensity += O_6;
+        if (dg_lt0(O_6)) return false;   /* O_6 < 0.0 */
+        const double O_7 = y[11];
+        mdensity += O_7;
+        if (dg_lt0(O_7)) return false;   /* O_7 < 0.0 */
+        const double O_8 = y[12];
+        mdensity += O_8;
+        if (dg_lt0(O_8)) return false;   /* O_8 < 0.0 */
+        const double O_9 = y[13];
+        mdensity += O_9;
+        if (dg_lt0(O_9)) return false;   /* O_9 < 0.0 */
+        const double de = y[14];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[15];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        (void)mdensity;
+        const double H_1_i = R[0];
+        (void)H_1_i;
+        const double H_2_r = R[1];
+        (void)H_2_r;
+        const double He_1_i = R[2];
+        (void)He_1_i;
+        const double He_2_i = R[3];
+        (void)He_2_i;
+        const double He_2_r = R[4];
+        (void)He_2_r;
+        const double He_3_r = R[5];
+        (void)He_3_r;
+        const double O_1_i = R[6];
+        (void)O_1_i;
+        const double O_2_i = R[7];
+        (void)O_2_i;
+        const double O_2_r = R[8];
+        (void)O_2_r;
+        const double O_3_i = R[9];
+        (void)O_3_i;
+        const double O_3_r = R[10];
+        (void)O_3_r;
+        const double O_4_i = R[11];
+        (void)O_4_i;
+        const double O_4_r = R[12];
+        (void)O_4_r;
+        const double O_5_i = R[13];
+        (void)O_5_i;
+        const double O_5_r = R[14];
+        (void)O_5_r;
+        const double O_6_i = R[15];
+        (void)O_6_i;
+        const double O_6_r = R[16];
+        (void)O_6_r;
+        const double O_7_i = R[17];
+        (void)O_7_i;
+        const double O_7_r = R[18];
+        (void)O_7_r;
+        const double O_8_i = R[19];
+        (void)O_8_i;
+        const double O_8_r = R[20];
+        (void)O_8_r;
+        const double O_9_r = R[21];
+        (void)O_9_r;
+        const double H_1_c_H_1_c = R[22];
+        (void)H_1_c_H_1_c;
+        const double H_2_c_H_2_c = R[23];
+        (void)H_2_c_H_2_c;
+        const double He_1_c_He_1_c = R[24];
+        (void)He_1_c_He_1_c;
+        const double He_2_c_He_2_c = R[25];
+        (void)He_2_c_He_2_c;
+        const double He_3_c_He_3_c = R[26];
+        (void)He_3_c_He_3_c;
+        const double O_1_c_O_1_c = R[27];
+        (void)O_1_c_O_1_c;
+        const double O_2_c_O_2_c = R[28];
+        (void)O_2_c_O_2_c;
+        const double O_3_c_O_3_c = R[29];
+        (void)O_3_c_O_3_c;
+        const double O_4_c_O_4_c = R[30];
+        (void)O_4_c_O_4_c;
+        const double O_5_c_O_5_c = R[31];
+        (void)O_5_c_O_5_c;
+        const double O_6_c_O_6_c = R[32];
+        (void)O_6_c_O_6_c;
+        const double O_7_c_O_7_c = R[33];
+        (void)O_7_c_O_7_c;
+        const double O_8_c_O_8_c = R[34];
+        (void)O_8_c_O_8_c;
+        const double O_9_c_O_9_c = R[35];
+        (void)O_9_c_O_9_c;
+        return true;
+    }
+
+    /* The Jacobian entries sop_tables leaves to scalar code, part P of
+     * SOP_JK (put() for each). */
+    template <int P, class RT, class Put>
+    __device__ __forceinline__ static bool jac_rest(const double (&y)[N], const RT &R, double Tge, double T,
+                                                    double z, const Put &put)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)Tge; (void)put;
+        const double H_1 = y[0];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[1];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double He_1 = y[2];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[3];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[4];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double O_1 = y[5];
+        mdensity += O_1;
+        if (dg_lt0(O_1)) return false;   /* O_1 < 0.0 */
+        const double O_2 = y[6];
+        mdensity += O_2;
+        if (dg_lt0(O_2)) return false;   /* O_2 < 0.0 */
+        const double O_3 = y[7];
+        mdensity += O_3;
+        if (dg_lt0(O_3)) return false;   /* O_3 < 0.0 */
+        const double O_4 = y[8];
+        mdensity += O_4;
+        if (dg_lt0(O_4)) return false;   /* O_4 < 0.0 */
+        const double O_5 = y[9];
+        mdensity += O_5;
+        if (dg_lt0(O_5)) return false;   /* O_5 < 0.0 */
+        const double O_6 = y[10];
+        mdensity += O_6;
+        if (dg_lt0(O_6)) return false;   /* O_6 < 0.0 */
+        const double O_7 = y[11];
+        mdensity += O_7;
+        if (dg_lt0(O_7)) return false;   /* O_7 < 0.0 */
+        const double O_8 = y[12];
+        mdensity += O_8;
+        if (dg_lt0(O_8)) return false;   /* O_8 < 0.0 */
+        const double O_9 = y[13];
+        mdensity += O_9;
+        if (dg_lt0(O_9)) return false;   /* O_9 < 0.0 */
+        const double de = y[14];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[15];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        const double H_1_i = R[0];
+        (void)H_1_i;
+        const double H_2_r = R[1];
+        (void)H_2_r;
+        const double He_1_i = R[2];
+        (void)He_1_i;
+        const double He_2_i = R[3];
+        (void)He_2_i;
+        const double He_2_r = R[4];
+        (void)He_2_r;
+        const double He_3_r = R[5];
+        (void)He_3_r;
+        const double O_1_i = R[6];
+        (void)O_1_i;
+        const double O_2_i = R[7];
+        (void)O_2_i;
+        const double O_2_r = R[8];
+        (void)O_2_r;
+        const double O_3_i = R[9];
+        (void)O_3_i;
+        const double O_3_r = R[10];
+        (void)O_3_r;
+        const double O_4_i = R[11];
+        (void)O_4_i;
+        const double O_4_r = R[12];
+        (void)O_4_r;
+        const double O_5_i = R[13];
+        (void)O_5_i;
+        const double O_5_r = R[14];
+        (void)O_5_r;
+        const double O_6_i = R[15];
+        (void)O_6_i;
+        const double O_6_r = R[16];
+        (void)O_6_r;
+        const double O_7_i = R[17];
+        (void)O_7_i;
+        const double O_7_r = R[18];
+        (void)O_7_r;
+        const double O_8_i = R[19];
+        (void)O_8_i;
+        const double O_8_r = R[20];
+        (void)O_8_r;
+        const double O_9_r = R[21];
+        (void)O_9_r;
+        const double H_1_c_H_1_c = R[22];
+        (void)H_1_c_H_1_c;
+        const double H_2_c_H_2_c = R[23];
+        (void)H_2_c_H_2_c;
+        const double He_1_c_He_1_c = R[24];
+        (void)He_1_c_He_1_c;
+        const double He_2_c_He_2_c = R[25];
+        (void)He_2_c_He_2_c;
+        const double He_3_c_He_3_c = R[26];
+        (void)He_3_c_He_3_c;
+        const double O_1_c_O_1_c = R[27];
+        (void)O_1_c_O_1_c;
+        const double O_2_c_O_2_c = R[28];
+        (void)O_2_c_O_2_c;
+        const double O_3_c_O_3_c = R[29];
+        (void)O_3_c_O_3_c;
+        const double O_4_c_O_4_c = R[30];
+        (void)O_4_c_O_4_c;
+        const double O_5_c_O_5_c = R[31];
+        (void)O_5_c_O_5_c;
+        const double O_6_c_O_6_c = R[32];
+        (void)O_6_c_O_6_c;
+        const double O_7_c_O_7_c = R[33];
+        (void)O_7_c_O_7_c;
+        const double O_8_c_O_8_c = R[34];
+        (void)O_8_c_O_8_c;
+        const double O_9_c_O_9_c = R[35];
+        (void)O_9_c_O_9_c;
+        const double rmd = 1.0 / mdensity;
+        (void)rmd;
+        double jv;
+        (void)jv;
+        return true;
+    }
+
+    /* mass density of the species counted by the generated code's
+     * `mdensity` (their sum in species order, times mh) */
+    __device__ __forceinline__ static double mdensity_of(const double *y)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        mdensity += y[0];
+        mdensity += y[1];
+        mdensity += y[2];
+        mdensity += y[3];
+        mdensity += y[4];
+        mdensity += y[5];
+        mdensity += y[6];
+        mdensity += y[7];
+        mdensity += y[8];
+        mdensity += y[9];
+        mdensity += y[10];
+        mdensity += y[11];
+        mdensity += y[12];
+        mdensity += y[13];
+        mdensity *= mh;
+        return mdensity;
     }
 
     /* The same Jacobian in extended-range FP32 (dg_xf.h), for the

@@ -65,6 +65,8 @@ struct Net {
         return v == 0 ? 0xc003ull : v == 1 ? 0xc003ull : v == 2 ? 0xc00cull : v == 3 ? 0xc01cull : v == 4 ? 0xc018ull : v == 5 ? 0xc060ull : v == 6 ? 0xc0e0ull : v == 7 ? 0xc1c0ull : v == 8 ? 0xc380ull : v == 9 ? 0xc700ull : v == 10 ? 0xce00ull : v == 11 ? 0xdc00ull : v == 12 ? 0xf800ull : v == 13 ? 0xf000ull : v == 14 ? 0xffffull : v == 15 ? 0x0ull : 0ull;
     }
     __host__ __device__ static constexpr bool jnz(int q, int v) { return q == v || ((jnz_col(v) >> q) & 1ull) != 0; }
+    /* structural nonzeros of J itself (d rhs_q / d y_v) */
+    __host__ __device__ static constexpr bool jraw(int q, int v) { return ((jnz_col(v) >> q) & 1ull) != 0; }
 
     static const char *species_name(int i)
     {
@@ -1612,6 +1614,451 @@ struct Net {
             put(15, 15, zero_both);
         }
         return true;
+    }
+
+    /* The RHS rows and Jacobian entries that are flat sums of signed
+     * products, as tables for lane-parallel evaluation (the wide engine).
+     * Operands (a per-cell array): [0, NT) the rates, [NT, NT+N) the
+     * species, then the powers dg_ipow<n>(species) that occur (sop_pow_n,
+     * sop_pow_sp), the literals (sop_lit) and 1.0 (SOP_ONE).  A term is
+     * SOP_FMAX operand indices, multiplied left to right, the first with
+     * bit 15 set when the term is negated; an entry sums its terms
+     * [t0, t1) left to right and applies post (RHS: 1 = / mdensity;
+     * Jacobian: 1 = dg_div by mdensity, 2 = * Tge, after the division) --
+     * the printed expressions' own operations, so the values are theirs bit
+     * for bit.  The other rows and entries (rhs_rest, jac_rest) are the
+     * generated scalar code, in SOP_RK / SOP_JK parts. */
+    static constexpr bool SOP = true;
+    static constexpr int SOP_NOPS = 75, SOP_ONE = 74, SOP_FMAX = 3;
+    static constexpr int SOP_NPOW = 0, SOP_LIT0 = 74, SOP_NLIT = 0;
+    static constexpr int SOP_RT = 124, SOP_RE = 16, SOP_RK = 0;
+    static constexpr int SOP_JT = 204, SOP_JE = 80, SOP_JK = 0;
+    /* the scalar part of RHS row i, -1 for a tabled row */
+    __host__ __device__ static constexpr int sop_rpart(int i)
+    {
+        return -1;
+    }
+    __host__ __device__ static int sop_pow_n(int k)
+    {
+        static const unsigned char T[] = { 0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_pow_sp(int k)
+    {
+        static const unsigned char T[] = { 0 };
+        return T[k];
+    }
+    __host__ __device__ static double sop_lit(int k)
+    {
+        static const double T[] = { 0.0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_rterm(int t, int f)
+    {
+        static const unsigned short T[] = { 32768, 58, 72, 32769, 58, 74, 2, 59, 72, 0, 58, 72, 1, 58, 74, 32770, 59, 72, 32771, 60, 72, 32772, 60, 74, 7, 61, 72, 3, 60, 72, 4, 60, 74, 32773, 61, 72, 32774, 61, 74, 32775, 61, 72, 8, 62, 72, 5, 61, 72, 6, 61, 74, 32776, 62, 72, 32777, 63, 72, 32778, 63, 74, 13, 64, 72, 9, 63, 72, 10, 63, 74, 32779, 64, 72, 32780, 64, 74, 32781, 64, 72, 16, 65, 72, 11, 64, 72, 12, 64, 74, 32782, 65, 72, 32783, 65, 74, 32784, 65, 72, 19, 66, 72, 14, 65, 72, 15, 65, 74, 32785, 66, 72, 32786, 66, 74, 32787, 66, 72, 22, 67, 72, 17, 66, 72, 18, 66, 74, 32788, 67, 72, 32789, 67, 74, 32790, 67, 72, 25, 68, 72, 20, 67, 72, 21, 67, 74, 32791, 68, 72, 32792, 68, 74, 32793, 68, 72, 28, 69, 72, 23, 68, 72, 24, 68, 74, 32794, 69, 72, 32795, 69, 74, 32796, 69, 72, 31, 70, 72, 26, 69, 72, 27, 69, 74, 32797, 70, 72, 32798, 70, 74, 32799, 70, 72, 32, 71, 72, 29, 70, 72, 30, 70, 74, 32800, 71, 72, 0, 58, 72, 1, 58, 74, 32770, 59, 72, 3, 60, 72, 4, 60, 74, 5, 61, 72, 6, 61, 74, 32775, 61, 72, 32776, 62, 72, 9, 63, 72, 10, 63, 74, 11, 64, 72, 12, 64, 74, 32781, 64, 72, 14, 65, 72, 15, 65, 74, 32784, 65, 72, 17, 66, 72, 18, 66, 74, 32787, 66, 72, 20, 67, 72, 21, 67, 74, 32790, 67, 72, 23, 68, 72, 24, 68, 74, 32793, 68, 72, 26, 69, 72, 27, 69, 74, 32796, 69, 72, 29, 70, 72, 30, 70, 74, 32799, 70, 72, 32800, 71, 72, 32826, 33, 72, 58, 34, 74, 32827, 35, 72, 32828, 36, 72, 60, 37, 74, 32829, 38, 72, 61, 39, 74, 32830, 40, 72, 32831, 41, 72, 63, 42, 74, 32832, 43, 72, 64, 44, 74, 32833, 45, 72, 65, 46, 74, 32834, 47, 72, 66, 48, 74, 32835, 49, 72, 67, 50, 74, 32836, 51, 72, 68, 52, 74, 32837, 53, 72, 69, 54, 74, 32838, 55, 72, 70, 56, 74, 32839, 57, 72, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    __host__ __device__ static int sop_jterm(int t, int f)
+    {
+        static const unsigned short T[] = { 32768, 72, 74, 32769, 74, 74, 0, 72, 74, 1, 74, 74, 0, 72, 74, 1, 74, 74, 32801, 72, 74, 34, 74, 74, 2, 72, 74, 32770, 72, 74, 32770, 72, 74, 32803, 72, 74, 32771, 72, 74, 32772, 74, 74, 3, 72, 74, 4, 74, 74, 3, 72, 74, 4, 74, 74, 32804, 72, 74, 37, 74, 74, 7, 72, 74, 32773, 72, 74, 32774, 74, 74, 32775, 72, 74, 5, 72, 74, 6, 74, 74, 5, 72, 74, 6, 74, 74, 32775, 72, 74, 32806, 72, 74, 39, 74, 74, 8, 72, 74, 32776, 72, 74, 32776, 72, 74, 32808, 72, 74, 32777, 72, 74, 32778, 74, 74, 9, 72, 74, 10, 74, 74, 9, 72, 74, 10, 74, 74, 32809, 72, 74, 42, 74, 74, 13, 72, 74, 32779, 72, 74, 32780, 74, 74, 32781, 72, 74, 11, 72, 74, 12, 74, 74, 11, 72, 74, 12, 74, 74, 32781, 72, 74, 32811, 72, 74, 44, 74, 74, 16, 72, 74, 32782, 72, 74, 32783, 74, 74, 32784, 72, 74, 14, 72, 74, 15, 74, 74, 14, 72, 74, 15, 74, 74, 32784, 72, 74, 32813, 72, 74, 46, 74, 74, 19, 72, 74, 32785, 72, 74, 32786, 74, 74, 32787, 72, 74, 17, 72, 74, 18, 74, 74, 17, 72, 74, 18, 74, 74, 32787, 72, 74, 32815, 72, 74, 48, 74, 74, 22, 72, 74, 32788, 72, 74, 32789, 74, 74, 32790, 72, 74, 20, 72, 74, 21, 74, 74, 20, 72, 74, 21, 74, 74, 32790, 72, 74, 32817, 72, 74, 50, 74, 74, 25, 72, 74, 32791, 72, 74, 32792, 74, 74, 32793, 72, 74, 23, 72, 74, 24, 74, 74, 23, 72, 74, 24, 74, 74, 32793, 72, 74, 32819, 72, 74, 52, 74, 74, 28, 72, 74, 32794, 72, 74, 32795, 74, 74, 32796, 72, 74, 26, 72, 74, 27, 74, 74, 26, 72, 74, 27, 74, 74, 32796, 72, 74, 32821, 72, 74, 54, 74, 74, 31, 72, 74, 32797, 72, 74, 32798, 74, 74, 32799, 72, 74, 29, 72, 74, 30, 74, 74, 29, 72, 74, 30, 74, 74, 32799, 72, 74, 32823, 72, 74, 56, 74, 74, 32, 72, 74, 32800, 72, 74, 32800, 72, 74, 32825, 72, 74, 32768, 58, 74, 2, 59, 74, 0, 58, 74, 32770, 59, 74, 32771, 60, 74, 7, 61, 74, 3, 60, 74, 32773, 61, 74, 32775, 61, 74, 8, 62, 74, 5, 61, 74, 32776, 62, 74, 32777, 63, 74, 13, 64, 74, 9, 63, 74, 32779, 64, 74, 32781, 64, 74, 16, 65, 74, 11, 64, 74, 32782, 65, 74, 32784, 65, 74, 19, 66, 74, 14, 65, 74, 32785, 66, 74, 32787, 66, 74, 22, 67, 74, 17, 66, 74, 32788, 67, 74, 32790, 67, 74, 25, 68, 74, 20, 67, 74, 32791, 68, 74, 32793, 68, 74, 28, 69, 74, 23, 68, 74, 32794, 69, 74, 32796, 69, 74, 31, 70, 74, 26, 69, 74, 32797, 70, 74, 32799, 70, 74, 32, 71, 74, 29, 70, 74, 32800, 71, 74, 0, 58, 74, 32770, 59, 74, 3, 60, 74, 5, 61, 74, 32775, 61, 74, 32776, 62, 74, 9, 63, 74, 11, 64, 74, 32781, 64, 74, 14, 65, 74, 32784, 65, 74, 17, 66, 74, 32787, 66, 74, 20, 67, 74, 32790, 67, 74, 23, 68, 74, 32793, 68, 74, 26, 69, 74, 32796, 69, 74, 29, 70, 74, 32799, 70, 74, 32800, 71, 74, 32826, 33, 74, 32827, 35, 74, 32828, 36, 74, 32829, 38, 74, 32830, 40, 74, 32831, 41, 74, 32832, 43, 74, 32833, 45, 74, 32834, 47, 74, 32835, 49, 74, 32836, 51, 74, 32837, 53, 74, 32838, 55, 74, 32839, 57, 74, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    /* RHS entry e: row, t0, t1, post */
+    __host__ __device__ static void sop_rentry(int e, int &row, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 3, 0, 1, 3, 6, 0, 2, 6, 9, 0, 3, 9, 15, 0, 4, 15, 18, 0, 5, 18, 21, 0, 6, 21, 27, 0, 7, 27, 33, 0, 8, 33, 39, 0, 9, 39, 45, 0, 10, 45, 51, 0, 11, 51, 57, 0, 12, 57, 63, 0, 13, 63, 66, 0, 14, 66, 99, 0, 15, 99, 124, 1, 0 };
+        row = T[4 * e];
+        t0 = T[4 * e + 1];
+        t1 = T[4 * e + 2];
+        post = T[4 * e + 3];
+    }
+    /* Jacobian entry e: equation q, variable v, t0, t1, post */
+    __host__ __device__ static void sop_jentry(int e, int &q, int &v, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 0, 2, 0, 1, 0, 2, 4, 0, 14, 0, 4, 6, 0, 15, 0, 6, 8, 1, 0, 1, 8, 9, 0, 1, 1, 9, 10, 0, 14, 1, 10, 11, 0, 15, 1, 11, 12, 1, 2, 2, 12, 14, 0, 3, 2, 14, 16, 0, 14, 2, 16, 18, 0, 15, 2, 18, 20, 1, 2, 3, 20, 21, 0, 3, 3, 21, 24, 0, 4, 3, 24, 26, 0, 14, 3, 26, 29, 0, 15, 3, 29, 31, 1, 3, 4, 31, 32, 0, 4, 4, 32, 33, 0, 14, 4, 33, 34, 0, 15, 4, 34, 35, 1, 5, 5, 35, 37, 0, 6, 5, 37, 39, 0, 14, 5, 39, 41, 0, 15, 5, 41, 43, 1, 5, 6, 43, 44, 0, 6, 6, 44, 47, 0, 7, 6, 47, 49, 0, 14, 6, 49, 52, 0, 15, 6, 52, 54, 1, 6, 7, 54, 55, 0, 7, 7, 55, 58, 0, 8, 7, 58, 60, 0, 14, 7, 60, 63, 0, 15, 7, 63, 65, 1, 7, 8, 65, 66, 0, 8, 8, 66, 69, 0, 9, 8, 69, 71, 0, 14, 8, 71, 74, 0, 15, 8, 74, 76, 1, 8, 9, 76, 77, 0, 9, 9, 77, 80, 0, 10, 9, 80, 82, 0, 14, 9, 82, 85, 0, 15, 9, 85, 87, 1, 9, 10, 87, 88, 0, 10, 10, 88, 91, 0, 11, 10, 91, 93, 0, 14, 10, 93, 96, 0, 15, 10, 96, 98, 1, 10, 11, 98, 99, 0, 11, 11, 99, 102, 0, 12, 11, 102, 104, 0, 14, 11, 104, 107, 0, 15, 11, 107, 109, 1, 11, 12, 109, 110, 0, 12, 12, 110, 113, 0, 13, 12, 113, 115, 0, 14, 12, 115, 118, 0, 15, 12, 118, 120, 1, 12, 13, 120, 121, 0, 13, 13, 121, 122, 0, 14, 13, 122, 123, 0, 15, 13, 123, 124, 1, 0, 14, 124, 126, 0, 1, 14, 126, 128, 0, 2, 14, 128, 130, 0, 3, 14, 130, 134, 0, 4, 14, 134, 136, 0, 5, 14, 136, 138, 0, 6, 14, 138, 142, 0, 7, 14, 142, 146, 0, 8, 14, 146, 150, 0, 9, 14, 150, 154, 0, 10, 14, 154, 158, 0, 11, 14, 158, 162, 0, 12, 14, 162, 166, 0, 13, 14, 166, 168, 0, 14, 14, 168, 190, 0, 15, 14, 190, 204, 1, 0 };
+        q = T[5 * e];
+        v = T[5 * e + 1];
+        t0 = T[5 * e + 2];
+        t1 = T[5 * e + 3];
+        post = T[5 * e + 4];
+    }
+
+    /* The RHS rows sop_tables leaves to scalar code, part P of SOP_RK. */
+    template <int P, class RT>
+    __device__ __forceinline__ static bool rhs_rest(const double (&y)[N], const RT &R, double T, double z,
+                                                    double (&f)[N])
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)f;
+        const double H_1 = y[0];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[1];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double He_1 = y[2];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[3];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[4];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double O_1 = y[5];
+        mdensity += O_1;
+        if (dg_lt0(O_1)) return false;   /* O_1 < 0.0 */
+        const double O_2 = y[6];
+        mdensity += O_2;
+        if (dg_lt0(O_2)) return false;   /* O_2 < 0.0 */
+        const double O_3 = y[7];
+        mdensity += O_3;
+        if (dg_lt0(O_3)) return false;   /* O_3 < 0.0 */
+        const double O_4 = y[8];
+        mdensity += O_4;
+        if (dg_lt0(O_4)) return false;   /* O_4 < 0.0 */
+        const double O_5 = y[9];
+        mdensity += O_5;
+        if (dg_lt0(O_5)) return false;   /* O_5 < 0.0 */
+        const double O_6 = y[10];
+        mdensity += O_6;
+        if (dg_lt0(O_6)) return false;   /* O_6 < 0.0 */
+        const double O_7 = y[11];
+        mdensity += O_7;
+        if (dg_lt0(O_7)) return false;   /* O_7 < 0.0 */
+        const double O_8 = y[12];
+        mdensity += O_8;
+        if (dg_lt0(O_8)) return false;   /* O_8 < 0.0 */
+        const double O_9 = y[13];
+        mdensity += O_9;
+        if (dg_lt0(O_9)) return false;   /* O_9 < 0.0 */
+        const double de = y[14];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[15];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        (void)mdensity;
+        const double H_1_i = R[0];
+        (void)H_1_i;
+        const double H_1_pi = R[1];
+        (void)H_1_pi;
+        const double H_2_r = R[2];
+        (void)H_2_r;
+        const double He_1_i = R[3];
+        (void)He_1_i;
+        const double He_1_pi = R[4];
+        (void)He_1_pi;
+        const double He_2_i = R[5];
+        (void)He_2_i;
+        const double He_2_pi = R[6];
+        (void)He_2_pi;
+        const double He_2_r = R[7];
+        (void)He_2_r;
+        const double He_3_r = R[8];
+        (void)He_3_r;
+        const double O_1_i = R[9];
+        (void)O_1_i;
+        const double O_1_pi = R[10];
+        (void)O_1_pi;
+        const double O_2_i = R[11];
+        (void)O_2_i;
+        const double O_2_pi = R[12];
+        (void)O_2_pi;
+        const double O_2_r = R[13];
+        (void)O_2_r;
+        const double O_3_i = R[14];
+        (void)O_3_i;
+        const double O_3_pi = R[15];
+        (void)O_3_pi;
+        const double O_3_r = R[16];
+        (void)O_3_r;
+        const double O_4_i = R[17];
+        (void)O_4_i;
+        const double O_4_pi = R[18];
+        (void)O_4_pi;
+        const double O_4_r = R[19];
+        (void)O_4_r;
+        const double O_5_i = R[20];
+        (void)O_5_i;
+        const double O_5_pi = R[21];
+        (void)O_5_pi;
+        const double O_5_r = R[22];
+        (void)O_5_r;
+        const double O_6_i = R[23];
+        (void)O_6_i;
+        const double O_6_pi = R[24];
+        (void)O_6_pi;
+        const double O_6_r = R[25];
+        (void)O_6_r;
+        const double O_7_i = R[26];
+        (void)O_7_i;
+        const double O_7_pi = R[27];
+        (void)O_7_pi;
+        const double O_7_r = R[28];
+        (void)O_7_r;
+        const double O_8_i = R[29];
+        (void)O_8_i;
+        const double O_8_pi = R[30];
+        (void)O_8_pi;
+        const double O_8_r = R[31];
+        (void)O_8_r;
+        const double O_9_r = R[32];
+        (void)O_9_r;
+        const double H_1_c_H_1_c = R[33];
+        (void)H_1_c_H_1_c;
+        const double H_1_ph_H_1_ph = R[34];
+        (void)H_1_ph_H_1_ph;
+        const double H_2_c_H_2_c = R[35];
+        (void)H_2_c_H_2_c;
+        const double He_1_c_He_1_c = R[36];
+        (void)He_1_c_He_1_c;
+        const double He_1_ph_He_1_ph = R[37];
+        (void)He_1_ph_He_1_ph;
+        const double He_2_c_He_2_c = R[38];
+        (void)He_2_c_He_2_c;
+        const double He_2_ph_He_2_ph = R[39];
+        (void)He_2_ph_He_2_ph;
+        const double He_3_c_He_3_c = R[40];
+        (void)He_3_c_He_3_c;
+        const double O_1_c_O_1_c = R[41];
+        (void)O_1_c_O_1_c;
+        const double O_1_ph_O_1_ph = R[42];
+        (void)O_1_ph_O_1_ph;
+        const double O_2_c_O_2_c = R[43];
+        (void)O_2_c_O_2_c;
+        const double O_2_ph_O_2_ph = R[44];
+        (void)O_2_ph_O_2_ph;
+        const double O_3_c_O_3_c = R[45];
+        (void)O_3_c_O_3_c;
+        const double O_3_ph_O_3_ph = R[46];
+        (void)O_3_ph_O_3_ph;
+        const double O_4_c_O_4_c = R[47];
+        (void)O_4_c_O_4_c;
+        const double O_4_ph_O_4_ph = R[48];
+        (void)O_4_ph_O_4_ph;
+        const double O_5_c_O_5_c = R[49];
+        (void)O_5_c_O_5_c;
+        const double O_5_ph_O_5_ph = R[50];
+        (void)O_5_ph_O_5_ph;
+        const double O_6_c_O_6_c = R[51];
+        (void)O_6_c_O_6_c;
+        const double O_6_ph_O_6_ph = R[52];
+        (void)O_6_ph_O_6_ph;
+        const double O_7_c_O_7_c = R[53];
+        (void)O_7_c_O_7_c;
+        const double O_7_ph_O_7_ph = R[54];
+        (void)O_7_ph_O_7_ph;
+        const double O_8_c_O_8_c = R[55];
+        (void)O_8_c_O_8_c;
+        const double O_8_ph_O_8_ph = R[56];
+        (void)O_8_ph_O_8_ph;
+        const double O_9_c_O_9_c = R[57];
+        (void)O_9_c_O_9_c;
+        return true;
+    }
+
+    /* The Jacobian entries sop_tables leaves to scalar code, part P of
+     * SOP_JK (put() for each). */
+    template <int P, class RT, class Put>
+    __device__ __forceinline__ static bool jac_rest(const double (&y)[N], const RT &R, double Tge, double T,
+                                                    double z, const Put &put)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)Tge; (void)put;
+        const double H_1 = y[0];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[1];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double He_1 = y[2];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[3];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[4];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double O_1 = y[5];
+        mdensity += O_1;
+        if (dg_lt0(O_1)) return false;   /* O_1 < 0.0 */
+        const double O_2 = y[6];
+        mdensity += O_2;
+        if (dg_lt0(O_2)) return false;   /* O_2 < 0.0 */
+        const double O_3 = y[7];
+        mdensity += O_3;
+        if (dg_lt0(O_3)) return false;   /* O_3 < 0.0 */
+        const double O_4 = y[8];
+        mdensity += O_4;
+        if (dg_lt0(O_4)) return false;   /* O_4 < 0.0 */
+        const double O_5 = y[9];
+        mdensity += O_5;
+        if (dg_lt0(O_5)) return false;   /* O_5 < 0.0 */
+        const double O_6 = y[10];
+        mdensity += O_6;
+        if (dg_lt0(O_6)) return false;   /* O_6 < 0.0 */
+        const double O_7 = y[11];
+        mdensity += O_7;
+        if (dg_lt0(O_7)) return false;   /* O_7 < 0.0 */
+        const double O_8 = y[12];
+        mdensity += O_8;
+        if (dg_lt0(O_8)) return false;   /* O_8 < 0.0 */
+        const double O_9 = y[13];
+        mdensity += O_9;
+        if (dg_lt0(O_9)) return false;   /* O_9 < 0.0 */
+        const double de = y[14];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[15];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        const double H_1_i = R[0];
+        (void)H_1_i;
+        const double H_1_pi = R[1];
+        (void)H_1_pi;
+        const double H_2_r = R[2];
+        (void)H_2_r;
+        const double He_1_i = R[3];
+        (void)He_1_i;
+        const double He_1_pi = R[4];
+        (void)He_1_pi;
+        const double He_2_i = R[5];
+        (void)He_2_i;
+        const double He_2_pi = R[6];
+        (void)He_2_pi;
+        const double He_2_r = R[7];
+        (void)He_2_r;
+        const double He_3_r = R[8];
+        (void)He_3_r;
+        const double O_1_i = R[9];
+        (void)O_1_i;
+        const double O_1_pi = R[10];
+        (void)O_1_pi;
+        const double O_2_i = R[11];
+        (void)O_2_i;
+        const double O_2_pi = R[12];
+        (void)O_2_pi;
+        const double O_2_r = R[13];
+        (void)O_2_r;
+        const double O_3_i = R[14];
+        (void)O_3_i;
+        const double O_3_pi = R[15];
+        (void)O_3_pi;
+        const double O_3_r = R[16];
+        (void)O_3_r;
+        const double O_4_i = R[17];
+        (void)O_4_i;
+        const double O_4_pi = R[18];
+        (void)O_4_pi;
+        const double O_4_r = R[19];
+        (void)O_4_r;
+        const double O_5_i = R[20];
+        (void)O_5_i;
+        const double O_5_pi = R[21];
+        (void)O_5_pi;
+        const double O_5_r = R[22];
+        (void)O_5_r;
+        const double O_6_i = R[23];
+        (void)O_6_i;
+        const double O_6_pi = R[24];
+        (void)O_6_pi;
+        const double O_6_r = R[25];
+        (void)O_6_r;
+        const double O_7_i = R[26];
+        (void)O_7_i;
+        const double O_7_pi = R[27];
+        (void)O_7_pi;
+        const double O_7_r = R[28];
+        (void)O_7_r;
+        const double O_8_i = R[29];
+        (void)O_8_i;
+        const double O_8_pi = R[30];
+        (void)O_8_pi;
+        const double O_8_r = R[31];
+        (void)O_8_r;
+        const double O_9_r = R[32];
+        (void)O_9_r;
+        const double H_1_c_H_1_c = R[33];
+        (void)H_1_c_H_1_c;
+        const double H_1_ph_H_1_ph = R[34];
+        (void)H_1_ph_H_1_ph;
+        const double H_2_c_H_2_c = R[35];
+        (void)H_2_c_H_2_c;
+        const double He_1_c_He_1_c = R[36];
+        (void)He_1_c_He_1_c;
+        const double He_1_ph_He_1_ph = R[37];
+        (void)He_1_ph_He_1_ph;
+        const double He_2_c_He_2_c = R[38];
+        (void)He_2_c_He_2_c;
+        const double He_2_ph_He_2_ph = R[39];
+        (void)He_2_ph_He_2_ph;
+        const double He_3_c_He_3_c = R[40];
+        (void)He_3_c_He_3_c;
+        const double O_1_c_O_1_c = R[41];
+        (void)O_1_c_O_1_c;
+        const double O_1_ph_O_1_ph = R[42];
+        (void)O_1_ph_O_1_ph;
+        const double O_2_c_O_2_c = R[43];
+        (void)O_2_c_O_2_c;
+        const double O_2_ph_O_2_ph = R[44];
+        (void)O_2_ph_O_2_ph;
+        const double O_3_c_O_3_c = R[45];
+        (void)O_3_c_O_3_c;
+        const double O_3_ph_O_3_ph = R[46];
+        (void)O_3_ph_O_3_ph;
+        const double O_4_c_O_4_c = R[47];
+        (void)O_4_c_O_4_c;
+        const double O_4_ph_O_4_ph = R[48];
+        (void)O_4_ph_O_4_ph;
+        const double O_5_c_O_5_c = R[49];
+        (void)O_5_c_O_5_c;
+        const double O_5_ph_O_5_ph = R[50];
+        (void)O_5_ph_O_5_ph;
+        const double O_6_c_O_6_c = R[51];
+        (void)O_6_c_O_6_c;
+        const double O_6_ph_O_6_ph = R[52];
+        (void)O_6_ph_O_6_ph;
+        const double O_7_c_O_7_c = R[53];
+        (void)O_7_c_O_7_c;
+        const double O_7_ph_O_7_ph = R[54];
+        (void)O_7_ph_O_7_ph;
+        const double O_8_c_O_8_c = R[55];
+        (void)O_8_c_O_8_c;
+        const double O_8_ph_O_8_ph = R[56];
+        (void)O_8_ph_O_8_ph;
+        const double O_9_c_O_9_c = R[57];
+        (void)O_9_c_O_9_c;
+        const double rmd = 1.0 / mdensity;
+        (void)rmd;
+        double jv;
+        (void)jv;
+        return true;
+    }
+
+    /* mass density of the species counted by the generated code's
+     * `mdensity` (their sum in species order, times mh) */
+    __device__ __forceinline__ static double mdensity_of(const double *y)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        mdensity += y[0];
+        mdensity += y[1];
+        mdensity += y[2];
+        mdensity += y[3];
+        mdensity += y[4];
+        mdensity += y[5];
+        mdensity += y[6];
+        mdensity += y[7];
+        mdensity += y[8];
+        mdensity += y[9];
+        mdensity += y[10];
+        mdensity += y[11];
+        mdensity += y[12];
+        mdensity += y[13];
+        mdensity *= mh;
+        return mdensity;
     }
 
     /* The same Jacobian in extended-range FP32 (dg_xf.h), for the

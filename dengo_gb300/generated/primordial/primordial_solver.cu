@@ -61,6 +61,8 @@ struct Net {
         return v == 0 ? 0x20full : v == 1 ? 0x11full : v == 2 ? 0x31full : v == 3 ? 0x31full : v == 4 ? 0x11full : v == 5 ? 0x360ull : v == 6 ? 0x3e0ull : v == 7 ? 0x3c0ull : v == 8 ? 0x3ffull : v == 9 ? 0x0ull : 0ull;
     }
     __host__ __device__ static constexpr bool jnz(int q, int v) { return q == v || ((jnz_col(v) >> q) & 1ull) != 0; }
+    /* structural nonzeros of J itself (d rhs_q / d y_v) */
+    __host__ __device__ static constexpr bool jraw(int q, int v) { return ((jnz_col(v) >> q) & 1ull) != 0; }
 
     static const char *species_name(int i)
     {
@@ -958,6 +960,382 @@ struct Net {
             put(9, 9, zero_both);
         }
         return true;
+    }
+
+    /* The RHS rows and Jacobian entries that are flat sums of signed
+     * products, as tables for lane-parallel evaluation (the wide engine).
+     * Operands (a per-cell array): [0, NT) the rates, [NT, NT+N) the
+     * species, then the powers dg_ipow<n>(species) that occur (sop_pow_n,
+     * sop_pow_sp), the literals (sop_lit) and 1.0 (SOP_ONE).  A term is
+     * SOP_FMAX operand indices, multiplied left to right, the first with
+     * bit 15 set when the term is negated; an entry sums its terms
+     * [t0, t1) left to right and applies post (RHS: 1 = / mdensity;
+     * Jacobian: 1 = dg_div by mdensity, 2 = * Tge, after the division) --
+     * the printed expressions' own operations, so the values are theirs bit
+     * for bit.  The other rows and entries (rhs_rest, jac_rest) are the
+     * generated scalar code, in SOP_RK / SOP_JK parts. */
+    static constexpr bool SOP = true;
+    static constexpr int SOP_NOPS = 64, SOP_ONE = 63, SOP_FMAX = 4;
+    static constexpr int SOP_NPOW = 4, SOP_LIT0 = 58, SOP_NLIT = 5;
+    static constexpr int SOP_RT = 66, SOP_RE = 9, SOP_RK = 1;
+    static constexpr int SOP_JT = 137, SOP_JE = 49, SOP_JK = 3;
+    /* the scalar part of RHS row i, -1 for a tabled row */
+    __host__ __device__ static constexpr int sop_rpart(int i)
+    {
+        return i == 9 ? 0 : -1;
+    }
+    __host__ __device__ static int sop_pow_n(int k)
+    {
+        static const unsigned char T[] = { 2, 2, 2, 3, 0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_pow_sp(int k)
+    {
+        static const unsigned char T[] = { 0, 2, 8, 2, 0 };
+        return T[k];
+    }
+    __host__ __device__ static double sop_lit(int k)
+    {
+        static const double T[] = { 2.0, 4.0, 3.0, 6.0, 4.0, 0.0 };
+        return T[k];
+    }
+    __host__ __device__ static int sop_rterm(int t, int f)
+    {
+        static const unsigned short T[] = { 7, 46, 48, 63, 9, 45, 46, 63, 32778, 44, 47, 63, 32779, 44, 52, 63, 32780, 44, 46, 63, 18, 45, 48, 63, 19, 44, 55, 63, 20, 57, 63, 63, 32789, 54, 63, 63, 8, 46, 47, 63, 32777, 45, 46, 63, 10, 44, 47, 63, 16, 47, 48, 63, 32785, 45, 52, 63, 32786, 45, 48, 63, 32768, 46, 52, 63, 1, 47, 52, 63, 32774, 46, 52, 63, 32775, 46, 48, 63, 32776, 46, 47, 63, 32777, 45, 46, 63, 10, 44, 47, 63, 58, 12, 44, 46, 13, 48, 52, 63, 14, 46, 48, 63, 58, 15, 47, 48, 58, 17, 45, 52, 18, 45, 48, 63, 32826, 19, 44, 55, 32826, 20, 57, 63, 58, 21, 54, 63, 0, 46, 52, 63, 32769, 47, 52, 63, 32776, 46, 47, 63, 9, 45, 46, 63, 32778, 44, 47, 63, 58, 11, 44, 52, 32783, 47, 48, 63, 32784, 47, 48, 63, 6, 46, 52, 63, 32775, 46, 48, 63, 32781, 48, 52, 63, 32782, 46, 48, 63, 32783, 47, 48, 63, 32784, 47, 48, 63, 32786, 45, 48, 63, 32770, 49, 52, 63, 3, 50, 52, 63, 2, 49, 52, 63, 32771, 50, 52, 63, 32772, 50, 52, 63, 5, 51, 52, 63, 4, 50, 52, 63, 32773, 51, 52, 63, 0, 46, 52, 63, 32769, 47, 52, 63, 2, 49, 52, 63, 32771, 50, 52, 63, 4, 50, 52, 63, 32773, 51, 52, 63, 32774, 46, 52, 63, 7, 46, 48, 63, 13, 48, 52, 63, 14, 46, 48, 63, 16, 47, 48, 63, 32785, 45, 52, 63, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    __host__ __device__ static int sop_jterm(int t, int f)
+    {
+        static const unsigned short T[] = { 32778, 47, 63, 63, 32779, 52, 63, 63, 32780, 46, 63, 63, 19, 55, 63, 63, 32826, 21, 44, 63, 10, 47, 63, 63, 10, 47, 63, 63, 58, 12, 46, 63, 32826, 19, 55, 63, 59, 21, 44, 63, 32778, 47, 63, 63, 58, 11, 52, 63, 9, 46, 63, 63, 18, 48, 63, 63, 32777, 46, 63, 63, 32785, 52, 63, 63, 32786, 48, 63, 63, 32777, 46, 63, 63, 58, 17, 52, 63, 18, 48, 63, 63, 9, 46, 63, 63, 32786, 48, 63, 63, 32785, 52, 63, 63, 7, 48, 63, 63, 9, 45, 63, 63, 32780, 44, 63, 63, 58, 19, 44, 46, 60, 20, 55, 63, 8, 47, 63, 63, 32777, 45, 63, 63, 32768, 52, 63, 63, 32774, 52, 63, 63, 32775, 48, 63, 63, 32776, 47, 63, 63, 32777, 45, 63, 63, 58, 12, 44, 63, 14, 48, 63, 63, 32827, 19, 44, 46, 32829, 20, 55, 63, 0, 52, 63, 63, 32776, 47, 63, 63, 9, 45, 63, 63, 6, 52, 63, 63, 32775, 48, 63, 63, 32782, 48, 63, 63, 0, 52, 63, 63, 32774, 52, 63, 63, 7, 48, 63, 63, 14, 48, 63, 63, 32778, 44, 63, 63, 8, 46, 63, 63, 10, 44, 63, 63, 16, 48, 63, 63, 1, 52, 63, 63, 32776, 46, 63, 63, 10, 44, 63, 63, 58, 15, 48, 63, 32769, 52, 63, 63, 32776, 46, 63, 63, 32778, 44, 63, 63, 32783, 48, 63, 63, 32784, 48, 63, 63, 32783, 48, 63, 63, 32784, 48, 63, 63, 32769, 52, 63, 63, 16, 48, 63, 63, 7, 46, 63, 63, 18, 45, 63, 63, 16, 47, 63, 63, 32786, 45, 63, 63, 32775, 46, 63, 63, 13, 52, 63, 63, 14, 46, 63, 63, 58, 15, 47, 63, 18, 45, 63, 63, 32783, 47, 63, 63, 32784, 47, 63, 63, 32775, 46, 63, 63, 32781, 52, 63, 63, 32782, 46, 63, 63, 32783, 47, 63, 63, 32784, 47, 63, 63, 32786, 45, 63, 63, 7, 46, 63, 63, 13, 52, 63, 63, 14, 46, 63, 63, 16, 47, 63, 63, 32770, 52, 63, 63, 2, 52, 63, 63, 2, 52, 63, 63, 3, 52, 63, 63, 32771, 52, 63, 63, 32772, 52, 63, 63, 4, 52, 63, 63, 32771, 52, 63, 63, 4, 52, 63, 63, 32790, 52, 63, 63, 32793, 52, 63, 63, 32792, 56, 63, 63, 32796, 52, 63, 63, 32797, 56, 63, 63, 32820, 41, 63, 63, 32820, 42, 63, 63, 5, 52, 63, 63, 32773, 52, 63, 63, 32773, 52, 63, 63, 32830, 22, 52, 63, 32820, 43, 63, 63, 32779, 44, 63, 63, 32785, 45, 63, 63, 32768, 46, 63, 63, 1, 47, 63, 63, 32774, 46, 63, 63, 13, 48, 63, 63, 58, 17, 45, 63, 0, 46, 63, 63, 32769, 47, 63, 63, 58, 11, 44, 63, 6, 46, 63, 63, 32781, 48, 63, 63, 32770, 49, 63, 63, 3, 50, 63, 63, 2, 49, 63, 63, 32771, 50, 63, 63, 32772, 50, 63, 63, 5, 51, 63, 63, 4, 50, 63, 63, 32773, 51, 63, 63, 0, 46, 63, 63, 32769, 47, 63, 63, 2, 49, 63, 63, 32771, 50, 63, 63, 4, 50, 63, 63, 32773, 51, 63, 63, 32774, 46, 63, 63, 13, 48, 63, 63, 32785, 45, 63, 63, 0 };
+        return T[t * SOP_FMAX + f];
+    }
+    /* RHS entry e: row, t0, t1, post */
+    __host__ __device__ static void sop_rentry(int e, int &row, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 9, 0, 1, 9, 15, 0, 2, 15, 31, 0, 3, 31, 39, 0, 4, 39, 46, 0, 5, 46, 48, 0, 6, 48, 52, 0, 7, 52, 54, 0, 8, 54, 66, 0, 0 };
+        row = T[4 * e];
+        t0 = T[4 * e + 1];
+        t1 = T[4 * e + 2];
+        post = T[4 * e + 3];
+    }
+    /* Jacobian entry e: equation q, variable v, t0, t1, post */
+    __host__ __device__ static void sop_jentry(int e, int &q, int &v, int &t0, int &t1, int &post)
+    {
+        static const unsigned short T[] = { 0, 0, 0, 5, 0, 1, 0, 5, 6, 0, 2, 0, 6, 10, 0, 3, 0, 10, 12, 0, 0, 1, 12, 14, 0, 1, 1, 14, 17, 0, 2, 1, 17, 20, 0, 3, 1, 20, 21, 0, 4, 1, 21, 22, 0, 8, 1, 22, 23, 0, 0, 2, 23, 28, 0, 1, 2, 28, 30, 0, 2, 2, 30, 39, 0, 3, 2, 39, 42, 0, 4, 2, 42, 45, 0, 8, 2, 45, 49, 0, 0, 3, 49, 50, 0, 1, 3, 50, 53, 0, 2, 3, 53, 57, 0, 3, 3, 57, 62, 0, 4, 3, 62, 64, 0, 8, 3, 64, 66, 0, 0, 4, 66, 68, 0, 1, 4, 68, 70, 0, 2, 4, 70, 75, 0, 3, 4, 75, 77, 0, 4, 4, 77, 83, 0, 8, 4, 83, 87, 0, 5, 5, 87, 88, 0, 6, 5, 88, 89, 0, 8, 5, 89, 90, 0, 5, 6, 90, 91, 0, 6, 6, 91, 93, 0, 7, 6, 93, 94, 0, 8, 6, 94, 96, 0, 9, 6, 96, 103, 1, 6, 7, 103, 104, 0, 7, 7, 104, 105, 0, 8, 7, 105, 106, 0, 9, 7, 106, 108, 1, 0, 8, 108, 109, 0, 1, 8, 109, 110, 0, 2, 8, 110, 115, 0, 3, 8, 115, 118, 0, 4, 8, 118, 120, 0, 5, 8, 120, 122, 0, 6, 8, 122, 126, 0, 7, 8, 126, 128, 0, 8, 8, 128, 137, 0, 0 };
+        q = T[5 * e];
+        v = T[5 * e + 1];
+        t0 = T[5 * e + 2];
+        t1 = T[5 * e + 3];
+        post = T[5 * e + 4];
+    }
+
+    /* The RHS rows sop_tables leaves to scalar code, part P of SOP_RK. */
+    template <int P, class RT>
+    __device__ __forceinline__ static bool rhs_rest(const double (&y)[N], const RT &R, double T, double z,
+                                                    double (&f)[N])
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)f;
+        const double H2_1 = y[0];
+        mdensity += H2_1;
+        if (dg_lt0(H2_1)) return false;   /* H2_1 < 0.0 */
+        const double H2_2 = y[1];
+        mdensity += H2_2;
+        if (dg_lt0(H2_2)) return false;   /* H2_2 < 0.0 */
+        const double H_1 = y[2];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[3];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double H_m0 = y[4];
+        mdensity += H_m0;
+        if (dg_lt0(H_m0)) return false;   /* H_m0 < 0.0 */
+        const double He_1 = y[5];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[6];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[7];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double de = y[8];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[9];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        (void)mdensity;
+        const double k01 = R[0];
+        (void)k01;
+        const double k02 = R[1];
+        (void)k02;
+        const double k03 = R[2];
+        (void)k03;
+        const double k04 = R[3];
+        (void)k04;
+        const double k05 = R[4];
+        (void)k05;
+        const double k06 = R[5];
+        (void)k06;
+        const double k07 = R[6];
+        (void)k07;
+        const double k08 = R[7];
+        (void)k08;
+        const double k09 = R[8];
+        (void)k09;
+        const double k10 = R[9];
+        (void)k10;
+        const double k11 = R[10];
+        (void)k11;
+        const double k12 = R[11];
+        (void)k12;
+        const double k13 = R[12];
+        (void)k13;
+        const double k14 = R[13];
+        (void)k14;
+        const double k15 = R[14];
+        (void)k15;
+        const double k16 = R[15];
+        (void)k16;
+        const double k17 = R[16];
+        (void)k17;
+        const double k18 = R[17];
+        (void)k18;
+        const double k19 = R[18];
+        (void)k19;
+        const double k21 = R[19];
+        (void)k21;
+        const double k22 = R[20];
+        (void)k22;
+        const double k23 = R[21];
+        (void)k23;
+        const double brem_brem = R[22];
+        (void)brem_brem;
+        const double ceHI_ceHI = R[23];
+        (void)ceHI_ceHI;
+        const double ceHeI_ceHeI = R[24];
+        (void)ceHeI_ceHeI;
+        const double ceHeII_ceHeII = R[25];
+        (void)ceHeII_ceHeII;
+        const double ciHI_ciHI = R[26];
+        (void)ciHI_ciHI;
+        const double ciHeI_ciHeI = R[27];
+        (void)ciHeI_ciHeI;
+        const double ciHeII_ciHeII = R[28];
+        (void)ciHeII_ciHeII;
+        const double ciHeIS_ciHeIS = R[29];
+        (void)ciHeIS_ciHeIS;
+        const double gammah_gammah = R[30];
+        (void)gammah_gammah;
+        const double gloverabel08_gaH2 = R[31];
+        (void)gloverabel08_gaH2;
+        const double gloverabel08_gaHI = R[32];
+        (void)gloverabel08_gaHI;
+        const double gloverabel08_gaHe = R[33];
+        (void)gloverabel08_gaHe;
+        const double gloverabel08_gaHp = R[34];
+        (void)gloverabel08_gaHp;
+        const double gloverabel08_gael = R[35];
+        (void)gloverabel08_gael;
+        const double gloverabel08_gphdl = R[36];
+        (void)gloverabel08_gphdl;
+        const double gloverabel08_gpldl = R[37];
+        (void)gloverabel08_gpldl;
+        const double h2formation_h2mcool = R[38];
+        (void)h2formation_h2mcool;
+        const double h2formation_h2mheat = R[39];
+        (void)h2formation_h2mheat;
+        const double reHII_reHII = R[40];
+        (void)reHII_reHII;
+        const double reHeII1_reHeII1 = R[41];
+        (void)reHeII1_reHeII1;
+        const double reHeII2_reHeII2 = R[42];
+        (void)reHeII2_reHeII2;
+        const double reHeIII_reHeIII = R[43];
+        (void)reHeIII_reHeIII;
+        if (0 == P) {
+            f[9] = -H2_1*H_1*h2formation_h2mcool - H2_1*gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0) + dg_ipow<3>(H_1)*h2formation_h2mheat - H_1*ceHI_ceHI*de - H_1*ciHI_ciHI*de - H_2*de*reHII_reHII - He_1*ciHeI_ciHeI*de - He_2*ceHeII_ceHeII*de - He_2*ceHeI_ceHeI*dg_ipow<2>(de) - He_2*ciHeII_ciHeII*de - He_2*ciHeIS_ciHeIS*dg_ipow<2>(de) - He_2*de*reHeII1_reHeII1 - He_2*de*reHeII2_reHeII2 - He_3*de*reHeIII_reHeIII - brem_brem*de*(H_2 + He_2 + 4.0*He_3);
+            f[9] /= mdensity;
+        }
+        return true;
+    }
+
+    /* The Jacobian entries sop_tables leaves to scalar code, part P of
+     * SOP_JK (put() for each). */
+    template <int P, class RT, class Put>
+    __device__ __forceinline__ static bool jac_rest(const double (&y)[N], const RT &R, double Tge, double T,
+                                                    double z, const Put &put)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        (void)T; (void)z; (void)Tge; (void)put;
+        const double H2_1 = y[0];
+        mdensity += H2_1;
+        if (dg_lt0(H2_1)) return false;   /* H2_1 < 0.0 */
+        const double H2_2 = y[1];
+        mdensity += H2_2;
+        if (dg_lt0(H2_2)) return false;   /* H2_2 < 0.0 */
+        const double H_1 = y[2];
+        mdensity += H_1;
+        if (dg_lt0(H_1)) return false;   /* H_1 < 0.0 */
+        const double H_2 = y[3];
+        mdensity += H_2;
+        if (dg_lt0(H_2)) return false;   /* H_2 < 0.0 */
+        const double H_m0 = y[4];
+        mdensity += H_m0;
+        if (dg_lt0(H_m0)) return false;   /* H_m0 < 0.0 */
+        const double He_1 = y[5];
+        mdensity += He_1;
+        if (dg_lt0(He_1)) return false;   /* He_1 < 0.0 */
+        const double He_2 = y[6];
+        mdensity += He_2;
+        if (dg_lt0(He_2)) return false;   /* He_2 < 0.0 */
+        const double He_3 = y[7];
+        mdensity += He_3;
+        if (dg_lt0(He_3)) return false;   /* He_3 < 0.0 */
+        const double de = y[8];
+        if (dg_lt0(de)) return false;   /* de < 0.0 */
+        const double ge = y[9];
+        if (dg_lt0(ge)) return false;   /* ge < 0.0 */
+        mdensity *= mh;
+        const double k01 = R[0];
+        (void)k01;
+        const double k02 = R[1];
+        (void)k02;
+        const double k03 = R[2];
+        (void)k03;
+        const double k04 = R[3];
+        (void)k04;
+        const double k05 = R[4];
+        (void)k05;
+        const double k06 = R[5];
+        (void)k06;
+        const double k07 = R[6];
+        (void)k07;
+        const double k08 = R[7];
+        (void)k08;
+        const double k09 = R[8];
+        (void)k09;
+        const double k10 = R[9];
+        (void)k10;
+        const double k11 = R[10];
+        (void)k11;
+        const double k12 = R[11];
+        (void)k12;
+        const double k13 = R[12];
+        (void)k13;
+        const double k14 = R[13];
+        (void)k14;
+        const double k15 = R[14];
+        (void)k15;
+        const double k16 = R[15];
+        (void)k16;
+        const double k17 = R[16];
+        (void)k17;
+        const double k18 = R[17];
+        (void)k18;
+        const double k19 = R[18];
+        (void)k19;
+        const double k21 = R[19];
+        (void)k21;
+        const double k22 = R[20];
+        (void)k22;
+        const double k23 = R[21];
+        (void)k23;
+        const double brem_brem = R[22];
+        (void)brem_brem;
+        const double ceHI_ceHI = R[23];
+        (void)ceHI_ceHI;
+        const double ceHeI_ceHeI = R[24];
+        (void)ceHeI_ceHeI;
+        const double ceHeII_ceHeII = R[25];
+        (void)ceHeII_ceHeII;
+        const double ciHI_ciHI = R[26];
+        (void)ciHI_ciHI;
+        const double ciHeI_ciHeI = R[27];
+        (void)ciHeI_ciHeI;
+        const double ciHeII_ciHeII = R[28];
+        (void)ciHeII_ciHeII;
+        const double ciHeIS_ciHeIS = R[29];
+        (void)ciHeIS_ciHeIS;
+        const double gammah_gammah = R[30];
+        (void)gammah_gammah;
+        const double gloverabel08_gaH2 = R[31];
+        (void)gloverabel08_gaH2;
+        const double gloverabel08_gaHI = R[32];
+        (void)gloverabel08_gaHI;
+        const double gloverabel08_gaHe = R[33];
+        (void)gloverabel08_gaHe;
+        const double gloverabel08_gaHp = R[34];
+        (void)gloverabel08_gaHp;
+        const double gloverabel08_gael = R[35];
+        (void)gloverabel08_gael;
+        const double gloverabel08_gphdl = R[36];
+        (void)gloverabel08_gphdl;
+        const double gloverabel08_gpldl = R[37];
+        (void)gloverabel08_gpldl;
+        const double h2formation_h2mcool = R[38];
+        (void)h2formation_h2mcool;
+        const double h2formation_h2mheat = R[39];
+        (void)h2formation_h2mheat;
+        const double reHII_reHII = R[40];
+        (void)reHII_reHII;
+        const double reHeII1_reHeII1 = R[41];
+        (void)reHeII1_reHeII1;
+        const double reHeII2_reHeII2 = R[42];
+        (void)reHeII2_reHeII2;
+        const double reHeIII_reHeIII = R[43];
+        (void)reHeIII_reHeIII;
+        const double rmd = 1.0 / mdensity;
+        (void)rmd;
+        double jv;
+        (void)jv;
+        if (1 == P) {
+            jv = -H2_1*gloverabel08_gaH2*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*h2formation_h2mcool - gloverabel08_gphdl/(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0);
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 0, jv);
+        }
+        if (2 == P) {
+            jv = -H2_1*gloverabel08_gaHI*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H2_1*h2formation_h2mcool + 3*dg_ipow<2>(H_1)*h2formation_h2mheat - ceHI_ceHI*de - ciHI_ciHI*de;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 2, jv);
+        }
+        if (2 == P) {
+            jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 3, jv);
+        }
+        if (1 == P) {
+            jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 5, jv);
+        }
+        if (0 == P) {
+            jv = -H2_1*gloverabel08_gael*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - H_1*ceHI_ceHI - H_1*ciHI_ciHI - H_2*reHII_reHII - He_1*ciHeI_ciHeI - He_2*ceHeII_ceHeII - 2*He_2*ceHeI_ceHeI*de - He_2*ciHeII_ciHeII - 2*He_2*ciHeIS_ciHeIS*de - He_2*reHeII1_reHeII1 - He_2*reHeII2_reHeII2 - He_3*reHeIII_reHeIII - brem_brem*(H_2 + He_2 + 4.0*He_3);
+            jv = dg_div(jv, mdensity, rmd);
+            put(9, 8, jv);
+        }
+        return true;
+    }
+
+    /* mass density of the species counted by the generated code's
+     * `mdensity` (their sum in species order, times mh) */
+    __device__ __forceinline__ static double mdensity_of(const double *y)
+    {
+        const double mh = 1.67e-24;
+        double mdensity = 0.0;
+        mdensity += y[0];
+        mdensity += y[1];
+        mdensity += y[2];
+        mdensity += y[3];
+        mdensity += y[4];
+        mdensity += y[5];
+        mdensity += y[6];
+        mdensity += y[7];
+        mdensity *= mh;
+        return mdensity;
     }
 
     /* The same Jacobian in extended-range FP32 (dg_xf.h), for the

@@ -142,12 +142,32 @@ struct hx_barrier {
 };
 static hx_barrier *hx_cta;      /* all lanes of the CTA */
 static hx_barrier *hx_warp[32];  /* the 32 lanes of each warp */
+/* named barriers (bar.sync id, n): made by their first caller */
+static hx_barrier *hx_named[16];
+static std::mutex hx_named_lock;
+#define DG_HOST_NAMED_SYNC
+namespace dg {
+static void dg_named_sync(int id, int n)
+{
+    hx_barrier *b;
+    {
+        std::lock_guard<std::mutex> g(hx_named_lock);
+        if (!hx_named[id]) hx_named[id] = new hx_barrier(n);
+        b = hx_named[id];
+    }
+    b->arrive_and_wait();
+}
+}
 /* A CTA of `threads` lanes (a multiple of 32): its barrier and one per warp. */
 static void hx_setup(int threads)
 {
     static std::vector<hx_barrier *> keep;
     for (hx_barrier *b : keep) delete b;
     keep.clear();
+    for (int i = 0; i < 16; i++) {
+        if (hx_named[i]) keep.push_back(hx_named[i]);
+        hx_named[i] = nullptr;
+    }
     hx_cta = new hx_barrier(threads);
     keep.push_back(hx_cta);
     for (int w = 0; w < (threads + 31) / 32; w++) {
