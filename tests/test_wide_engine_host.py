@@ -118,3 +118,26 @@ def test_wide_resume_nonfinite_scale(libs, tables):
     assert split["sweeps"][3] > 20 and split["status"][3] == 2
     assert wide["resumed"] == split["resumed"]
     _same(wide, split)
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_wide_oxygen_equals_split(tmp_path_factory, mixed):
+    """The 16-equation ion network, every RHS row and Jacobian entry from the
+    sum-of-products tables (no scalar parts): four of the golden input cells
+    set aside after 20 sweeps and resumed on the wide engine equal the split
+    engine's, FP64 and mixed."""
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "oxygen_golden.npz")))
+    t = read_table_file(os.path.join(network_dir("oxygen"), "oxygen_tables.dgt"))
+    tabs = [np.ascontiguousarray(t[k]) for k in g["table_order"]]
+    d = tmp_path_factory.mktemp("wide_oxygen")
+    split_so = he.compile_engine("oxygen", d, engine="split")
+    wide_so = he.compile_engine("oxygen", d, engine="wide")
+    st, dtf = g["evolve_in"][:4], np.asarray(g["evolve_dtf"])[:4]
+    split = he.evolve_in_subprocess(split_so, tabs, st, dtf, timeout=900, sweep_budget=20,
+                                    mixed=mixed)
+    wide = he.evolve_in_subprocess(wide_so, tabs, st, dtf, timeout=900, sweep_budget=20,
+                                   mixed=mixed)
+    assert wide["resumed"] > 0 and wide["resumed"] == split["resumed"]
+    _same(wide, split)
