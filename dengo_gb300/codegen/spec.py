@@ -309,6 +309,135 @@ def sop_tables(species, tables, rhs_dev, jac_dev, jac_nz):
             "jac_rest": jac_rest}
 
 
+_CX_TOK = re.compile(r"\s*(dg_ipow<\d+>|dg_div|[A-Za-z_][A-Za-z0-9_]*|"
+                     r"\d+\.\d*(?:e[+-]?\d+)?|\d+(?:e[+-]?\d+)?|[-+*/(),])")
+
+
+def _cx_parse(text):
+    """Expression tree of a printed C expression (nested tuples), or None."""
+    toks, pos = [], 0
+    text = text.strip()
+    while pos < len(text):
+        m = _CX_TOK.match(text, pos)
+        if not m or m.end() == pos:
+            return None
+        toks.append(m.group(1))
+        pos = m.end()
+    i = [0]
+
+    def peek():
+        return toks[i[0]] if i[0] < len(toks) else None
+
+    def take():
+        i[0] += 1
+        return toks[i[0] - 1]
+
+    def expr():
+        n = term()
+        while peek() in ("+", "-"):
+            op = take()
+            n = (op, n, term())
+        return n
+
+    def term():
+        n = unary()
+        while peek() in ("*", "/"):
+            op = take()
+            n = (op, n, unary())
+        return n
+
+    def unary():
+        if peek() == "-":
+            take()
+            return ("neg", unary())
+        return atom()
+
+    def atom():
+        x = take()
+        if x == "(":
+            n = expr()
+            take()
+            return n
+        if peek() == "(":
+            take()
+            args = [expr()]
+            while peek() == ",":
+                take()
+                args.append(expr())
+            take()
+            return ("call", x, tuple(args))
+        return ("leaf", x)
+
+    try:
+        n = expr()
+    except IndexError:
+        return None
+    return n if i[0] == len(toks) else None
+
+
+def _cx_nodes(n, acc):
+    """The operation nodes of tree n with their FP64 cost (a division 9, a
+    dg_div 3, a cube or other power 6, other calls 20)."""
+    if n[0] == "leaf" or n in acc:
+        return
+    if n[0] == "neg":
+        _cx_nodes(n[1], acc)
+        return
+    if n[0] == "call":
+        name = n[1]
+        acc[n] = 3 if name == "dg_div" else (1 if name == "dg_ipow<2>" else
+                                             (6 if name.startswith("dg_ipow") else 20))
+        for a in n[2]:
+            _cx_nodes(a, acc)
+        return
+    acc[n] = 9 if n[0] == "/" else 1
+    _cx_nodes(n[1], acc)
+    _cx_nodes(n[2], acc)
+
+
+def balance_shared(texts, nparts):
+    """Part index for each statement: longest-first greedy onto the part
+    whose resulting cost is lowest, where a part's cost counts each
+    operation of its statements' expressions once -- the compiler computes
+    a subexpression several statements of one part share only once -- so
+    statements that share large subexpressions (the ge row's cooling terms)
+    end up together.  None texts (structural zeros) cost 0.5."""
+    nodes = []
+    for t in texts:
+        if t is None:
+            nodes.append(None)
+            continue
+        m = re.match(r"^\s*[A-Za-z_][A-Za-z0-9_\[\]]* = (.*?);", t, re.S)
+        tree = _cx_parse(m.group(1)) if m else None
+        acc = {}
+        if tree is not None:
+            _cx_nodes(tree, acc)
+        else:
+            acc[("text", t)] = float(len(t)) / 8.0
+        nodes.append(acc)
+    own = [0.5 if a is None else sum(a.values()) + 4.0 for a in nodes]
+    sets = [dict() for _ in range(nparts)]
+    loads = [0.0] * nparts
+    part = [0] * len(texts)
+    for k in sorted(range(len(texts)), key=lambda k: (-own[k], k)):
+        best = None
+        for p in range(nparts):
+            if nodes[k] is None:
+                new = loads[p] + 0.5
+            else:
+                extra = sum(c for n, c in nodes[k].items() if n not in sets[p])
+                new = loads[p] + extra + 4.0
+            key = (max([new] + [loads[q] for q in range(nparts) if q != p]), new, p)
+            if best is None or key < best[0]:
+                best = (key, p, new)
+        _, p, new = best
+        part[k] = p
+        loads[p] = new
+        if nodes[k] is not None:
+            sets[p].update(nodes[k])
+    return part
+
+
 def balance(costs, nparts):
     """Part index for each item: longest-first greedy onto the least-loaded
     part (ties to the lowest part), so parts carry similar operation counts."""
@@ -399,7 +528,8 @@ def network_spec(net, name):
     rhs_part, jac_part = {}, {}
     for npart in (1, 2, 4):
         rhs_part[npart] = balance(rhs_cost, npart)
-        flat = balance(jac_cost, npart)
+        flat = balance_shared([jac_dev[v][q] for v in range(N) for q in range(N)], npart) \
+            if npart > 1 else balance(jac_cost, npart)
         jac_part[npart] = [flat[v * N:(v + 1) * N] for v in range(N)]
     md = net.mass_density_expression()
     T = net.temperature_expression(False)

@@ -640,18 +640,18 @@ struct Net {
         const double rmd = 1.0 / mdensity;
         (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H_1_i*de;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = H_1_i*de;
             put(1, 0, jv);
         }
         if (pick(NP, 0, 0, 1) == P) {
             put.zero(2, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 0);
         }
         if (pick(NP, 0, 0, 1) == P) {
@@ -666,22 +666,22 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 0);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(12, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(13, 0);
         }
         if (pick(NP, 0, 0, 1) == P) {
@@ -693,66 +693,66 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(15, 0, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = H_2_r*de;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -H_2_r*de;
             put(1, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(2, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 1);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 1);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(12, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(13, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -H_2_r*de;
             put(14, 1, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_2_c_H_2_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(0, 2);
         }
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 2);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -He_1_i*de;
             put(2, 2, jv);
         }
@@ -790,11 +790,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = He_1_i*de;
             put(14, 2, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -He_1_c_He_1_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 2, jv);
@@ -805,15 +805,15 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 3);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = He_2_r*de;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_2_i*de - He_2_r*de;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = He_2_i*de;
             put(4, 3, jv);
         }
@@ -844,11 +844,11 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_2_i*de - He_2_r*de;
             put(14, 3, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_2_c_He_2_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 3, jv);
@@ -862,11 +862,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_3_r*de;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -He_3_r*de;
             put(4, 4, jv);
         }
@@ -897,11 +897,11 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 4);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -He_3_r*de;
             put(14, 4, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_3_c_He_3_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 4, jv);
@@ -921,11 +921,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_1_i*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_1_i*de;
             put(6, 5, jv);
         }
@@ -950,7 +950,7 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 5);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_1_i*de;
             put(14, 5, jv);
         }
@@ -978,11 +978,11 @@ struct Net {
             jv = O_2_r*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_2_i*de - O_2_r*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_2_i*de;
             put(7, 6, jv);
         }
@@ -1004,11 +1004,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 6);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_2_i*de - O_2_r*de;
             put(14, 6, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -O_2_c_O_2_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 6, jv);
@@ -1031,15 +1031,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_3_r*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_3_i*de - O_3_r*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*de;
             put(8, 7, jv);
         }
@@ -1058,11 +1058,11 @@ struct Net {
         if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_i*de - O_3_r*de;
             put(14, 7, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -O_3_c_O_3_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 7, jv);
@@ -1088,15 +1088,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 8);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_4_r*de;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_4_i*de - O_4_r*de;
             put(8, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_4_i*de;
             put(9, 8, jv);
         }
@@ -1112,11 +1112,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 8);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_4_i*de - O_4_r*de;
             put(14, 8, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_4_c_O_4_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 8, jv);
@@ -1149,11 +1149,11 @@ struct Net {
             jv = O_5_r*de;
             put(8, 9, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_5_i*de - O_5_r*de;
             put(9, 9, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_5_i*de;
             put(10, 9, jv);
         }
@@ -1170,7 +1170,7 @@ struct Net {
             jv = O_5_i*de - O_5_r*de;
             put(14, 9, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_5_c_O_5_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 9, jv);
@@ -1202,15 +1202,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(8, 10);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_6_r*de;
             put(9, 10, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_i*de - O_6_r*de;
             put(10, 10, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de;
             put(11, 10, jv);
         }
@@ -1220,11 +1220,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 10);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de - O_6_r*de;
             put(14, 10, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_c_O_6_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 10, jv);
@@ -1259,26 +1259,26 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_r*de;
             put(10, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_i*de - O_7_r*de;
             put(11, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de;
             put(12, 11, jv);
         }
         if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de - O_7_r*de;
             put(14, 11, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_c_O_7_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 11, jv);
@@ -1316,23 +1316,23 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 12);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_r*de;
             put(11, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_8_i*de - O_8_r*de;
             put(12, 12, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_8_i*de;
             put(13, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_i*de - O_8_r*de;
             put(14, 12, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_8_c_O_8_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 12, jv);
@@ -1373,32 +1373,32 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_9_r*de;
             put(12, 13, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_9_r*de;
             put(13, 13, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_9_r*de;
             put(14, 13, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_9_c_O_9_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 13, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_1_i*H_1 + H_2_r*H_2;
             put(0, 14, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = H_1_i*H_1 - H_2_r*H_2;
             put(1, 14, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -He_1_i*He_1 + He_2_r*He_2;
             put(2, 14, jv);
         }
@@ -1406,11 +1406,11 @@ struct Net {
             jv = He_1_i*He_1 - He_2_i*He_2 - He_2_r*He_2 + He_3_r*He_3;
             put(3, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = He_2_i*He_2 - He_3_r*He_3;
             put(4, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_1_i*O_1 + O_2_r*O_2;
             put(5, 14, jv);
         }
@@ -1418,31 +1418,31 @@ struct Net {
             jv = O_1_i*O_1 - O_2_i*O_2 - O_2_r*O_2 + O_3_r*O_3;
             put(6, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_2_i*O_2 - O_3_i*O_3 - O_3_r*O_3 + O_4_r*O_4;
             put(7, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*O_3 - O_4_i*O_4 - O_4_r*O_4 + O_5_r*O_5;
             put(8, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_4_i*O_4 - O_5_i*O_5 - O_5_r*O_5 + O_6_r*O_6;
             put(9, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*O_5 - O_6_i*O_6 - O_6_r*O_6 + O_7_r*O_7;
             put(10, 14, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_6_i*O_6 - O_7_i*O_7 - O_7_r*O_7 + O_8_r*O_8;
             put(11, 14, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_7_i*O_7 - O_8_i*O_8 - O_8_r*O_8 + O_9_r*O_9;
             put(12, 14, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_8_i*O_8 - O_9_r*O_9;
             put(13, 14, jv);
         }
@@ -1963,18 +1963,18 @@ struct Net {
         const XF O_8_c_O_8_c = xf(R[34]);
         const XF O_9_c_O_9_c = xf(R[35]);
         XF jv;
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H_1_i*de;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = H_1_i*de;
             put(1, 0, jv);
         }
         if (pick(NP, 0, 0, 1) == P) {
             put.zero(2, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 0);
         }
         if (pick(NP, 0, 0, 1) == P) {
@@ -1989,22 +1989,22 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 0);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 0);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(12, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(13, 0);
         }
         if (pick(NP, 0, 0, 1) == P) {
@@ -2016,66 +2016,66 @@ struct Net {
             jv = jv / mdensity;
             put(15, 0, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = H_2_r*de;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -H_2_r*de;
             put(1, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(2, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 1);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 1);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(12, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(13, 1);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -H_2_r*de;
             put(14, 1, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_2_c_H_2_c*de;
             jv = jv / mdensity;
             put(15, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(0, 2);
         }
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 2);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -He_1_i*de;
             put(2, 2, jv);
         }
@@ -2113,11 +2113,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = He_1_i*de;
             put(14, 2, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -He_1_c_He_1_c*de;
             jv = jv / mdensity;
             put(15, 2, jv);
@@ -2128,15 +2128,15 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 3);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = He_2_r*de;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_2_i*de - He_2_r*de;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = He_2_i*de;
             put(4, 3, jv);
         }
@@ -2167,11 +2167,11 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_2_i*de - He_2_r*de;
             put(14, 3, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_2_c_He_2_c*de;
             jv = jv / mdensity;
             put(15, 3, jv);
@@ -2185,11 +2185,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_3_r*de;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -He_3_r*de;
             put(4, 4, jv);
         }
@@ -2220,11 +2220,11 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 4);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -He_3_r*de;
             put(14, 4, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_3_c_He_3_c*de;
             jv = jv / mdensity;
             put(15, 4, jv);
@@ -2244,11 +2244,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_1_i*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_1_i*de;
             put(6, 5, jv);
         }
@@ -2273,7 +2273,7 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 5);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_1_i*de;
             put(14, 5, jv);
         }
@@ -2301,11 +2301,11 @@ struct Net {
             jv = O_2_r*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_2_i*de - O_2_r*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_2_i*de;
             put(7, 6, jv);
         }
@@ -2327,11 +2327,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 6);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_2_i*de - O_2_r*de;
             put(14, 6, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -O_2_c_O_2_c*de;
             jv = jv / mdensity;
             put(15, 6, jv);
@@ -2354,15 +2354,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_3_r*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_3_i*de - O_3_r*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*de;
             put(8, 7, jv);
         }
@@ -2381,11 +2381,11 @@ struct Net {
         if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_i*de - O_3_r*de;
             put(14, 7, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -O_3_c_O_3_c*de;
             jv = jv / mdensity;
             put(15, 7, jv);
@@ -2411,15 +2411,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 8);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_4_r*de;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_4_i*de - O_4_r*de;
             put(8, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_4_i*de;
             put(9, 8, jv);
         }
@@ -2435,11 +2435,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 8);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_4_i*de - O_4_r*de;
             put(14, 8, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_4_c_O_4_c*de;
             jv = jv / mdensity;
             put(15, 8, jv);
@@ -2472,11 +2472,11 @@ struct Net {
             jv = O_5_r*de;
             put(8, 9, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_5_i*de - O_5_r*de;
             put(9, 9, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_5_i*de;
             put(10, 9, jv);
         }
@@ -2493,7 +2493,7 @@ struct Net {
             jv = O_5_i*de - O_5_r*de;
             put(14, 9, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_5_c_O_5_c*de;
             jv = jv / mdensity;
             put(15, 9, jv);
@@ -2525,15 +2525,15 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(8, 10);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_6_r*de;
             put(9, 10, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_i*de - O_6_r*de;
             put(10, 10, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de;
             put(11, 10, jv);
         }
@@ -2543,11 +2543,11 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 10);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de - O_6_r*de;
             put(14, 10, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_c_O_6_c*de;
             jv = jv / mdensity;
             put(15, 10, jv);
@@ -2582,26 +2582,26 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_r*de;
             put(10, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_i*de - O_7_r*de;
             put(11, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de;
             put(12, 11, jv);
         }
         if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de - O_7_r*de;
             put(14, 11, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_c_O_7_c*de;
             jv = jv / mdensity;
             put(15, 11, jv);
@@ -2639,23 +2639,23 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 12);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_r*de;
             put(11, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_8_i*de - O_8_r*de;
             put(12, 12, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_8_i*de;
             put(13, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_i*de - O_8_r*de;
             put(14, 12, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_8_c_O_8_c*de;
             jv = jv / mdensity;
             put(15, 12, jv);
@@ -2696,32 +2696,32 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_9_r*de;
             put(12, 13, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_9_r*de;
             put(13, 13, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_9_r*de;
             put(14, 13, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_9_c_O_9_c*de;
             jv = jv / mdensity;
             put(15, 13, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_1_i*H_1 + H_2_r*H_2;
             put(0, 14, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = H_1_i*H_1 - H_2_r*H_2;
             put(1, 14, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -He_1_i*He_1 + He_2_r*He_2;
             put(2, 14, jv);
         }
@@ -2729,11 +2729,11 @@ struct Net {
             jv = He_1_i*He_1 - He_2_i*He_2 - He_2_r*He_2 + He_3_r*He_3;
             put(3, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = He_2_i*He_2 - He_3_r*He_3;
             put(4, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_1_i*O_1 + O_2_r*O_2;
             put(5, 14, jv);
         }
@@ -2741,31 +2741,31 @@ struct Net {
             jv = O_1_i*O_1 - O_2_i*O_2 - O_2_r*O_2 + O_3_r*O_3;
             put(6, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_2_i*O_2 - O_3_i*O_3 - O_3_r*O_3 + O_4_r*O_4;
             put(7, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*O_3 - O_4_i*O_4 - O_4_r*O_4 + O_5_r*O_5;
             put(8, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_4_i*O_4 - O_5_i*O_5 - O_5_r*O_5 + O_6_r*O_6;
             put(9, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*O_5 - O_6_i*O_6 - O_6_r*O_6 + O_7_r*O_7;
             put(10, 14, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_6_i*O_6 - O_7_i*O_7 - O_7_r*O_7 + O_8_r*O_8;
             put(11, 14, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_7_i*O_7 - O_8_i*O_8 - O_8_r*O_8 + O_9_r*O_9;
             put(12, 14, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_8_i*O_8 - O_9_r*O_9;
             put(13, 14, jv);
         }

@@ -750,15 +750,15 @@ struct Net {
         const double rmd = 1.0 / mdensity;
         (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H_1_i*de - H_1_pi;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = H_1_i*de + H_1_pi;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(2, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
@@ -770,19 +770,19 @@ struct Net {
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 0);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(9, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(10, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
@@ -794,20 +794,20 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = H_1_i*de + H_1_pi;
             put(14, 0, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -H_1_c_H_1_c*de + H_1_ph_H_1_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 0, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = H_2_r*de;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -H_2_r*de;
             put(1, 1, jv);
         }
@@ -832,206 +832,206 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 1);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -H_2_r*de;
             put(14, 1, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_2_c_H_2_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 2);
         }
         if (pick(NP, 0, 0, 3) == P) {
             jv = -He_1_i*de - He_1_pi;
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = He_1_i*de + He_1_pi;
             put(3, 2, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(6, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 2);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 2);
         }
         if (pick(NP, 0, 1, 0) == P) {
             jv = He_1_i*de + He_1_pi;
             put(14, 2, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_1_c_He_1_c*de + He_1_ph_He_1_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 3);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = He_2_r*de;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_2_i*de - He_2_pi - He_2_r*de;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = He_2_i*de + He_2_pi;
             put(4, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_2_i*de + He_2_pi - He_2_r*de;
             put(14, 3, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_2_c_He_2_c*de + He_2_ph_He_2_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = He_3_r*de;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -He_3_r*de;
             put(4, 4, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 4);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 4);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_3_r*de;
             put(14, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -He_3_c_He_3_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_1_i*de - O_1_pi;
             put(5, 5, jv);
         }
@@ -1039,82 +1039,82 @@ struct Net {
             jv = O_1_i*de + O_1_pi;
             put(6, 5, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 5);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_1_i*de + O_1_pi;
             put(14, 5, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_1_c_O_1_c*de + O_1_ph_O_1_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_2_r*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_2_i*de - O_2_pi - O_2_r*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_2_i*de + O_2_pi;
             put(7, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(8, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(12, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_2_i*de + O_2_pi - O_2_r*de;
             put(14, 6, jv);
         }
@@ -1123,388 +1123,388 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(15, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(0, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(1, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(2, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_r*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_3_i*de - O_3_pi - O_3_r*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_3_i*de + O_3_pi;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(9, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(10, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(11, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(12, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 7);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_i*de + O_3_pi - O_3_r*de;
             put(14, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_3_c_O_3_c*de + O_3_ph_O_3_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 7, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(0, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(1, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(2, 8);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(3, 8);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 8);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_4_r*de;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_4_i*de - O_4_pi - O_4_r*de;
             put(8, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_4_i*de + O_4_pi;
             put(9, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 8);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 8);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_4_i*de + O_4_pi - O_4_r*de;
             put(14, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_4_c_O_4_c*de + O_4_ph_O_4_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 9);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 9);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_5_r*de;
             put(8, 9, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_5_i*de - O_5_pi - O_5_r*de;
             put(9, 9, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*de + O_5_pi;
             put(10, 9, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_5_i*de + O_5_pi - O_5_r*de;
             put(14, 9, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_5_c_O_5_c*de + O_5_ph_O_5_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 9, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 10);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 10);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 10);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(5, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 10);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(8, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_6_r*de;
             put(9, 10, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_i*de - O_6_pi - O_6_r*de;
             put(10, 10, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_6_i*de + O_6_pi;
             put(11, 10, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(12, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de + O_6_pi - O_6_r*de;
             put(14, 10, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_6_c_O_6_c*de + O_6_ph_O_6_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 10, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(0, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(1, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(2, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 11);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(6, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 11);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_r*de;
             put(10, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_i*de - O_7_pi - O_7_r*de;
             put(11, 11, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_7_i*de + O_7_pi;
             put(12, 11, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 11);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de + O_7_pi - O_7_r*de;
             put(14, 11, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_7_c_O_7_c*de + O_7_ph_O_7_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 11, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(0, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(1, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(2, 12);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(3, 12);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 12);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 12);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 12);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_8_r*de;
             put(11, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_8_i*de - O_8_pi - O_8_r*de;
             put(12, 12, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_8_i*de + O_8_pi;
             put(13, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_i*de + O_8_pi - O_8_r*de;
             put(14, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_8_c_O_8_c*de + O_8_ph_O_8_ph;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 13);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 13);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(8, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 13);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_9_r*de;
             put(12, 13, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_9_r*de;
             put(13, 13, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_9_r*de;
             put(14, 13, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_9_c_O_9_c*de;
             jv = dg_div(jv, mdensity, rmd);
             put(15, 13, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -H_1_i*H_1 + H_2_r*H_2;
             put(0, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = H_1_i*H_1 - H_2_r*H_2;
             put(1, 14, jv);
         }
@@ -1520,7 +1520,7 @@ struct Net {
             jv = He_2_i*He_2 - He_3_r*He_3;
             put(4, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -O_1_i*O_1 + O_2_r*O_2;
             put(5, 14, jv);
         }
@@ -1528,31 +1528,31 @@ struct Net {
             jv = O_1_i*O_1 - O_2_i*O_2 - O_2_r*O_2 + O_3_r*O_3;
             put(6, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_2_i*O_2 - O_3_i*O_3 - O_3_r*O_3 + O_4_r*O_4;
             put(7, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*O_3 - O_4_i*O_4 - O_4_r*O_4 + O_5_r*O_5;
             put(8, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_4_i*O_4 - O_5_i*O_5 - O_5_r*O_5 + O_6_r*O_6;
             put(9, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*O_5 - O_6_i*O_6 - O_6_r*O_6 + O_7_r*O_7;
             put(10, 14, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_6_i*O_6 - O_7_i*O_7 - O_7_r*O_7 + O_8_r*O_8;
             put(11, 14, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_7_i*O_7 - O_8_i*O_8 - O_8_r*O_8 + O_9_r*O_9;
             put(12, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_8_i*O_8 - O_9_r*O_9;
             put(13, 14, jv);
         }
@@ -1565,52 +1565,52 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(15, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(0, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(1, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(2, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(3, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(4, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(5, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(6, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(7, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(8, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(9, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(10, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(11, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(12, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(13, 15, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(14, 15, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(15, 15, zero_both);
         }
         return true;
@@ -2183,15 +2183,15 @@ struct Net {
         const XF O_8_ph_O_8_ph = xf(R[56]);
         const XF O_9_c_O_9_c = xf(R[57]);
         XF jv;
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H_1_i*de - H_1_pi;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = H_1_i*de + H_1_pi;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(2, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
@@ -2203,19 +2203,19 @@ struct Net {
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 0);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(9, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(10, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
@@ -2227,20 +2227,20 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 0);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = H_1_i*de + H_1_pi;
             put(14, 0, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -H_1_c_H_1_c*de + H_1_ph_H_1_ph;
             jv = jv / mdensity;
             put(15, 0, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = H_2_r*de;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -H_2_r*de;
             put(1, 1, jv);
         }
@@ -2265,206 +2265,206 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 1);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 1);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -H_2_r*de;
             put(14, 1, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -H_2_c_H_2_c*de;
             jv = jv / mdensity;
             put(15, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 2);
         }
         if (pick(NP, 0, 0, 3) == P) {
             jv = -He_1_i*de - He_1_pi;
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = He_1_i*de + He_1_pi;
             put(3, 2, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(6, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 2);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 2);
         }
         if (pick(NP, 0, 1, 0) == P) {
             jv = He_1_i*de + He_1_pi;
             put(14, 2, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_1_c_He_1_c*de + He_1_ph_He_1_ph;
             jv = jv / mdensity;
             put(15, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 3);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = He_2_r*de;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_2_i*de - He_2_pi - He_2_r*de;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = He_2_i*de + He_2_pi;
             put(4, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 3);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 3);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = He_2_i*de + He_2_pi - He_2_r*de;
             put(14, 3, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -He_2_c_He_2_c*de + He_2_ph_He_2_ph;
             jv = jv / mdensity;
             put(15, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = He_3_r*de;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -He_3_r*de;
             put(4, 4, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 4);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 4);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 4);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 4);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -He_3_r*de;
             put(14, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -He_3_c_He_3_c*de;
             jv = jv / mdensity;
             put(15, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_1_i*de - O_1_pi;
             put(5, 5, jv);
         }
@@ -2472,82 +2472,82 @@ struct Net {
             jv = O_1_i*de + O_1_pi;
             put(6, 5, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 5);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_1_i*de + O_1_pi;
             put(14, 5, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_1_c_O_1_c*de + O_1_ph_O_1_ph;
             jv = jv / mdensity;
             put(15, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_2_r*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_2_i*de - O_2_pi - O_2_r*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_2_i*de + O_2_pi;
             put(7, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(8, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(12, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_2_i*de + O_2_pi - O_2_r*de;
             put(14, 6, jv);
         }
@@ -2556,388 +2556,388 @@ struct Net {
             jv = jv / mdensity;
             put(15, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(0, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(1, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(2, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_r*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_3_i*de - O_3_pi - O_3_r*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = O_3_i*de + O_3_pi;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(9, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(10, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(11, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(12, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 7);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_3_i*de + O_3_pi - O_3_r*de;
             put(14, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_3_c_O_3_c*de + O_3_ph_O_3_ph;
             jv = jv / mdensity;
             put(15, 7, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(0, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(1, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(2, 8);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(3, 8);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 8);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_4_r*de;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_4_i*de - O_4_pi - O_4_r*de;
             put(8, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_4_i*de + O_4_pi;
             put(9, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(10, 8);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(11, 8);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(12, 8);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(13, 8);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_4_i*de + O_4_pi - O_4_r*de;
             put(14, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_4_c_O_4_c*de + O_4_ph_O_4_ph;
             jv = jv / mdensity;
             put(15, 8, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 9);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 9);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_5_r*de;
             put(8, 9, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_5_i*de - O_5_pi - O_5_r*de;
             put(9, 9, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*de + O_5_pi;
             put(10, 9, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(11, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(12, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(13, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_5_i*de + O_5_pi - O_5_r*de;
             put(14, 9, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_5_c_O_5_c*de + O_5_ph_O_5_ph;
             jv = jv / mdensity;
             put(15, 9, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 10);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 10);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 10);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(5, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 10);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(8, 10);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = O_6_r*de;
             put(9, 10, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_6_i*de - O_6_pi - O_6_r*de;
             put(10, 10, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_6_i*de + O_6_pi;
             put(11, 10, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(12, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 10);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_6_i*de + O_6_pi - O_6_r*de;
             put(14, 10, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_6_c_O_6_c*de + O_6_ph_O_6_ph;
             jv = jv / mdensity;
             put(15, 10, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(0, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(1, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(2, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 11);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(6, 11);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 11);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 11);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 11);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_r*de;
             put(10, 11, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -O_7_i*de - O_7_pi - O_7_r*de;
             put(11, 11, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_7_i*de + O_7_pi;
             put(12, 11, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(13, 11);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = O_7_i*de + O_7_pi - O_7_r*de;
             put(14, 11, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -O_7_c_O_7_c*de + O_7_ph_O_7_ph;
             jv = jv / mdensity;
             put(15, 11, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(0, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(1, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(2, 12);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(3, 12);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 12);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(7, 12);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(8, 12);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(9, 12);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(10, 12);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_8_r*de;
             put(11, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_8_i*de - O_8_pi - O_8_r*de;
             put(12, 12, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = O_8_i*de + O_8_pi;
             put(13, 12, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_8_i*de + O_8_pi - O_8_r*de;
             put(14, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -O_8_c_O_8_c*de + O_8_ph_O_8_ph;
             jv = jv / mdensity;
             put(15, 12, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 13);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 13);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(8, 13);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 13);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 13);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 13);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_9_r*de;
             put(12, 13, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -O_9_r*de;
             put(13, 13, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -O_9_r*de;
             put(14, 13, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -O_9_c_O_9_c*de;
             jv = jv / mdensity;
             put(15, 13, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -H_1_i*H_1 + H_2_r*H_2;
             put(0, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = H_1_i*H_1 - H_2_r*H_2;
             put(1, 14, jv);
         }
@@ -2953,7 +2953,7 @@ struct Net {
             jv = He_2_i*He_2 - He_3_r*He_3;
             put(4, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -O_1_i*O_1 + O_2_r*O_2;
             put(5, 14, jv);
         }
@@ -2961,31 +2961,31 @@ struct Net {
             jv = O_1_i*O_1 - O_2_i*O_2 - O_2_r*O_2 + O_3_r*O_3;
             put(6, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_2_i*O_2 - O_3_i*O_3 - O_3_r*O_3 + O_4_r*O_4;
             put(7, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = O_3_i*O_3 - O_4_i*O_4 - O_4_r*O_4 + O_5_r*O_5;
             put(8, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_4_i*O_4 - O_5_i*O_5 - O_5_r*O_5 + O_6_r*O_6;
             put(9, 14, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_5_i*O_5 - O_6_i*O_6 - O_6_r*O_6 + O_7_r*O_7;
             put(10, 14, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = O_6_i*O_6 - O_7_i*O_7 - O_7_r*O_7 + O_8_r*O_8;
             put(11, 14, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = O_7_i*O_7 - O_8_i*O_8 - O_8_r*O_8 + O_9_r*O_9;
             put(12, 14, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = O_8_i*O_8 - O_9_r*O_9;
             put(13, 14, jv);
         }
@@ -2998,52 +2998,52 @@ struct Net {
             jv = jv / mdensity;
             put(15, 14, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 15);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 15);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 15);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 15);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 15);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 15);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 15);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 15);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(8, 15);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(9, 15);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(10, 15);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(11, 15);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(12, 15);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(13, 15);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(14, 15);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(15, 15);
         }
         return true;

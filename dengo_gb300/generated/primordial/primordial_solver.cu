@@ -598,35 +598,35 @@ struct Net {
         const double rmd = 1.0 / mdensity;
         (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k11*H_2;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
             put(2, 0, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k11*H_2 + 2*k12*de;
             put(3, 0, jv);
         }
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(6, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 0);
         }
         if (pick(NP, 0, 1, 1) == P) {
@@ -634,47 +634,47 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k10*H_1 + k19*H_m0;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k10*H_1 - k18*de - k19*H_m0;
             put(1, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k10*H_1 + 2*k18*de + k19*H_m0;
             put(2, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k10*H_1;
             put(3, 1, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k19*H_m0;
             put(4, 1, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 1);
         }
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k18*de;
             put(8, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put(9, 1, zero_row);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
             put(0, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k09*H_2 - k10*H2_2;
             put(1, 2, jv);
         }
@@ -682,7 +682,7 @@ struct Net {
             jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k01*de - k09*H_2 + k10*H2_2;
             put(3, 2, jv);
         }
@@ -690,16 +690,16 @@ struct Net {
             jv = k07*de - k08*H_m0 - k15*H_m0;
             put(4, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(6, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
             put(8, 2, jv);
         }
@@ -708,33 +708,33 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H2_1;
             put(0, 3, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k09*H_1 + k11*H2_1 + k17*H_m0;
             put(1, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k16*H_m0 - k17*H_m0;
             put(4, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(7, 3);
         }
         if (pick(NP, 0, 0, 0) == P) {
@@ -746,36 +746,36 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k08*H_1 + k19*H2_2;
             put(0, 4, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k17*H_2 - k19*H2_2;
             put(1, 4, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
             put(2, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k16*H_2 - k17*H_2;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
             put(4, 4, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(6, 4);
         }
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
             put(8, 4, jv);
         }
@@ -785,27 +785,27 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(1, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(2, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(3, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k03*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k03*de;
             put(6, 5, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 5);
         }
         if (pick(NP, 0, 0, 2) == P) {
@@ -817,30 +817,30 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k04*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k04*de - k05*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k05*de;
             put(7, 6, jv);
         }
@@ -848,71 +848,71 @@ struct Net {
             jv = -k04*de + k05*de;
             put(8, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k06*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k06*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k06*de;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -4.0*brem_brem*de - de*reHeIII_reHeIII;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k12*H2_1;
             put(0, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k18*H2_2;
             put(1, 8, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k01*H_1 + k02*H_2 - k07*H_1 + k14*H_m0 + 2*k18*H2_2;
             put(2, 8, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
             put(3, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k07*H_1 - k14*H_m0;
             put(4, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k03*He_1 + k04*He_2;
             put(5, 8, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
             put(6, 8, jv);
         }
@@ -929,34 +929,34 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(0, 9, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(1, 9, zero_col);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(2, 9, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(3, 9, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(4, 9, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(5, 9, zero_col);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put(6, 9, zero_col);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put(7, 9, zero_col);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put(8, 9, zero_col);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put(9, 9, zero_both);
         }
         return true;
@@ -1428,35 +1428,35 @@ struct Net {
         const XF reHeII2_reHeII2 = xf(R[42]);
         const XF reHeIII_reHeIII = xf(R[43]);
         XF jv;
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k11*H_2;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
             put(2, 0, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k11*H_2 + 2*k12*de;
             put(3, 0, jv);
         }
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(6, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(8, 0);
         }
         if (pick(NP, 0, 1, 1) == P) {
@@ -1464,47 +1464,47 @@ struct Net {
             jv = jv / mdensity;
             put(9, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k10*H_1 + k19*H_m0;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k10*H_1 - k18*de - k19*H_m0;
             put(1, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k10*H_1 + 2*k18*de + k19*H_m0;
             put(2, 1, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k10*H_1;
             put(3, 1, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k19*H_m0;
             put(4, 1, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 1);
         }
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k18*de;
             put(8, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
             put(0, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k09*H_2 - k10*H2_2;
             put(1, 2, jv);
         }
@@ -1512,7 +1512,7 @@ struct Net {
             jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k01*de - k09*H_2 + k10*H2_2;
             put(3, 2, jv);
         }
@@ -1520,16 +1520,16 @@ struct Net {
             jv = k07*de - k08*H_m0 - k15*H_m0;
             put(4, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 2);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(6, 2);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
             put(8, 2, jv);
         }
@@ -1538,33 +1538,33 @@ struct Net {
             jv = jv / mdensity;
             put(9, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H2_1;
             put(0, 3, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k09*H_1 + k11*H2_1 + k17*H_m0;
             put(1, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k16*H_m0 - k17*H_m0;
             put(4, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(5, 3);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(6, 3);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(7, 3);
         }
         if (pick(NP, 0, 0, 0) == P) {
@@ -1576,36 +1576,36 @@ struct Net {
             jv = jv / mdensity;
             put(9, 3, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k08*H_1 + k19*H2_2;
             put(0, 4, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k17*H_2 - k19*H2_2;
             put(1, 4, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
             put(2, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k16*H_2 - k17*H_2;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
             put(4, 4, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 4);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(6, 4);
         }
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
             put(8, 4, jv);
         }
@@ -1615,27 +1615,27 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 5);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             put.zero(1, 5);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             put.zero(2, 5);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             put.zero(3, 5);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k03*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k03*de;
             put(6, 5, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 5);
         }
         if (pick(NP, 0, 0, 2) == P) {
@@ -1647,30 +1647,30 @@ struct Net {
             jv = jv / mdensity;
             put(9, 5, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(0, 6);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(1, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(2, 6);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(3, 6);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k04*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k04*de - k05*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k05*de;
             put(7, 6, jv);
         }
@@ -1678,71 +1678,71 @@ struct Net {
             jv = -k04*de + k05*de;
             put(8, 6, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
             jv = jv / mdensity;
             put(9, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(0, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(1, 7);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(2, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(3, 7);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(4, 7);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = k06*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k06*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k06*de;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -4.0f*brem_brem*de - de*reHeIII_reHeIII;
             jv = jv / mdensity;
             put(9, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k12*H2_1;
             put(0, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k18*H2_2;
             put(1, 8, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k01*H_1 + k02*H_2 - k07*H_1 + k14*H_m0 + 2*k18*H2_2;
             put(2, 8, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
             put(3, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k07*H_1 - k14*H_m0;
             put(4, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k03*He_1 + k04*He_2;
             put(5, 8, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
             put(6, 8, jv);
         }
@@ -1759,34 +1759,34 @@ struct Net {
             jv = jv / mdensity;
             put(9, 8, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(0, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(1, 9);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(2, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(3, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(4, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 9);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             put.zero(6, 9);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 9);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             put.zero(8, 9);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(9, 9);
         }
         return true;

@@ -603,35 +603,35 @@ struct Net {
         const double rmd = 1.0 / mdensity;
         (void)zero_row; (void)zero_col; (void)zero_both; (void)rmd;
         double jv;
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k11*H_2;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
             put(2, 0, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 + 2*k12*de;
             put(3, 0, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             put.zero(8, 0);
         }
         if (pick(NP, 0, 1, 1) == P) {
@@ -639,11 +639,11 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 0, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k10*H_1 + k19*H_m0;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k10*H_1 - k18*de - k19*H_m0;
             put(1, 1, jv);
         }
@@ -659,23 +659,23 @@ struct Net {
             jv = -k19*H_m0;
             put(4, 1, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 1);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k18*de;
             put(8, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             put(9, 1, zero_row);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
             put(0, 2, jv);
         }
@@ -683,19 +683,19 @@ struct Net {
             jv = k09*H_2 - k10*H2_2;
             put(1, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k01*de - k09*H_2 + k10*H2_2;
             put(3, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k07*de - k08*H_m0 - k15*H_m0;
             put(4, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 2);
         }
         if (pick(NP, 0, 0, 2) == P) {
@@ -704,7 +704,7 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
             put(8, 2, jv);
         }
@@ -713,11 +713,11 @@ struct Net {
             jv = dg_div(jv, mdensity, rmd);
             put(9, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k11*H2_1;
             put(0, 3, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k09*H_1 + k11*H2_1 + k17*H_m0;
             put(1, 3, jv);
         }
@@ -725,11 +725,11 @@ struct Net {
             jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k16*H_m0 - k17*H_m0;
             put(4, 3, jv);
         }
@@ -742,32 +742,32 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 3);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k02*de + k17*H_m0;
             put(8, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 3, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k08*H_1 + k19*H2_2;
             put(0, 4, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k17*H_2 - k19*H2_2;
             put(1, 4, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
             put(2, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k16*H_2 - k17*H_2;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
             put(4, 4, jv);
         }
@@ -780,7 +780,7 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
             put(8, 4, jv);
         }
@@ -802,11 +802,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k03*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k03*de;
             put(6, 5, jv);
         }
@@ -817,7 +817,7 @@ struct Net {
             jv = k03*de;
             put(8, 5, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 5, jv);
@@ -837,23 +837,23 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k04*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k04*de - k05*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k05*de;
             put(7, 6, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k04*de + k05*de;
             put(8, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 6, jv);
@@ -876,28 +876,28 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k06*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -k06*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k06*de;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -4.0*brem_brem*de - de*reHeIII_reHeIII;
             jv = dg_div(jv, mdensity, rmd);
             put(9, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k12*H2_1;
             put(0, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k18*H2_2;
             put(1, 8, jv);
         }
@@ -909,23 +909,23 @@ struct Net {
             jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
             put(3, 8, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k07*H_1 - k14*H_m0;
             put(4, 8, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k03*He_1 + k04*He_2;
             put(5, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
             put(6, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k05*He_2 - k06*He_3;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
             put(8, 8, jv);
         }
@@ -1438,35 +1438,35 @@ struct Net {
         const XF reHeII2_reHeII2 = xf(R[43]);
         const XF reHeIII_reHeIII = xf(R[44]);
         XF jv;
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 - k12*de - k13*H_1 + k21*dg_ipow<2>(H_1) - 2*k23*H2_1;
             put(0, 0, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k11*H_2;
             put(1, 0, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k11*H_2 + 2*k13*H_1 - 2*k21*dg_ipow<2>(H_1) + 4*k23*H2_1;
             put(2, 0, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k11*H_2 + 2*k12*de;
             put(3, 0, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(5, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(6, 0);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(7, 0);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             put.zero(8, 0);
         }
         if (pick(NP, 0, 1, 1) == P) {
@@ -1474,11 +1474,11 @@ struct Net {
             jv = jv / mdensity;
             put(9, 0, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k10*H_1 + k19*H_m0;
             put(0, 1, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k10*H_1 - k18*de - k19*H_m0;
             put(1, 1, jv);
         }
@@ -1494,23 +1494,23 @@ struct Net {
             jv = -k19*H_m0;
             put(4, 1, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 1);
         }
         if (pick(NP, 0, 1, 2) == P) {
             put.zero(6, 1);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 1);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k18*de;
             put(8, 1, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             put.zero(9, 1);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k08*H_m0 + k10*H2_2 - k13*H2_1 + 2*k21*H2_1*H_1 + 3*k22*dg_ipow<2>(H_1);
             put(0, 2, jv);
         }
@@ -1518,19 +1518,19 @@ struct Net {
             jv = k09*H_2 - k10*H2_2;
             put(1, 2, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k01*de - k07*de - k08*H_m0 - k09*H_2 - k10*H2_2 + 2*k13*H2_1 + k15*H_m0 - 4*k21*H2_1*H_1 - 6*k22*dg_ipow<2>(H_1);
             put(2, 2, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k01*de - k09*H_2 + k10*H2_2;
             put(3, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k07*de - k08*H_m0 - k15*H_m0;
             put(4, 2, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             put.zero(5, 2);
         }
         if (pick(NP, 0, 0, 2) == P) {
@@ -1539,7 +1539,7 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(7, 2);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = k01*de - k07*de + k08*H_m0 + k15*H_m0;
             put(8, 2, jv);
         }
@@ -1548,11 +1548,11 @@ struct Net {
             jv = jv / mdensity;
             put(9, 2, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k11*H2_1;
             put(0, 3, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k09*H_1 + k11*H2_1 + k17*H_m0;
             put(1, 3, jv);
         }
@@ -1560,11 +1560,11 @@ struct Net {
             jv = k02*de - k09*H_1 + k11*H2_1 + 2*k16*H_m0;
             put(2, 3, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k02*de - k09*H_1 - k11*H2_1 - k16*H_m0 - k17*H_m0;
             put(3, 3, jv);
         }
-        if (pick(NP, 0, 0, 0) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k16*H_m0 - k17*H_m0;
             put(4, 3, jv);
         }
@@ -1577,32 +1577,32 @@ struct Net {
         if (pick(NP, 0, 0, 2) == P) {
             put.zero(7, 3);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k02*de + k17*H_m0;
             put(8, 3, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = -H2_1*gloverabel08_gaHp*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - brem_brem*de - de*reHII_reHII;
             jv = jv / mdensity;
             put(9, 3, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k08*H_1 + k19*H2_2;
             put(0, 4, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k17*H_2 - k19*H2_2;
             put(1, 4, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -k08*H_1 + k14*de + k15*H_1 + 2*k16*H_2 + k19*H2_2;
             put(2, 4, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 1, 2) == P) {
             jv = -k16*H_2 - k17*H_2;
             put(3, 4, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k08*H_1 - k14*de - k15*H_1 - k16*H_2 - k17*H_2 - k19*H2_2;
             put(4, 4, jv);
         }
@@ -1615,7 +1615,7 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(7, 4);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k08*H_1 + k14*de + k15*H_1 + k17*H_2;
             put(8, 4, jv);
         }
@@ -1637,11 +1637,11 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(4, 5);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k03*de;
             put(5, 5, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = k03*de;
             put(6, 5, jv);
         }
@@ -1652,7 +1652,7 @@ struct Net {
             jv = k03*de;
             put(8, 5, jv);
         }
-        if (pick(NP, 0, 1, 3) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -H2_1*gloverabel08_gaHe*dg_ipow<2>(gloverabel08_gphdl)/(dg_ipow<2>(gloverabel08_gphdl/(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael) + 1.0f)*dg_ipow<2>(H2_1*gloverabel08_gaH2 + H_1*gloverabel08_gaHI + H_2*gloverabel08_gaHp + He_1*gloverabel08_gaHe + de*gloverabel08_gael)) - ciHeI_ciHeI*de;
             jv = jv / mdensity;
             put(9, 5, jv);
@@ -1672,23 +1672,23 @@ struct Net {
         if (pick(NP, 0, 1, 1) == P) {
             put.zero(4, 6);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = k04*de;
             put(5, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 0) == P) {
             jv = -k04*de - k05*de;
             put(6, 6, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k05*de;
             put(7, 6, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = -k04*de + k05*de;
             put(8, 6, jv);
         }
-        if (pick(NP, 0, 0, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -brem_brem*de - ceHeII_ceHeII*de - ceHeI_ceHeI*dg_ipow<2>(de) - ciHeII_ciHeII*de - ciHeIS_ciHeIS*dg_ipow<2>(de) - de*reHeII1_reHeII1 - de*reHeII2_reHeII2;
             jv = jv / mdensity;
             put(9, 6, jv);
@@ -1711,28 +1711,28 @@ struct Net {
         if (pick(NP, 0, 1, 3) == P) {
             put.zero(5, 7);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 3) == P) {
             jv = k06*de;
             put(6, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -k06*de;
             put(7, 7, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = -k06*de;
             put(8, 7, jv);
         }
-        if (pick(NP, 0, 0, 3) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = -4.0f*brem_brem*de - de*reHeIII_reHeIII;
             jv = jv / mdensity;
             put(9, 7, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 1, 0) == P) {
             jv = -k12*H2_1;
             put(0, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k18*H2_2;
             put(1, 8, jv);
         }
@@ -1744,23 +1744,23 @@ struct Net {
             jv = k01*H_1 - k02*H_2 + 2*k12*H2_1;
             put(3, 8, jv);
         }
-        if (pick(NP, 0, 1, 0) == P) {
+        if (pick(NP, 0, 0, 2) == P) {
             jv = k07*H_1 - k14*H_m0;
             put(4, 8, jv);
         }
-        if (pick(NP, 0, 0, 1) == P) {
+        if (pick(NP, 0, 0, 3) == P) {
             jv = -k03*He_1 + k04*He_2;
             put(5, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k03*He_1 - k04*He_2 - k05*He_2 + k06*He_3;
             put(6, 8, jv);
         }
-        if (pick(NP, 0, 1, 2) == P) {
+        if (pick(NP, 0, 1, 1) == P) {
             jv = k05*He_2 - k06*He_3;
             put(7, 8, jv);
         }
-        if (pick(NP, 0, 1, 1) == P) {
+        if (pick(NP, 0, 0, 1) == P) {
             jv = k01*H_1 - k02*H_2 + k03*He_1 - k04*He_2 + k05*He_2 - k06*He_3 - k07*H_1 + k14*H_m0 - k18*H2_2;
             put(8, 8, jv);
         }
