@@ -4,19 +4,27 @@
  *
  * The split engine (dg_split.cuh) gives each lane its own cell, which is
  * what a full GPU wants; but after the first launches of a step only a few
- * stiff cells are left, each needing 10^4-10^5 more sequential Newton
- * sweeps, one per SM at most, and then a lone cell's sweep runs its
+ * hundred stiff cells are left, each needing 10^4-10^5 more sequential
+ * Newton sweeps, and a lone cell's sweep in the split engine runs its
  * elimination one row and one column after another on the 64-cycle FP64
  * issue of its warps' sub-partitions (measured with an instrumented copy: of
  * ~124k cycles per sweep, 44k in the LU row updates, 20k in the back
- * substitution).  Here the cell's lanes share the work instead: the table
- * interpolation, the residual, the Jacobian's scaling, each elimination
- * step's multipliers and its (row, column) updates, the x update and the
- * Newton update run one entry per lane, so each such FP64 warp instruction
- * does up to 128 of the cell's operations.  The RHS rows and Jacobian
- * entries are the same four generated parts as in the split engine (lane 0
- * of warp w computes part w), the pivot search, the back substitution, the
- * temperature and the substep control run on thread 0.
+ * substitution).  Here the cell's 128 lanes share each phase instead:
+ *   - temperature: the density and sum of n_i/(gamma-1) terms one per lane
+ *     (generated term lists), T with log T and the bin on thread 0, Tge on
+ *     warp 1;
+ *   - the table interpolation, the residual, the Jacobian's scaling and
+ *     the Newton update one entry per lane;
+ *   - RHS rows and Jacobian entries that are flat sums of products: one
+ *     term per lane from generated tables, then one sum per lane; the other
+ *     rows and entries as generated scalar code on up to three warps
+ *     meanwhile (networks without the tables: four scalar parts);
+ *   - FP64 elimination: column j belongs to warp j mod 4; the owner of
+ *     column k picks the pivot by a warp reduction and forms the
+ *     multipliers one row per lane, then after one barrier every warp
+ *     updates its own columns one entry per lane; rows stay in place
+ *     (a row order records the interchanges);
+ *   - back substitution on warp 0, lane i holding row i in registers.
  *
  * Mixed precision (the Newton matrix formed from FP64 products): the
  * equilibration exponents, the FP32 rounding and MixedSolve::factor's
@@ -29,11 +37,12 @@
  * Every value is computed with exactly the split engine's operations in the
  * same order (the scaling of a Jacobian entry, the skip tests of the
  * elimination, dg_div with the pivot's reciprocal, the FP32 pivots and
- * fused multiply-adds), so the results are bit-identical to it and, on the
- * FP64 path, to the reference.  The kernel serves the resume
- * launches of the stiff-cell redistribution when at most cfg.wide_max cells
- * were set aside (one per SM); otherwise it returns at once and the split
- * engine's launch does the work.
+ * fused multiply-adds, the printed expressions' products and sums), so the
+ * results are bit-identical to it and, on the FP64 path, to the reference.
+ * The kernel serves the resume launches of the stiff-cell redistribution
+ * when at most cfg.wide_max cells were set aside (wide_tail per SM), CTA b
+ * taking the b-th; otherwise it returns at once and the split engine's
+ * launch does the work.
  */
 #ifndef DG_WIDE_CUH
 #define DG_WIDE_CUH
@@ -42,8 +51,9 @@
 
 namespace dg {
 
-/* A barrier among the first n threads of warps [from, ...): the CTA's
- * named barrier id (bar.sync id, n); the host build supplies its own. */
+/* A barrier among n threads of the CTA (named barrier id: bar.sync id, n),
+ * called by every thread of the warps taking part; the host build supplies
+ * its own. */
 #if defined(__CUDA_ARCH__)
 __device__ __forceinline__ void dg_named_sync(int id, int n)
 {
