@@ -45,8 +45,8 @@ def _same(a, b):
 
 # (workload, cells, seed, picked cells, sweep budget); the picked config3
 # and top cells take 400-2200 sweeps with 4-35 rejected substeps each
-CASES = [("cold", 24, 23, None, 60),
-         ("config3", 64, 23, [4, 11, 15, 41, 43, 48], 40),
+CASES = [("cold", 24, 23, [0, 2, 5, 9, 13, 17], 60),
+         ("config3", 64, 23, [4, 11, 41], 40),
          ("top", 64, 23, [11, 14, 47], 40)]
 
 
@@ -92,7 +92,7 @@ def test_wide_conservation_resolve_equals_split(libs, tables):
     resumed on the wide engine, both the first solve and the re-solve equal
     the split engine's."""
     from dengo_gb300.workloads import primordial_cells
-    st, dtf = primordial_cells(8, "cold", seed=41)
+    st, dtf = primordial_cells(4, "cold", seed=41)
     split = he.evolve_in_subprocess(libs["split"], tables, st, dtf, timeout=900, mixed=True,
                                     sweep_budget=40, cons_tol=-1.0)
     wide = he.evolve_in_subprocess(libs["wide"], tables, st, dtf, timeout=900, mixed=True,
@@ -120,10 +120,17 @@ def test_wide_resume_nonfinite_scale(libs, tables):
     _same(wide, split)
 
 
+@pytest.fixture(scope="module")
+def oxygen_libs(tmp_path_factory):
+    d = tmp_path_factory.mktemp("wide_oxygen")
+    return (he.compile_engine("oxygen", d, engine="split"),
+            he.compile_engine("oxygen", d, engine="wide"))
+
+
 @pytest.mark.parametrize("mixed", [0, 1])
-def test_wide_oxygen_equals_split(tmp_path_factory, mixed):
+def test_wide_oxygen_equals_split(oxygen_libs, mixed):
     """The 16-equation ion network, every RHS row and Jacobian entry from the
-    sum-of-products tables (no scalar parts): four of the golden input cells
+    sum-of-products tables (no scalar parts): two of the golden input cells
     set aside after 20 sweeps and resumed on the wide engine equal the split
     engine's, FP64 and mixed."""
     from dengo_gb300.build import network_dir
@@ -131,10 +138,8 @@ def test_wide_oxygen_equals_split(tmp_path_factory, mixed):
     g = dict(np.load(os.path.join(ROOT, "tests", "golden", "oxygen_golden.npz")))
     t = read_table_file(os.path.join(network_dir("oxygen"), "oxygen_tables.dgt"))
     tabs = [np.ascontiguousarray(t[k]) for k in g["table_order"]]
-    d = tmp_path_factory.mktemp("wide_oxygen")
-    split_so = he.compile_engine("oxygen", d, engine="split")
-    wide_so = he.compile_engine("oxygen", d, engine="wide")
-    st, dtf = g["evolve_in"][:4], np.asarray(g["evolve_dtf"])[:4]
+    split_so, wide_so = oxygen_libs
+    st, dtf = g["evolve_in"][:2], np.asarray(g["evolve_dtf"])[:2]
     split = he.evolve_in_subprocess(split_so, tabs, st, dtf, timeout=900, sweep_budget=20,
                                     mixed=mixed)
     wide = he.evolve_in_subprocess(wide_so, tabs, st, dtf, timeout=900, sweep_budget=20,
