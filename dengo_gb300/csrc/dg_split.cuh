@@ -91,12 +91,13 @@ evolve_split_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *q
     constexpr int N = Net::N;
     extern __shared__ double dg_smem[];
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    /* The per-cell serial phases go to different warps -- each warp of a
-     * CTA runs on its own SM sub-partition, so with several CTAs per SM no
-     * sub-partition's FP64 unit carries all of them: the control (warp 0),
-     * T(ge) and log T (W_T), the pivot search or the mixed path's FP32
-     * factorisation (W_PIV), the back substitution or the refinement's
-     * corrections (W_BS). */
+    /* The per-cell serial phases go to different warps, so that with
+     * several CTAs per SM they need not all queue on one sub-partition's
+     * FP64 unit: the control (warp 0), T(ge) and log T (W_T), the pivot
+     * search or the mixed path's FP32 factorisation (W_PIV), the back
+     * substitution or the refinement's corrections (W_BS).  (On the
+     * config-2 bench's first step, three CTAs per SM, the time did not
+     * change measurably: 15.37 s before, 15.46 s after.) */
     constexpr int W_T = 1 % NP, W_PIV = 2 % NP, W_BS = 3 % NP;
     double *cellbase = dg_smem + l;
     const Slots<32> J{cellbase + L::J * 32}, R{cellbase + L::R * 32}, Y{cellbase + L::Y * 32},
