@@ -146,3 +146,26 @@ def test_wide_oxygen_equals_split(oxygen_libs, mixed):
                                    mixed=mixed)
     assert wide["resumed"] > 0 and wide["resumed"] == split["resumed"]
     _same(wide, split)
+
+
+def test_wide_compton_equals_split(tmp_path_factory):
+    """The primordial network with Compton cooling, whose ge row reads the
+    cell's temperature and the call's redshift directly (scalar parts):
+    four cold cells at the golden set's highest redshift, set aside after 20
+    sweeps and resumed on the wide engine, equal the split engine's."""
+    from dengo_gb300.workloads import primordial_cells
+    from dengo_gb300.build import network_dir
+    from dengo_gb300.tablefile import read_table_file
+    name = "primordial_compton"
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", name + "_golden.npz")))
+    t = read_table_file(os.path.join(network_dir(name), name + "_tables.dgt"))
+    tabs = [np.ascontiguousarray(t[k]) for k in g["table_order"]]
+    d = tmp_path_factory.mktemp("wide_compton")
+    split_so = he.compile_engine(name, d, engine="split")
+    wide_so = he.compile_engine(name, d, engine="wide")
+    z = max(float(x) for x in g["redshifts"])
+    st, dtf = primordial_cells(4, "cold", seed=29)
+    split = he.evolve_in_subprocess(split_so, tabs, st, dtf, timeout=900, sweep_budget=20, z=z)
+    wide = he.evolve_in_subprocess(wide_so, tabs, st, dtf, timeout=900, sweep_budget=20, z=z)
+    assert wide["resumed"] > 0 and wide["resumed"] == split["resumed"]
+    _same(wide, split)
