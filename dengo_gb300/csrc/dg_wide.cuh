@@ -356,7 +356,7 @@ evolve_wide_kernel(CellIO io, TableSet ts, KernelCfg cfg, unsigned long long *qu
             /* ---- P2a: the species and their powers as operands; any
              *      negative value fails the RHS ---- */
             sop_operands(Y, s_okr);
-            if (Net::SOP_RE && tid == 96) SMD[0] = Net::mdensity_of(Y);
+            if (Net::SOP_RMD && tid == 96) SMD[0] = Net::mdensity_of(Y);
             __syncthreads();
             /* ---- P2b: warps [0, SOP_RK) the scalar rows, lane 0 each;
              *      the other warps every term, one per lane, then every

@@ -1632,6 +1632,8 @@ struct Net {
     static constexpr int SOP_NOPS = 75, SOP_ONE = 74, SOP_FMAX = 3;
     static constexpr int SOP_NPOW = 0, SOP_LIT0 = 74, SOP_NLIT = 0;
     static constexpr int SOP_RT = 124, SOP_RE = 16, SOP_RK = 0;
+    /* a tabled RHS row divides by mdensity (the ge row) */
+    static constexpr bool SOP_RMD = true;
     static constexpr int SOP_JT = 204, SOP_JE = 80, SOP_JK = 0;
     /* the scalar part of RHS row i, -1 for a tabled row */
     __host__ __device__ static constexpr int sop_rpart(int i)

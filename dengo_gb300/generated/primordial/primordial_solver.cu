@@ -978,6 +978,8 @@ struct Net {
     static constexpr int SOP_NOPS = 64, SOP_ONE = 63, SOP_FMAX = 4;
     static constexpr int SOP_NPOW = 4, SOP_LIT0 = 58, SOP_NLIT = 5;
     static constexpr int SOP_RT = 66, SOP_RE = 9, SOP_RK = 1;
+    /* a tabled RHS row divides by mdensity (the ge row) */
+    static constexpr bool SOP_RMD = false;
     static constexpr int SOP_JT = 137, SOP_JE = 49, SOP_JK = 3;
     /* the scalar part of RHS row i, -1 for a tabled row */
     __host__ __device__ static constexpr int sop_rpart(int i)
